@@ -1,0 +1,58 @@
+"""Convert the reference's own test fixtures into small .npz golden files.
+
+Run in a container where the reference tree is mounted (it reads it from
+/root/reference); the GPU machine never needs the reference, only the .npz files
+written here.  Sources:
+
+* sucemfem/ProblemConfigurations/tests/LHS_matrix.npy and RHS_vector.pickle
+  (test_EMDrivenProblem.py:64-82): InscribedTet, order 1, f=1e8 Hz, ABC,
+  point source at the origin with value [2,-1,3].
+* sucemfem/Sources/tests/fillament_source_test_data.pickle
+  (test_fillament_source.py:34-69): order-2 filament RHS contributions.
+* sucemfem/PostProcessing/tests/data/power_flux_reference_dofs_*.pickle
+  (generator power_flux_generate_dofs.py:33-102): order-2 driven solution.
+* sucemfem/PostProcessing/tests/data/reference_dofs-2-0.149896229-*.pickle
+  (generator ntff_generate_dofs.py:40-95): order-2 driven solution of a
+  point dipole on a shifted 5^3 cube.
+"""
+import os
+import pickle
+import sys
+
+import numpy as np
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def load_pickle(path):
+    with open(path, "rb") as f:
+        return pickle.load(f, encoding="latin1")
+
+
+def main():
+    pc = os.path.join(REF, "sucemfem/ProblemConfigurations/tests")
+    lhs = np.load(os.path.join(pc, "LHS_matrix.npy"))
+    rhs = np.asarray(load_pickle(os.path.join(pc, "RHS_vector.pickle")))
+    np.savez_compressed(os.path.join(OUT, "driven_inscribed_tet_o1.npz"),
+                        lhs=lhs, rhs=rhs, frequency=1e8,
+                        source_coord=np.array([0, 0, 0.]), source_value=np.array([2, -1, 3.]))
+    d = load_pickle(os.path.join(REF, "sucemfem/Sources/tests/fillament_source_test_data.pickle"))
+    np.savez_compressed(os.path.join(OUT, "fillament_source_o2.npz"),
+                        **{k: np.asarray(v) for k, v in d.items()})
+    dd = os.path.join(REF, "sucemfem/PostProcessing/tests/data")
+    d = load_pickle(os.path.join(dd, "power_flux_reference_dofs_f-1000000000.000000_o-2_s-0.074948_l-0.100000_h-0.166667.pickle"))
+    np.savez_compressed(os.path.join(OUT, "power_flux_solution_o2.npz"),
+                        x=d["x"], freq=d["freq"], order=d["order"], I=d["I"],
+                        source_endpoints=d["source_endpoints"],
+                        domain_size=0.25 * 299792458 / 1e9, max_edge_len=299792458 / 1e9 / 6,
+                        no_integration_points=100)
+    d = load_pickle(os.path.join(dd, "reference_dofs-2-0.149896229-0.0499654096667.pickle"))
+    np.savez_compressed(os.path.join(OUT, "ntff_solution_o2.npz"),
+                        x=d["x"], freq=d["freq"], order=d["order"],
+                        domain_size=d["domain_size"], max_edge_len=d["max_edge_len"],
+                        source_value=np.array([0, 0, 1.]) * 299792458 / 1e9 / 1000)
+
+
+if __name__ == "__main__":
+    main()
