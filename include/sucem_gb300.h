@@ -1,0 +1,157 @@
+/* libsucem_gb300 -- C-ABI of the GB300 N1curl system-matrix and solve path.
+ *
+ * The reference (cemagg/sucem-fem) is Python; its FFI for this path is the
+ * Python call into DOLFIN/FFC/scipy.  Each entry point below names the
+ * reference call it replaces.  Conventions:
+ *   - every function returns an int status: SUCEM_OK (0) or a negative
+ *     SUCEM_ERR_* code; sucem_last_error() gives the message (per thread);
+ *   - plain pointers and sizes only.  "device" pointers are CUDA device
+ *     addresses on the device the space was uploaded to; "host" pointers are
+ *     ordinary host memory; "stream" is a cudaStream_t (NULL = legacy stream);
+ *   - the caller owns every buffer it passes; the library owns what sits
+ *     behind a sucem_space handle and frees it in sucem_space_destroy;
+ *   - handles are not thread safe; use one per thread or serialise calls.
+ */
+#ifndef SUCEM_GB300_H
+#define SUCEM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SUCEM_ABI_VERSION 1
+
+#define SUCEM_OK 0
+#define SUCEM_ERR_ARG -1       /* bad argument (ValueError in the Python layer) */
+#define SUCEM_ERR_MEMORY -2    /* host or device allocation refused */
+#define SUCEM_ERR_CUDA -3      /* a CUDA call failed */
+#define SUCEM_ERR_STATE -4     /* call order (e.g. space not uploaded) */
+#define SUCEM_ERR_NOCONV -5    /* iterative solve did not converge */
+#define SUCEM_ERR_BREAKDOWN -6 /* Krylov breakdown / zero pivot / NaN */
+
+typedef struct sucem_space sucem_space;
+
+/* value dtypes of CSR arrays and vectors */
+#define SUCEM_F32 0
+#define SUCEM_F64 1
+#define SUCEM_C64 2  /* interleaved complex float */
+#define SUCEM_C128 3 /* interleaved complex double */
+
+int sucem_version(void);
+const char* sucem_last_error(void);
+
+/* Mesh + N1curl function space.  Replaces dolfin.FunctionSpace(mesh,
+ * "Nedelec 1st kind H(curl)", order) and the sparsity pass of
+ * dolfin.assemble (sucemfem/ProblemConfigurations/EMProblem.py:100-105,
+ * sucemfem/SystemMatrices.py:54).  coords: nv*3 doubles; cells: nt*4
+ * vertex ids (any vertex order; sorted internally as DOLFIN orders meshes);
+ * order 1 or 2.  Builds entities, the DOF map (DOLFIN numbering), the CSR
+ * pattern and the row-gather tables on the host. */
+int sucem_space_create(const double* coords, int64_t nv, const int64_t* cells, int64_t nt,
+                       int order, sucem_space** out);
+void sucem_space_destroy(sucem_space* sp);
+
+/* out[10] = {n_dofs (global_dimension, EMProblem.py:44-47), nnz, nv, nt,
+ *            n_edges, n_faces, n_exterior_facets, n_boundary_dofs,
+ *            longest_row, n_incidences} */
+int sucem_space_sizes(const sucem_space* sp, int64_t* out);
+
+#define SUCEM_COPY_INDPTR 0         /* int64[n+1] CSR row pointer */
+#define SUCEM_COPY_INDICES 1        /* int32[nnz] CSR columns (sorted per row) */
+#define SUCEM_COPY_CELL_DOFS 2      /* int32[nt*ndof] DOF map (dofmap().tabulate_dofs) */
+#define SUCEM_COPY_BOUNDARY_DOFS 3  /* int32[n_boundary_dofs] PEC DOFs (essential.py:86-99) */
+#define SUCEM_COPY_EDGES 4          /* int32[ne*2] */
+#define SUCEM_COPY_FACES 5          /* int32[nf*3] */
+#define SUCEM_COPY_CELLS 6          /* int32[nt*4] ordered cells */
+#define SUCEM_COPY_EXT_MASK 7       /* uint8[nt] exterior-facet bit mask */
+#define SUCEM_COPY_CELL_EDGES 8     /* int32[nt*6] cell -> edge ids (UFC local order) */
+#define SUCEM_COPY_CELL_FACES 9     /* int32[nt*4] cell -> face ids (= facet numbering) */
+int sucem_space_copy(const sucem_space* sp, int what, void* host_dst);
+
+/* Copies the space to CUDA device `device` (idempotent). */
+int sucem_space_upload(sucem_space* sp, int device);
+
+#define SUCEM_DEV_INDPTR 0          /* int32[n+1] */
+#define SUCEM_DEV_INDICES 1         /* int32[nnz] */
+#define SUCEM_DEV_CELL_DOFS 2       /* int32[nt*ndof] */
+#define SUCEM_DEV_BOUNDARY_DOFS 3   /* int32[n_boundary_dofs] */
+int sucem_space_device_ptr(const sucem_space* sp, int what, void** out);
+
+/* Assembly of the interior forms and the ABC form into CSR values on the
+ * space's pattern.  Replaces dolfin.assemble of
+ *   S   = dot(curl(v), curl(u))/mu_r*dx   (sucemfem/Forms.py:79-85)
+ *   M=T = eps_r*inner(v, u)*dx            (sucemfem/Forms.py:71-77)
+ *   S_0 = inner(cross(n,v), cross(n,u))*ds over every exterior facet
+ *         (sucemfem/BoundaryConditions/ABC.py:56-57)
+ * as called from SystemMatrices.calc_system_matrices
+ * (sucemfem/SystemMatrices.py:46-58).  real_bytes = 4 (float) or 8
+ * (double) selects the precision of the coefficients and outputs.
+ * eps_r, mu_r_inv: device arrays of nt values (NULL = 1, the material
+ * defaults of sucemfem/Materials.py:31).  S, T, B: device arrays of nnz
+ * values; any may be NULL to skip that matrix. */
+int sucem_assemble(const sucem_space* sp, int real_bytes, const void* eps_r,
+                   const void* mu_r_inv, void* S, void* T, void* B, void* stream);
+
+/* Fused driven-problem matrix A = S - k0^2 T + 1j*k0*B written as
+ * interleaved complex (complex64 for real_bytes 4, complex128 for 8) on the
+ * full cell pattern.  Replaces DrivenProblemABC.get_LHS_matrix
+ * (sucemfem/ProblemConfigurations/EMDrivenProblem.py:67-72) without the
+ * exact-zero compaction scipy's sparse arithmetic performs. */
+int sucem_assemble_helmholtz(const sucem_space* sp, int real_bytes, const void* eps_r,
+                             const void* mu_r_inv, double k0, void* A, void* stream);
+
+/* Same as sucem_assemble with host buffers: copies in, assembles, copies
+ * back (synchronous).  The end-to-end form of dolfin.assemble. */
+int sucem_assemble_host(const sucem_space* sp, int real_bytes, const void* eps_r_host,
+                        const void* mu_r_inv_host, void* S_host, void* T_host, void* B_host);
+
+/* Essential (PEC) rows: zero each listed row of a value array on the
+ * space's pattern and set its diagonal to 1, columns untouched.  Replaces
+ * dolfin.DirichletBC(...).apply(A) as called by
+ * EssentialBoundaryCondition.get_essential_application_func
+ * (sucemfem/BoundaryConditions/essential.py:65-81).  dtype F32 or F64;
+ * rows: device int32[nrows]. */
+int sucem_apply_essential(const sucem_space* sp, int dtype, void* vals, const int32_t* rows,
+                          int64_t nrows, void* stream);
+
+/* y = A x on the space's pattern (device arrays).  Replaces the matrix-vector
+ * products M*x of sucemfem/ProblemConfigurations/EMVectorWaveEigenproblem.py:86,98
+ * and A*x of calculate_residual (sucemfem/Utilities/LinalgSolvers.py:297-305). */
+int sucem_spmv(const sucem_space* sp, int dtype, const void* vals, const void* x, void* y,
+               void* stream);
+
+/* out = a*X + b*Y (+ j*c*Z when complex_out) elementwise over m values
+ * (device arrays, NULL operands skipped).  Replaces the sparse linear
+ * combinations S - sigma*M (EMVectorWaveEigenproblem.py:76) and
+ * S - k0**2*M + 1j*k0*S_0 (EMDrivenProblem.py:72) on a shared pattern. */
+int sucem_combine(int64_t m, int real_bytes, double a, const void* X, double b, const void* Y,
+                  double c, const void* Z, void* out, int complex_out, void* stream);
+
+/* Drop exact (complex) zeros from a complex CSR on the space's pattern, as
+ * scipy's sparse binary operators do for the result of get_LHS_matrix
+ * (EMDrivenProblem.py:72).  Two steps: count (writes out_indptr[n+1];
+ * work = device int32[n]) then fill (out_indices, out_vals sized
+ * out_indptr[n]). */
+int sucem_compact_count(const sucem_space* sp, int dtype, const void* vals, int32_t* out_indptr,
+                        int32_t* work, void* stream);
+int sucem_compact_fill(const sucem_space* sp, int dtype, const void* vals,
+                       const int32_t* out_indptr, int32_t* out_indices, void* out_vals,
+                       void* stream);
+
+/* Point current sources: locate each point (lowest-index cell whose closure
+ * contains it) and evaluate N_i(p) . value for the ndof basis functions of
+ * that cell.  Replaces calc_pointsource_contrib
+ * (sucemfem/Sources/point_source.py:49-94).  Device arrays: pts double
+ * [npts*3]; values complex128 [npts*3] (interleaved); cells_out int32
+ * [npts] (0x7f7f7f7f when the point is outside the mesh); contrib
+ * complex128 [npts*ndof]. */
+int sucem_point_sources(const sucem_space* sp, const double* pts, const double* values, int npts,
+                        int32_t* cells_out, double* contrib, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SUCEM_GB300_H */

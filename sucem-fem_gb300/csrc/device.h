@@ -1,0 +1,58 @@
+// Device-resident copies of a Space and the kernel launchers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "space.h"
+
+namespace sucem {
+
+struct DeviceSpace {
+  int device = 0;
+  int64_t nt = 0, nv = 0, n = 0, nnz = 0, n_ent = 0, ninc = 0;
+  int order = 1, nd = 6, dpe = 1, rec_bytes = 8, max_row = 0;
+  int4* cells = nullptr;          // nt
+  float4* xyz_hi = nullptr;       // nv (w unused)
+  float4* xyz_lo = nullptr;       // nv
+  double* xyz = nullptr;          // nv*3
+  uint8_t* ext_mask = nullptr;    // nt
+  int32_t* ent_ptr = nullptr;     // n_ent+1
+  int32_t* inc_cell = nullptr;    // ninc
+  uint8_t* inc_rec = nullptr;     // ninc*rec_bytes
+  int32_t* indptr = nullptr;      // n+1
+  int32_t* indices = nullptr;     // nnz
+  int32_t* cell_dofs = nullptr;   // nt*nd
+  int32_t* boundary_dofs = nullptr;
+  int64_t n_boundary = 0;
+  // reference tensors [6][nd][nd] (curl, mass) and [4][6][nd][nd] (face)
+  float* kc_f = nullptr;
+  float* km_f = nullptr;
+  float* kf_f = nullptr;
+  double* kc_d = nullptr;
+  double* km_d = nullptr;
+  double* kf_d = nullptr;
+};
+
+// Copies the host space to the current device.  Returns "" or an error.
+std::string upload_space(Space& s, int device);
+void free_device_space(DeviceSpace* d);
+
+// Row-gather assembly.  real_bytes = 4 (float) or 8 (double).
+//   mode 0: S, T, B written to separate real arrays (any may be null)
+//   mode 1: A = S - k0^2 T + j k0 B written as interleaved complex
+struct AssembleArgs {
+  int real_bytes = 8;
+  int mode = 0;
+  const void* eps_r = nullptr;     // per cell, Real; null = 1
+  const void* mu_r_inv = nullptr;  // per cell, Real; null = 1
+  void* S = nullptr;
+  void* T = nullptr;
+  void* B = nullptr;
+  void* A = nullptr;
+  double k0 = 0.0;
+};
+cudaError_t launch_assemble(const DeviceSpace& d, const AssembleArgs& a, cudaStream_t stream);
+
+}  // namespace sucem

@@ -1,0 +1,258 @@
+"""Generate ``n1curl_tables.h``: reference-element constants of the
+Nedelec first-kind H(curl) element of orders 1 and 2.
+
+The element is the one the reference requests with
+``dolfin.FunctionSpace(mesh, "Nedelec 1st kind H(curl)", order)``
+(sucemfem/ProblemConfigurations/EMProblem.py:36,104-105), i.e. FIAT's
+definition: UFC reference tetrahedron, space P_{k-1}^3 + x cross
+homogeneous P_{k-1}^3, dual basis of tangential point evaluations on the
+edges (interior lattice points of k+1 intervals, unnormalised tangent
+v1-v0) and, for k=2, two tangential evaluations per face at the centroid
+(tangents v1-v0, v2-v0 of the face).
+
+Everything is computed in exact rational arithmetic (``fractions``) with no
+third-party package, so the same script runs on any host.  Written tables
+(all ``double``; the kernels convert to float where needed), with the six
+unique entries of a symmetric 3x3 metric ordered (00,11,22,01,02,12) and
+off-diagonal weights symmetrised (K_pq + K_qp):
+
+* ``KC<o>[6][n][n]``     int_ref curl N_a,p curl N_b,q
+* ``KM<o>[6][n][n]``     int_ref N_a,p N_b,q
+* ``KF<o>[4][6][n][n]``  int over reference face f (parameter measure ds dt)
+* ``NB<o>[n][3][10]``    monomial coefficients of N_a,p in
+                         1,x,y,z,x^2,y^2,z^2,xy,xz,yz (point sources)
+"""
+from fractions import Fraction as F
+from math import factorial
+import os
+import sys
+
+VERTS = [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1)]
+EDGES = [(2, 3), (1, 3), (1, 2), (0, 3), (0, 2), (0, 1)]
+FACES = [(1, 2, 3), (0, 2, 3), (0, 1, 3), (0, 1, 2)]
+SYM = [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
+MONO10 = [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (2, 0, 0), (0, 2, 0),
+          (0, 0, 2), (1, 1, 0), (1, 0, 1), (0, 1, 1)]
+
+
+# ---- sparse polynomials: dict {exponent tuple: Fraction} -------------------
+def padd(a, b, s=1):
+    out = dict(a)
+    for k, v in b.items():
+        out[k] = out.get(k, 0) + s * v
+    return {k: v for k, v in out.items() if v != 0}
+
+
+def pmul(a, b):
+    out = {}
+    for ka, va in a.items():
+        for kb, vb in b.items():
+            k = tuple(x + y for x, y in zip(ka, kb))
+            out[k] = out.get(k, 0) + va * vb
+    return {k: v for k, v in out.items() if v != 0}
+
+
+def pscale(a, s):
+    return {k: v * s for k, v in a.items() if v * s != 0}
+
+
+def pdiff(a, d):
+    out = {}
+    for k, v in a.items():
+        if k[d] > 0:
+            kk = list(k)
+            kk[d] -= 1
+            out[tuple(kk)] = out.get(tuple(kk), 0) + v * k[d]
+    return out
+
+
+def peval(a, pt):
+    tot = F(0)
+    for k, v in a.items():
+        term = v
+        for e, x in zip(k, pt):
+            term *= F(x) ** e
+        tot += term
+    return tot
+
+
+def mono(e):
+    return {tuple(e): F(1)}
+
+
+def int_tet(a):
+    return sum(v * F(factorial(k[0]) * factorial(k[1]) * factorial(k[2]),
+                     factorial(k[0] + k[1] + k[2] + 3)) for k, v in a.items())
+
+
+def int_face(a, f):
+    """Integral over reference face f in the parameter measure ds dt."""
+    va, vb, vc = (VERTS[i] for i in FACES[f])
+    # each coordinate as an affine polynomial in (s, t)
+    coord = []
+    for d in range(3):
+        c = {}
+        if va[d]:
+            c[(0, 0)] = F(va[d])
+        if vb[d] - va[d]:
+            c[(1, 0)] = F(vb[d] - va[d])
+        if vc[d] - va[d]:
+            c[(0, 1)] = F(vc[d] - va[d])
+        coord.append(c)
+    tot = {}
+    for k, v in a.items():
+        term = {(0, 0): v}
+        for d in range(3):
+            for _ in range(k[d]):
+                term = pmul(term, coord[d])
+        tot = padd(tot, term)
+    return sum(v * F(factorial(k[0]) * factorial(k[1]), factorial(k[0] + k[1] + 2))
+               for k, v in tot.items())
+
+
+# ---- element ---------------------------------------------------------------
+def span(order):
+    k = order
+    vecs = []
+    full = [(a, b, c) for a in range(k) for b in range(k) for c in range(k) if a + b + c <= k - 1]
+    for m in full:
+        for d in range(3):
+            v = [{}, {}, {}]
+            v[d] = mono(m)
+            vecs.append(v)
+    homog = [(a, b, c) for a in range(k) for b in range(k) for c in range(k) if a + b + c == k - 1]
+    X = [mono((1, 0, 0)), mono((0, 1, 0)), mono((0, 0, 1))]
+    for m in homog:
+        for d in range(3):
+            q = [{}, {}, {}]
+            q[d] = mono(m)
+            # x cross q
+            vecs.append([padd(pmul(X[1], q[2]), pmul(X[2], q[1]), -1),
+                         padd(pmul(X[2], q[0]), pmul(X[0], q[2]), -1),
+                         padd(pmul(X[0], q[1]), pmul(X[1], q[0]), -1)])
+    return vecs
+
+
+def dofs(order):
+    n = order + 1
+    out = []
+    for a, b in EDGES:
+        t = [VERTS[b][d] - VERTS[a][d] for d in range(3)]
+        for i in range(1, n):
+            out.append(([VERTS[a][d] + F(i, n) * t[d] for d in range(3)], t))
+    if order == 2:
+        for a, b, c in FACES:
+            t0 = [VERTS[b][d] - VERTS[a][d] for d in range(3)]
+            t1 = [VERTS[c][d] - VERTS[a][d] for d in range(3)]
+            p = [VERTS[a][d] + F(1, 3) * t0[d] + F(1, 3) * t1[d] for d in range(3)]
+            out.append((p, t0))
+            out.append((p, t1))
+    return out
+
+
+def solve(A, B):
+    """Exact Gauss-Jordan: solve A X = B (lists of Fractions)."""
+    n = len(A)
+    M = [list(A[i]) + list(B[i]) for i in range(n)]
+    for c in range(n):
+        p = next(r for r in range(c, n) if M[r][c] != 0)
+        M[c], M[p] = M[p], M[c]
+        piv = M[c][c]
+        M[c] = [x / piv for x in M[c]]
+        for r in range(n):
+            if r != c and M[r][c] != 0:
+                f = M[r][c]
+                M[r] = [x - f * y for x, y in zip(M[r], M[c])]
+    return [row[n:] for row in M]
+
+
+def independent(vecs):
+    """Greedy independent subset of vector polynomials."""
+    keys = sorted({(d, k) for v in vecs for d in range(3) for k in v[d]})
+    basis_rows, chosen = [], []
+    for v in vecs:
+        row = [v[d].get(k, F(0)) for d, k in keys]
+        for piv_col, brow in basis_rows:
+            if row[piv_col] != 0:
+                f = row[piv_col] / brow[piv_col]
+                row = [x - f * y for x, y in zip(row, brow)]
+        nz = next((i for i, x in enumerate(row) if x != 0), None)
+        if nz is not None:
+            basis_rows.append((nz, row))
+            chosen.append(v)
+    return chosen
+
+
+def basis(order):
+    phis = independent(span(order))
+    L = dofs(order)
+    n = len(L)
+    assert len(phis) == n
+    D = [[sum(peval(phis[j][d], p) * t[d] for d in range(3)) for j in range(n)] for p, t in L]
+    # N_i = sum_j C[j][i] phi_j with D C = I
+    C = solve(D, [[F(int(i == j)) for j in range(n)] for i in range(n)])
+    out = []
+    for i in range(n):
+        v = [{}, {}, {}]
+        for j in range(n):
+            if C[j][i] != 0:
+                for d in range(3):
+                    v[d] = padd(v[d], pscale(phis[j][d], C[j][i]))
+        out.append(v)
+    return out
+
+
+def curl(v):
+    return [padd(pdiff(v[2], 1), pdiff(v[1], 2), -1),
+            padd(pdiff(v[0], 2), pdiff(v[2], 0), -1),
+            padd(pdiff(v[1], 0), pdiff(v[0], 1), -1)]
+
+
+def tables(order):
+    N = basis(order)
+    C = [curl(v) for v in N]
+    n = len(N)
+
+    def sym6(fn):
+        out = [[[F(0)] * n for _ in range(n)] for _ in range(6)]
+        for a in range(n):
+            for b in range(n):
+                for m, (p, q) in enumerate(SYM):
+                    val = fn(a, b, p, q)
+                    if p != q:
+                        val += fn(a, b, q, p)
+                    out[m][a][b] = val
+        return out
+
+    KC = sym6(lambda a, b, p, q: int_tet(pmul(C[a][p], C[b][q])))
+    KM = sym6(lambda a, b, p, q: int_tet(pmul(N[a][p], N[b][q])))
+    KF = [sym6(lambda a, b, p, q, f=f: int_face(pmul(N[a][p], N[b][q]), f)) for f in range(4)]
+    NB = [[[N[a][p].get(e, F(0)) for e in MONO10] for p in range(3)] for a in range(n)]
+    return KC, KM, KF, NB
+
+
+def _fmt(x, depth):
+    if isinstance(x, list):
+        inner = ",".join(_fmt(y, depth + 1) for y in x)
+        return "{" + inner + "}" + ("\n" if depth <= 1 else "")
+    return repr(float(x))
+
+
+def main(path):
+    lines = ["// Generated by gen_tables.py: N1curl reference-element constants.",
+             "// Do not edit; rerun the generator.", "#pragma once", ""]
+    for order in (1, 2):
+        KC, KM, KF, NB = tables(order)
+        n = len(NB)
+        lines.append("static const double KC%d[6][%d][%d] = %s;" % (order, n, n, _fmt(KC, 0)))
+        lines.append("static const double KM%d[6][%d][%d] = %s;" % (order, n, n, _fmt(KM, 0)))
+        lines.append("static const double KF%d[4][6][%d][%d] = %s;" % (order, n, n, _fmt(KF, 0)))
+        lines.append("static const double NB%d[%d][3][10] = %s;" % (order, n, _fmt(NB, 0)))
+        lines.append("")
+    with open(path, "w") as f:
+        f.write("\n".join(lines))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else
+         os.path.join(os.path.dirname(os.path.abspath(__file__)), "n1curl_tables.h"))

@@ -1,0 +1,328 @@
+// Sparse linear-algebra kernels on the space's CSR pattern: essential-row
+// treatment, SpMV (real / complex, single / double), linear combinations of
+// value arrays and exact-zero compaction.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/sucem_gb300.h"
+#include "device.h"
+#include "linalg.h"
+#include "handle.h"
+
+namespace sucem {
+
+int fail(const std::string& msg, int code);
+int cuda_fail(cudaError_t e, const char* where);
+
+namespace {
+
+// ---- essential rows: zero the row, unit diagonal (DirichletBC.apply) ----
+template <typename V>
+__global__ void ident_rows_kernel(const int32_t* __restrict__ indptr,
+                                  const int32_t* __restrict__ indices,
+                                  const int32_t* __restrict__ rows, int64_t nrows, V* vals) {
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= nrows) return;
+  const int r = rows[w];
+  const int a = indptr[r], b = indptr[r + 1];
+  for (int k = a + lane; k < b; k += 32) vals[k] = indices[k] == r ? V(1) : V(0);
+}
+
+template <typename R>
+struct C2;
+template <>
+struct C2<float> {
+  using T = float2;
+};
+template <>
+struct C2<double> {
+  using T = double2;
+};
+
+template <typename R>
+__device__ __forceinline__ typename C2<R>::T cmul(typename C2<R>::T a, typename C2<R>::T b) {
+  typename C2<R>::T z;
+  z.x = a.x * b.x - a.y * b.y;
+  z.y = a.x * b.y + a.y * b.x;
+  return z;
+}
+
+// ---- SpMV: y = A x, TPR lanes per row, shuffle reduction ----
+template <typename R, bool CPLX, int TPR>
+__global__ void spmv_kernel(int64_t n, const int32_t* __restrict__ indptr,
+                            const int32_t* __restrict__ indices, const void* __restrict__ vals_,
+                            const void* __restrict__ x_, void* __restrict__ y_) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t row = tid / TPR;
+  const int sub = threadIdx.x % TPR;
+  // no early return: every lane of the warp takes part in the shuffles
+  const bool valid = row < n;
+  const int a = valid ? __ldg(&indptr[row]) : 0, b = valid ? __ldg(&indptr[row + 1]) : 0;
+  if (!CPLX) {
+    const R* vals = (const R*)vals_;
+    const R* x = (const R*)x_;
+    R acc = 0;
+    for (int k = a + sub; k < b; k += TPR) acc += __ldg(&vals[k]) * __ldg(&x[__ldg(&indices[k])]);
+#pragma unroll
+    for (int o = TPR / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, TPR);
+    if (valid && sub == 0) ((R*)y_)[row] = acc;
+  } else {
+    using CT = typename C2<R>::T;
+    const CT* vals = (const CT*)vals_;
+    const CT* x = (const CT*)x_;
+    R ar = 0, ai = 0;
+    for (int k = a + sub; k < b; k += TPR) {
+      const CT v = vals[k];
+      const CT xv = x[__ldg(&indices[k])];
+      ar += v.x * xv.x - v.y * xv.y;
+      ai += v.x * xv.y + v.y * xv.x;
+    }
+#pragma unroll
+    for (int o = TPR / 2; o > 0; o >>= 1) {
+      ar += __shfl_down_sync(0xffffffffu, ar, o, TPR);
+      ai += __shfl_down_sync(0xffffffffu, ai, o, TPR);
+    }
+    if (valid && sub == 0) {
+      CT z;
+      z.x = ar;
+      z.y = ai;
+      ((CT*)y_)[row] = z;
+    }
+  }
+}
+
+template <typename R, bool CPLX>
+cudaError_t spmv_dispatch(int64_t n, int64_t nnz, const int32_t* indptr, const int32_t* indices,
+                          const void* vals, const void* x, void* y, cudaStream_t s) {
+  const double mean = n ? (double)nnz / (double)n : 0.0;
+  const int threads = 256;
+#define LAUNCH(TPR)                                                                     \
+  {                                                                                     \
+    int64_t blocks = (n * TPR + threads - 1) / threads;                                 \
+    spmv_kernel<R, CPLX, TPR><<<(unsigned)blocks, threads, 0, s>>>(n, indptr, indices, \
+                                                                    vals, x, y);        \
+    return cudaGetLastError();                                                          \
+  }
+  if (mean <= 12) LAUNCH(4);
+  if (mean <= 24) LAUNCH(8);
+  if (mean <= 56) LAUNCH(16);
+  LAUNCH(32);
+#undef LAUNCH
+}
+
+// ---- linear combination of value arrays ----
+// real out:    out = a*X + b*Y
+// complex out: out = (a*X + b*Y) + j*(c*Z)
+template <typename R>
+__global__ void combine_kernel(int64_t m, R a, const R* __restrict__ X, R b,
+                               const R* __restrict__ Y, R c, const R* __restrict__ Z, R* out,
+                               int cplx) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  R re = (X ? a * X[i] : R(0)) + (Y ? b * Y[i] : R(0));
+  if (cplx) {
+    out[2 * i] = re;
+    out[2 * i + 1] = Z ? c * Z[i] : R(0);
+  } else {
+    out[i] = re;
+  }
+}
+
+// ---- exact-zero compaction of a complex CSR (scipy binop semantics) ----
+template <typename R>
+__global__ void count_nonzero_kernel(int64_t n, const int32_t* __restrict__ indptr,
+                                     const R* __restrict__ vals, int32_t* __restrict__ counts) {
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= n) return;
+  const int a = indptr[w], b = indptr[w + 1];
+  int c = 0;
+  for (int k = a + lane; k < b; k += 32) c += (vals[2 * k] != R(0) || vals[2 * k + 1] != R(0));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if (lane == 0) counts[w] = c;
+}
+
+// single-block exclusive scan over n counts -> out_indptr[0..n]
+__global__ void scan_kernel(int64_t n, const int32_t* __restrict__ counts,
+                            int32_t* __restrict__ out_indptr) {
+  __shared__ int32_t part[1024];
+  const int t = threadIdx.x;
+  const int64_t chunk = (n + blockDim.x - 1) / blockDim.x;
+  const int64_t lo = t * chunk, hi = lo + chunk < n ? lo + chunk : n;
+  int32_t s = 0;
+  for (int64_t i = lo; i < hi; ++i) s += counts[i];
+  part[t] = s;
+  __syncthreads();
+  if (t == 0) {
+    int32_t run = 0;
+    for (int i = 0; i < (int)blockDim.x; ++i) {
+      int32_t v = part[i];
+      part[i] = run;
+      run += v;
+    }
+    out_indptr[n] = run;
+  }
+  __syncthreads();
+  int32_t run = part[t];
+  for (int64_t i = lo; i < hi; ++i) {
+    out_indptr[i] = run;
+    run += counts[i];
+  }
+}
+
+template <typename R>
+__global__ void compact_kernel(int64_t n, const int32_t* __restrict__ indptr,
+                               const int32_t* __restrict__ indices, const R* __restrict__ vals,
+                               const int32_t* __restrict__ out_indptr, int32_t* out_indices,
+                               R* out_vals) {
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= n) return;
+  const int a = indptr[w], b = indptr[w + 1];
+  int base = out_indptr[w];
+  for (int k0 = a; k0 < b; k0 += 32) {
+    const int k = k0 + lane;
+    const bool keep = k < b && (vals[2 * k] != R(0) || vals[2 * k + 1] != R(0));
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (keep) {
+      const int pos = base + __popc(m & ((1u << lane) - 1u));
+      out_indices[pos] = indices[k];
+      out_vals[2 * pos] = vals[2 * k];
+      out_vals[2 * pos + 1] = vals[2 * k + 1];
+    }
+    base += __popc(m);
+  }
+}
+
+}  // namespace
+
+cudaError_t spmv(const DeviceSpace& d, int dtype, const void* vals, const void* x, void* y,
+                 cudaStream_t s) {
+  return spmv_raw(d.n, d.nnz, d.indptr, d.indices, dtype, vals, x, y, s);
+}
+
+cudaError_t spmv_raw(int64_t n, int64_t nnz, const int32_t* indptr, const int32_t* indices,
+                     int dtype, const void* vals, const void* x, void* y, cudaStream_t s) {
+  switch (dtype) {
+    case SUCEM_F32: return spmv_dispatch<float, false>(n, nnz, indptr, indices, vals, x, y, s);
+    case SUCEM_F64: return spmv_dispatch<double, false>(n, nnz, indptr, indices, vals, x, y, s);
+    case SUCEM_C64: return spmv_dispatch<float, true>(n, nnz, indptr, indices, vals, x, y, s);
+    case SUCEM_C128: return spmv_dispatch<double, true>(n, nnz, indptr, indices, vals, x, y, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace sucem
+
+using sucem::fail;
+using sucem::cuda_fail;
+
+static const sucem::DeviceSpace* dev_of(const sucem_space* sp) {
+  return sp ? sp->s.dev : nullptr;
+}
+
+extern "C" {
+
+int sucem_apply_essential(const sucem_space* sp, int dtype, void* vals, const int32_t* rows,
+                          int64_t nrows, void* stream) {
+  const sucem::DeviceSpace* d = dev_of(sp);
+  if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  if (nrows == 0) return SUCEM_OK;
+  if (!vals || !rows) return fail("null argument", SUCEM_ERR_ARG);
+  const int threads = 256;
+  const unsigned blocks = (unsigned)((nrows * 32 + threads - 1) / threads);
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (dtype) {
+    case SUCEM_F32:
+      sucem::ident_rows_kernel<float><<<blocks, threads, 0, s>>>(d->indptr, d->indices, rows, nrows,
+                                                                 (float*)vals);
+      break;
+    case SUCEM_F64:
+      sucem::ident_rows_kernel<double><<<blocks, threads, 0, s>>>(d->indptr, d->indices, rows,
+                                                                  nrows, (double*)vals);
+      break;
+    default: return fail("essential rows: dtype must be F32 or F64", SUCEM_ERR_ARG);
+  }
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_apply_essential");
+}
+
+int sucem_spmv(const sucem_space* sp, int dtype, const void* vals, const void* x, void* y,
+               void* stream) {
+  const sucem::DeviceSpace* d = dev_of(sp);
+  if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  if (!vals || !x || !y) return fail("null argument", SUCEM_ERR_ARG);
+  cudaError_t e = sucem::spmv(*d, dtype, vals, x, y, (cudaStream_t)stream);
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_spmv");
+}
+
+int sucem_combine(int64_t m, int real_bytes, double a, const void* X, double b, const void* Y,
+                  double c, const void* Z, void* out, int complex_out, void* stream) {
+  if (!out) return fail("null output", SUCEM_ERR_ARG);
+  if (m == 0) return SUCEM_OK;
+  const int threads = 256;
+  const unsigned blocks = (unsigned)((m + threads - 1) / threads);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (real_bytes == 4)
+    sucem::combine_kernel<float><<<blocks, threads, 0, s>>>(m, (float)a, (const float*)X, (float)b,
+                                                            (const float*)Y, (float)c,
+                                                            (const float*)Z, (float*)out,
+                                                            complex_out);
+  else if (real_bytes == 8)
+    sucem::combine_kernel<double><<<blocks, threads, 0, s>>>(m, a, (const double*)X, b,
+                                                             (const double*)Y, c,
+                                                             (const double*)Z, (double*)out,
+                                                             complex_out);
+  else
+    return fail("real_bytes must be 4 or 8", SUCEM_ERR_ARG);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_combine");
+}
+
+int sucem_compact_count(const sucem_space* sp, int dtype, const void* vals, int32_t* out_indptr,
+                        int32_t* work, void* stream) {
+  const sucem::DeviceSpace* d = dev_of(sp);
+  if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  if (!vals || !out_indptr || !work) return fail("null argument", SUCEM_ERR_ARG);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int threads = 256;
+  const unsigned blocks = (unsigned)((d->n * 32 + threads - 1) / threads);
+  if (dtype == SUCEM_C64)
+    sucem::count_nonzero_kernel<float><<<blocks, threads, 0, s>>>(d->n, d->indptr,
+                                                                  (const float*)vals, work);
+  else if (dtype == SUCEM_C128)
+    sucem::count_nonzero_kernel<double><<<blocks, threads, 0, s>>>(d->n, d->indptr,
+                                                                   (const double*)vals, work);
+  else
+    return fail("compaction needs a complex dtype", SUCEM_ERR_ARG);
+  sucem::scan_kernel<<<1, 1024, 0, s>>>(d->n, work, out_indptr);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_compact_count");
+}
+
+int sucem_compact_fill(const sucem_space* sp, int dtype, const void* vals,
+                       const int32_t* out_indptr, int32_t* out_indices, void* out_vals,
+                       void* stream) {
+  const sucem::DeviceSpace* d = dev_of(sp);
+  if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int threads = 256;
+  const unsigned blocks = (unsigned)((d->n * 32 + threads - 1) / threads);
+  if (dtype == SUCEM_C64)
+    sucem::compact_kernel<float><<<blocks, threads, 0, s>>>(d->n, d->indptr, d->indices,
+                                                            (const float*)vals, out_indptr,
+                                                            out_indices, (float*)out_vals);
+  else if (dtype == SUCEM_C128)
+    sucem::compact_kernel<double><<<blocks, threads, 0, s>>>(d->n, d->indptr, d->indices,
+                                                             (const double*)vals, out_indptr,
+                                                             out_indices, (double*)out_vals);
+  else
+    return fail("compaction needs a complex dtype", SUCEM_ERR_ARG);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_compact_fill");
+}
+
+}  // extern "C"

@@ -1,0 +1,262 @@
+// Host builder for the N1curl function space (the part of DOLFIN that the
+// reference reaches through dolfin.FunctionSpace and dolfin.assemble's
+// sparsity pass: sucemfem/ProblemConfigurations/EMProblem.py:100-105,
+// sucemfem/SystemMatrices.py:54).
+//
+// Numbering rules (kept identical to DOLFIN so DOF numbers are bit-exact):
+//  * each cell's vertices are sorted by global index (mesh ordering);
+//  * edges and faces are numbered by first encounter while walking the cells
+//    in order and each cell's local entities in UFC order;
+//  * order 1: dof = edge; order 2: dofs 2e, 2e+1 per edge, then
+//    2E + 2f, 2E + 2f + 1 per face.
+// The CSR pattern is the union of all cell-pair couplings with sorted
+// columns (explicit zeros kept), i.e. DOLFIN's cell sparsity pattern.
+#include "space.h"
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace sucem {
+
+namespace {
+
+// First-encounter numbering of entities keyed by their smallest vertex.
+struct EntityTable {
+  // per smallest vertex: list of (other-vertex key, id)
+  std::vector<std::vector<std::pair<int64_t, int32_t>>> buckets;
+  int32_t count = 0;
+  explicit EntityTable(int64_t nv) : buckets(nv) {}
+  int32_t find_or_add(int32_t vmin, int64_t rest) {
+    auto& b = buckets[vmin];
+    for (auto& p : b)
+      if (p.first == rest) return p.second;
+    b.emplace_back(rest, count);
+    return count++;
+  }
+};
+
+}  // namespace
+
+std::string build_space(Space& s, const double* coords, int64_t nv, const int64_t* cells,
+                        int64_t nt, int order) {
+  if (order != 1 && order != 2) return "order must be 1 or 2";
+  if (nv <= 0 || nt <= 0) return "empty mesh";
+  if (nv >= (int64_t(1) << 31) || nt >= (int64_t(1) << 31)) return "mesh too large for int32 ids";
+  s.order = order;
+  s.ndof_cell = order == 1 ? 6 : 20;
+  s.dofs_per_entity = order == 1 ? 1 : 2;
+  s.rec_bytes = order == 1 ? 8 : 24;
+  s.nv = nv;
+  s.nt = nt;
+  s.coords.assign(coords, coords + nv * 3);
+  s.cells.resize(nt * 4);
+  for (int64_t c = 0; c < nt; ++c) {
+    int64_t v[4];
+    for (int k = 0; k < 4; ++k) {
+      v[k] = cells[c * 4 + k];
+      if (v[k] < 0 || v[k] >= nv) return "cell vertex index out of range";
+    }
+    std::sort(v, v + 4);
+    for (int k = 0; k < 3; ++k)
+      if (v[k] == v[k + 1]) return "degenerate cell (repeated vertex)";
+    for (int k = 0; k < 4; ++k) s.cells[c * 4 + k] = int32_t(v[k]);
+  }
+
+  // ---- entities (serial: the numbering is order dependent) ----
+  s.cell_edges.resize(nt * 6);
+  s.cell_faces.resize(nt * 4);
+  {
+    EntityTable et(nv);
+    for (int64_t c = 0; c < nt; ++c) {
+      const int32_t* v = &s.cells[c * 4];
+      for (int le = 0; le < 6; ++le) {
+        int32_t a = v[kEdgeVerts[le][0]], b = v[kEdgeVerts[le][1]];
+        s.cell_edges[c * 6 + le] = et.find_or_add(a, b);
+      }
+    }
+    s.ne = et.count;
+    s.edges.resize(s.ne * 2);
+    for (int64_t vm = 0; vm < nv; ++vm)
+      for (auto& p : et.buckets[vm]) {
+        s.edges[p.second * 2] = int32_t(vm);
+        s.edges[p.second * 2 + 1] = int32_t(p.first);
+      }
+  }
+  {
+    EntityTable ft(nv);
+    for (int64_t c = 0; c < nt; ++c) {
+      const int32_t* v = &s.cells[c * 4];
+      for (int lf = 0; lf < 4; ++lf) {
+        int32_t a = v[kFaceVerts[lf][0]], b = v[kFaceVerts[lf][1]], d = v[kFaceVerts[lf][2]];
+        s.cell_faces[c * 4 + lf] = ft.find_or_add(a, int64_t(b) * nv + d);
+      }
+    }
+    s.nf = ft.count;
+    s.faces.resize(s.nf * 3);
+    for (int64_t vm = 0; vm < nv; ++vm)
+      for (auto& p : ft.buckets[vm]) {
+        s.faces[p.second * 3] = int32_t(vm);
+        s.faces[p.second * 3 + 1] = int32_t(p.first / nv);
+        s.faces[p.second * 3 + 2] = int32_t(p.first % nv);
+      }
+  }
+
+  // ---- exterior facets ----
+  std::vector<int32_t> face_count(s.nf, 0);
+  for (int64_t i = 0; i < nt * 4; ++i) face_count[s.cell_faces[i]]++;
+  s.ext_mask.assign(nt, 0);
+  s.n_ext_facets = 0;
+  for (int64_t c = 0; c < nt; ++c)
+    for (int lf = 0; lf < 4; ++lf)
+      if (face_count[s.cell_faces[c * 4 + lf]] == 1) {
+        s.ext_mask[c] |= uint8_t(1u << lf);
+        s.n_ext_facets++;
+      }
+
+  // ---- DOF map ----
+  const int nd = s.ndof_cell;
+  s.n = order == 1 ? s.ne : 2 * s.ne + 2 * s.nf;
+  if (s.n >= (int64_t(1) << 31)) return "too many DOFs for int32 indices";
+  s.cell_dofs.resize(nt * nd);
+  for (int64_t c = 0; c < nt; ++c) {
+    int32_t* d = &s.cell_dofs[c * nd];
+    if (order == 1) {
+      for (int le = 0; le < 6; ++le) d[le] = s.cell_edges[c * 6 + le];
+    } else {
+      for (int le = 0; le < 6; ++le) {
+        d[2 * le] = 2 * s.cell_edges[c * 6 + le];
+        d[2 * le + 1] = 2 * s.cell_edges[c * 6 + le] + 1;
+      }
+      for (int lf = 0; lf < 4; ++lf) {
+        d[12 + 2 * lf] = int32_t(2 * s.ne + 2 * s.cell_faces[c * 4 + lf]);
+        d[13 + 2 * lf] = int32_t(2 * s.ne + 2 * s.cell_faces[c * 4 + lf] + 1);
+      }
+    }
+  }
+
+  // ---- entity -> incident cells (in cell order) ----
+  s.n_ent = order == 1 ? s.ne : s.ne + s.nf;
+  s.ent_ptr.assign(s.n_ent + 1, 0);
+  for (int64_t c = 0; c < nt; ++c) {
+    for (int le = 0; le < 6; ++le) s.ent_ptr[s.cell_edges[c * 6 + le] + 1]++;
+    if (order == 2)
+      for (int lf = 0; lf < 4; ++lf) s.ent_ptr[s.ne + s.cell_faces[c * 4 + lf] + 1]++;
+  }
+  for (int64_t k = 0; k < s.n_ent; ++k) s.ent_ptr[k + 1] += s.ent_ptr[k];
+  const int64_t ninc = s.ent_ptr[s.n_ent];
+  s.inc_cell.resize(ninc);
+  std::vector<uint8_t> inc_local(ninc);
+  {
+    std::vector<int32_t> fill(s.ent_ptr.begin(), s.ent_ptr.end() - 1);
+    for (int64_t c = 0; c < nt; ++c) {
+      for (int le = 0; le < 6; ++le) {
+        int32_t k = s.cell_edges[c * 6 + le];
+        int32_t pos = fill[k]++;
+        s.inc_cell[pos] = int32_t(c);
+        inc_local[pos] = uint8_t(le);
+      }
+      if (order == 2)
+        for (int lf = 0; lf < 4; ++lf) {
+          int64_t k = s.ne + s.cell_faces[c * 4 + lf];
+          int32_t pos = fill[k]++;
+          s.inc_cell[pos] = int32_t(c);
+          inc_local[pos] = uint8_t(6 + lf);
+        }
+    }
+  }
+
+  // ---- pattern: column list per entity (shared by its rows) ----
+  const int dpe = s.dofs_per_entity;
+  std::vector<int64_t> ent_len(s.n_ent, 0);
+  std::vector<int64_t> ent_col_ptr(s.n_ent + 1, 0);
+  std::vector<int32_t> ent_cols;
+  {
+    // pass 1: lengths
+#pragma omp parallel
+    {
+      std::vector<int32_t> buf;
+#pragma omp for schedule(dynamic, 1024)
+      for (int64_t k = 0; k < s.n_ent; ++k) {
+        buf.clear();
+        for (int32_t i = s.ent_ptr[k]; i < s.ent_ptr[k + 1]; ++i) {
+          const int32_t* d = &s.cell_dofs[int64_t(s.inc_cell[i]) * nd];
+          buf.insert(buf.end(), d, d + nd);
+        }
+        std::sort(buf.begin(), buf.end());
+        ent_len[k] = std::unique(buf.begin(), buf.end()) - buf.begin();
+      }
+    }
+    for (int64_t k = 0; k < s.n_ent; ++k) ent_col_ptr[k + 1] = ent_col_ptr[k] + ent_len[k];
+    ent_cols.resize(ent_col_ptr[s.n_ent]);
+    int64_t maxlen = 0;
+    for (int64_t k = 0; k < s.n_ent; ++k) maxlen = std::max(maxlen, ent_len[k]);
+    if (maxlen > 255)
+      return "a CSR row has more than 255 columns (cell valence too high for the 8-bit slot tables)";
+    s.max_row = int(maxlen);
+    s.inc_rec.assign(ninc * s.rec_bytes, 0);
+    // pass 2: columns and slots
+#pragma omp parallel
+    {
+      std::vector<int32_t> buf;
+#pragma omp for schedule(dynamic, 1024)
+      for (int64_t k = 0; k < s.n_ent; ++k) {
+        buf.clear();
+        for (int32_t i = s.ent_ptr[k]; i < s.ent_ptr[k + 1]; ++i) {
+          const int32_t* d = &s.cell_dofs[int64_t(s.inc_cell[i]) * nd];
+          buf.insert(buf.end(), d, d + nd);
+        }
+        std::sort(buf.begin(), buf.end());
+        buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
+        std::copy(buf.begin(), buf.end(), ent_cols.begin() + ent_col_ptr[k]);
+        for (int32_t i = s.ent_ptr[k]; i < s.ent_ptr[k + 1]; ++i) {
+          uint8_t* rec = &s.inc_rec[int64_t(i) * s.rec_bytes];
+          rec[0] = inc_local[i];
+          const int32_t* d = &s.cell_dofs[int64_t(s.inc_cell[i]) * nd];
+          for (int b = 0; b < nd; ++b)
+            rec[1 + b] = uint8_t(std::lower_bound(buf.begin(), buf.end(), d[b]) - buf.begin());
+        }
+      }
+    }
+  }
+  // rows: entity k owns rows dpe*k .. dpe*k+dpe-1
+  s.indptr.assign(s.n + 1, 0);
+  for (int64_t k = 0; k < s.n_ent; ++k)
+    for (int j = 0; j < dpe; ++j) s.indptr[dpe * k + j + 1] = ent_len[k];
+  for (int64_t r = 0; r < s.n; ++r) s.indptr[r + 1] += s.indptr[r];
+  s.nnz = s.indptr[s.n];
+  if (s.nnz >= (int64_t(1) << 31)) return "pattern has 2^31 or more entries";
+  s.indices.resize(s.nnz);
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < s.n_ent; ++k)
+    for (int j = 0; j < dpe; ++j)
+      std::copy(ent_cols.begin() + ent_col_ptr[k], ent_cols.begin() + ent_col_ptr[k + 1],
+                s.indices.begin() + s.indptr[dpe * k + j]);
+
+  // ---- boundary DOFs (closure of the exterior facets) ----
+  {
+    std::vector<uint8_t> mark(s.n, 0);
+    for (int64_t c = 0; c < nt; ++c) {
+      if (!s.ext_mask[c]) continue;
+      for (int lf = 0; lf < 4; ++lf) {
+        if (!(s.ext_mask[c] >> lf & 1)) continue;
+        for (int le = 0; le < 6; ++le) {
+          if (kEdgeVerts[le][0] == lf || kEdgeVerts[le][1] == lf) continue;  // edge not on face lf
+          for (int j = 0; j < dpe; ++j) mark[s.cell_dofs[c * nd + dpe * le + j]] = 1;
+        }
+        if (order == 2)
+          for (int j = 0; j < dpe; ++j) mark[s.cell_dofs[c * nd + 12 + 2 * lf + j]] = 1;
+      }
+    }
+    s.boundary_dofs.clear();
+    for (int64_t r = 0; r < s.n; ++r)
+      if (mark[r]) s.boundary_dofs.push_back(int32_t(r));
+  }
+  return "";
+}
+
+}  // namespace sucem

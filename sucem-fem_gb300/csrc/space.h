@@ -1,0 +1,59 @@
+// Host-side function space: mesh entities, N1curl DOF map, CSR pattern and
+// the entity -> incident-cell tables the row-gather assembly kernels read.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace sucem {
+
+// UFC local numbering of a tetrahedron.
+static const int kEdgeVerts[6][2] = {{2, 3}, {1, 3}, {1, 2}, {0, 3}, {0, 2}, {0, 1}};
+static const int kFaceVerts[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+
+struct DeviceSpace;  // device copies, defined in the CUDA sources
+
+struct Space {
+  int order = 1;
+  int ndof_cell = 6;        // 6 (order 1) or 20 (order 2)
+  int dofs_per_entity = 1;  // 1 (order 1) or 2 (order 2)
+  int64_t nv = 0, nt = 0, ne = 0, nf = 0;
+  int64_t n = 0;            // global dimension
+  int64_t nnz = 0;
+  int max_row = 0;          // longest CSR row
+
+  std::vector<double> coords;          // nv*3
+  std::vector<int32_t> cells;          // nt*4, vertices sorted per cell
+  std::vector<int32_t> cell_edges;     // nt*6 (first-encounter numbering)
+  std::vector<int32_t> cell_faces;     // nt*4
+  std::vector<int32_t> edges;          // ne*2
+  std::vector<int32_t> faces;          // nf*3
+  std::vector<int32_t> cell_dofs;      // nt*ndof_cell
+  std::vector<uint8_t> ext_mask;       // nt: bit f set if local face f is exterior
+  int64_t n_ext_facets = 0;
+
+  // CSR pattern (rows sorted, columns sorted)
+  std::vector<int64_t> indptr;         // n+1
+  std::vector<int32_t> indices;        // nnz
+
+  // Row-gather tables.  Entities are the edges (order 1) or the edges
+  // followed by the faces (order 2); entity k owns dofs_per_entity
+  // consecutive rows that share one column list.
+  int64_t n_ent = 0;
+  std::vector<int32_t> ent_ptr;        // n_ent+1
+  std::vector<int32_t> inc_cell;       // per incidence: the cell
+  std::vector<uint8_t> inc_rec;        // per incidence: rec_bytes bytes:
+                                       //   [0] local entity index (0..5 edge, 6..9 face)
+                                       //   [1..ndof_cell] column slot of each local dof
+  int rec_bytes = 8;
+
+  std::vector<int32_t> boundary_dofs;  // closure of the exterior facets, sorted
+
+  DeviceSpace* dev = nullptr;
+};
+
+// Builds everything above; returns an empty string or an error message.
+std::string build_space(Space& s, const double* coords, int64_t nv, const int64_t* cells,
+                        int64_t nt, int order);
+
+}  // namespace sucem
