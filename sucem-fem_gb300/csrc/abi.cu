@@ -38,11 +38,11 @@ cudaError_t up(T** dst, const T* src, size_t count) {
 
 template <int ND>
 void flatten_tables(const double (&kc)[6][ND][ND], const double (&km)[6][ND][ND],
-                    const double (&kf)[4][6][ND][ND], std::vector<double>& c,
+                    const double (&kf)[4][3][ND][ND], std::vector<double>& c,
                     std::vector<double>& m, std::vector<double>& f) {
   c.assign(&kc[0][0][0], &kc[0][0][0] + 6 * ND * ND);
   m.assign(&km[0][0][0], &km[0][0][0] + 6 * ND * ND);
-  f.assign(&kf[0][0][0][0], &kf[0][0][0][0] + 4 * 6 * ND * ND);
+  f.assign(&kf[0][0][0][0], &kf[0][0][0][0] + 4 * 3 * ND * ND);
 }
 
 }  // namespace
@@ -54,8 +54,8 @@ void free_device_space(DeviceSpace* d) {
   cudaSetDevice(d->device);
   void* ptrs[] = {d->cells,   d->xyz_hi,  d->xyz_lo,    d->xyz,           d->ext_mask,
                   d->ent_ptr, d->inc_cell, d->inc_rec,  d->indptr,        d->indices,
-                  d->cell_dofs, d->boundary_dofs, d->kc_f, d->km_f, d->kf_f,
-                  d->kc_d,    d->km_d,    d->kf_d};
+                  d->cell_dofs, d->boundary_dofs, d->kc_f, d->km_f, d->kt_f,
+                  d->kc_d,    d->km_d,    d->kt_d};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   cudaSetDevice(prev);
@@ -98,9 +98,9 @@ std::string upload_space(Space& s, int device) {
   for (int64_t r = 0; r <= s.n; ++r) indptr32[r] = (int32_t)s.indptr[r];
   std::vector<double> kc, km, kf;
   if (s.order == 1)
-    flatten_tables<6>(KC1, KM1, KF1, kc, km, kf);
+    flatten_tables<6>(KC1, KM1, KT1, kc, km, kf);
   else
-    flatten_tables<20>(KC2, KM2, KF2, kc, km, kf);
+    flatten_tables<20>(KC2, KM2, KT2, kc, km, kf);
   std::vector<float> kcf(kc.begin(), kc.end()), kmf(km.begin(), km.end()),
       kff(kf.begin(), kf.end());
 #define UP(field, src, cnt)                                                            \
@@ -126,10 +126,10 @@ std::string upload_space(Space& s, int device) {
   UP(boundary_dofs, s.boundary_dofs.data(), s.boundary_dofs.size());
   UP(kc_f, kcf.data(), kcf.size());
   UP(km_f, kmf.data(), kmf.size());
-  UP(kf_f, kff.data(), kff.size());
+  UP(kt_f, kff.data(), kff.size());
   UP(kc_d, kc.data(), kc.size());
   UP(km_d, km.data(), km.size());
-  UP(kf_d, kf.data(), kf.size());
+  UP(kt_d, kf.data(), kf.size());
 #undef UP
   d->n_boundary = (int64_t)s.boundary_dofs.size();
   s.dev = d;

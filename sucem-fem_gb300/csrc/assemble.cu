@@ -14,8 +14,12 @@
 // Piola N = J^-T N_hat):
 //   T_e[a][b] = eps   |det J|    sum_pq (J^-1 J^-T)_pq KM[a][b][p][q]
 //   S_e[a][b] = 1/mu  / |det J|  sum_pq (J^T J)_pq    KC[a][b][p][q]
-//   B_e[a][b] = sum_{exterior f} |cross| sum_pq (J^-1 (I - n n^T) J^-T)_pq KF_f[a][b][p][q]
-// with the symmetric 3x3 metrics stored as their 6 unique entries.
+//   B_e[a][b] = sum_{exterior f} (|b|^2 KT_f0 - (a.b) KT_f1 + |a|^2 KT_f2)[a][b] / |a x b|
+// with the symmetric 3x3 metrics stored as their 6 unique entries, a, b the
+// physical edge vectors of face f and KT_f the tangential reference tensors
+// ((n x u).(n x v) = tangential part of u.v; the tangential projector of the
+// face pulled back by J^-1 is [a^ b^] G^-1 [a^ b^]^T with G the Gram matrix
+// of a, b, so no normal vector and no cancellation is needed).
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -110,10 +114,10 @@ __global__ void __launch_bounds__(kWarps * 32)
   Real* warp_base = sKM + KSZ;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int acc_len = DPE * NMAT * p.max_row;
-  const int per_warp = 32 * 12 + (WITH_B ? 32 * 24 : 0) + acc_len;
+  const int per_warp = 32 * 12 + (WITH_B ? 32 * 12 : 0) + acc_len;
   Real* gbuf = warp_base + warp * per_warp;   // [32][12]
-  Real* hbuf = gbuf + 32 * 12;                // [32][24] (WITH_B)
-  Real* acc = hbuf + (WITH_B ? 32 * 24 : 0);  // [DPE][NMAT][max_row]
+  Real* hbuf = gbuf + 32 * 12;                // [32][4 faces][3] (WITH_B)
+  Real* acc = hbuf + (WITH_B ? 32 * 12 : 0);  // [DPE][NMAT][max_row]
   __shared__ int masks[kWarps][32];
 
   for (int i = threadIdx.x; i < KSZ; i += blockDim.x) {
@@ -157,18 +161,18 @@ __global__ void __launch_bounds__(kWarps * 32)
         const Real sS = load_coef(mu_inv, c) / adet;
         const Real sT = load_coef(eps_r, c) * adet;
         Real* g = gbuf + lane * 12;
-        Real gt_raw[6];
 #pragma unroll
         for (int m = 0; m < 6; ++m) {
           const int pp = sym_p(m), qq = sym_q(m);
           g[m] = (J[0][pp] * J[0][qq] + J[1][pp] * J[1][qq] + J[2][pp] * J[2][qq]) * sS;
-          gt_raw[m] = Ji[pp][0] * Ji[qq][0] + Ji[pp][1] * Ji[qq][1] + Ji[pp][2] * Ji[qq][2];
-          g[6 + m] = gt_raw[m] * sT;
+          g[6 + m] = (Ji[pp][0] * Ji[qq][0] + Ji[pp][1] * Ji[qq][1] + Ji[pp][2] * Ji[qq][2]) * sT;
         }
         int mask = 0;
         if (WITH_B) {
+          // ABC block of exterior face f from its edge vectors a, b:
+          // (|b|^2 KT[f][0] - (a.b) KT[f][1] + |a|^2 KT[f][2]) / |a x b|
           mask = __ldg(&p.ext_mask[c]);
-          Real* h = hbuf + lane * 24;
+          Real* h = hbuf + lane * 12;
 #pragma unroll
           for (int f = 0; f < 4; ++f) {
             if (!(mask >> f & 1)) continue;
@@ -192,13 +196,10 @@ __global__ void __launch_bounds__(kWarps * 32)
             const Real cx = a[1] * b[2] - a[2] * b[1];
             const Real cy = a[2] * b[0] - a[0] * b[2];
             const Real cz = a[0] * b[1] - a[1] * b[0];
-            const Real ta = sqrt(cx * cx + cy * cy + cz * cz);
-            const Real nx = cx / ta, ny = cy / ta, nz = cz / ta;
-            Real w[3];
-#pragma unroll
-            for (int r = 0; r < 3; ++r) w[r] = Ji[r][0] * nx + Ji[r][1] * ny + Ji[r][2] * nz;
-#pragma unroll
-            for (int m = 0; m < 6; ++m) h[f * 6 + m] = ta * (gt_raw[m] - w[sym_p(m)] * w[sym_q(m)]);
+            const Real ita = Real(1) / sqrt(cx * cx + cy * cy + cz * cz);
+            h[f * 3 + 0] = (b[0] * b[0] + b[1] * b[1] + b[2] * b[2]) * ita;
+            h[f * 3 + 1] = -(a[0] * b[0] + a[1] * b[1] + a[2] * b[2]) * ita;
+            h[f * 3 + 2] = (a[0] * a[0] + a[1] * a[1] + a[2] * a[2]) * ita;
           }
         }
         masks[warp][lane] = mask;
@@ -225,14 +226,14 @@ __global__ void __launch_bounds__(kWarps * 32)
             ar[slot] += s;
             ar[p.max_row + slot] += t;
             if (WITH_B && mask) {
-              const Real* h = hbuf + k * 24;
+              const Real* h = hbuf + k * 12;
               Real bsum = 0;
 #pragma unroll
               for (int f = 0; f < 4; ++f) {
                 if (!(mask >> f & 1)) continue;
 #pragma unroll
-                for (int m = 0; m < 6; ++m)
-                  bsum += h[f * 6 + m] * __ldg(&kf[((f * 6 + m) * ND + a) * ND + lane]);
+                for (int m = 0; m < 3; ++m)
+                  bsum += h[f * 3 + m] * __ldg(&kf[((f * 3 + m) * ND + a) * ND + lane]);
               }
               ar[2 * p.max_row + slot] += bsum;
             }
@@ -285,7 +286,7 @@ cudaError_t launch_t(const DeviceSpace& d, const AssembleArgs& a, cudaStream_t s
   p.indptr = d.indptr;
   p.n_ent = d.n_ent;
   p.max_row = d.max_row;
-  const size_t per_warp = 32 * 12 + (WITH_B ? 32 * 24 : 0) + (size_t)DPE * NMAT * d.max_row;
+  const size_t per_warp = 32 * 12 + (WITH_B ? 32 * 12 : 0) + (size_t)DPE * NMAT * d.max_row;
   const size_t smem = sizeof(Real) * (2 * 6 * ND * ND + kWarps * per_warp);
   auto kern = assemble_rows_kernel<ORDER, Real, WITH_B, MODE>;
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -300,7 +301,7 @@ cudaError_t launch_t(const DeviceSpace& d, const AssembleArgs& a, cudaStream_t s
   if (grid < 1) grid = 1;
   const Real* kc = sizeof(Real) == 4 ? (const Real*)d.kc_f : (const Real*)d.kc_d;
   const Real* km = sizeof(Real) == 4 ? (const Real*)d.km_f : (const Real*)d.km_d;
-  const Real* kf = sizeof(Real) == 4 ? (const Real*)d.kf_f : (const Real*)d.kf_d;
+  const Real* kf = sizeof(Real) == 4 ? (const Real*)d.kt_f : (const Real*)d.kt_d;
   kern<<<(unsigned)grid, kWarps * 32, smem, stream>>>(
       p, (const Real*)a.eps_r, (const Real*)a.mu_r_inv, kc, km, kf, (Real*)a.S, (Real*)a.T,
       (Real*)a.B, (typename Cplx<Real>::T*)a.A, (Real)a.k0);

@@ -26,13 +26,13 @@ struct DeviceSpace {
   int32_t* cell_dofs = nullptr;   // nt*nd
   int32_t* boundary_dofs = nullptr;
   int64_t n_boundary = 0;
-  // reference tensors [6][nd][nd] (curl, mass) and [4][6][nd][nd] (face)
+  // reference tensors [6][nd][nd] (curl, mass), [4][3][nd][nd] (face tangential)
   float* kc_f = nullptr;
   float* km_f = nullptr;
-  float* kf_f = nullptr;
+  float* kt_f = nullptr;
   double* kc_d = nullptr;
   double* km_d = nullptr;
-  double* kf_d = nullptr;
+  double* kt_d = nullptr;
 };
 
 // Copies the host space to the current device.  Returns "" or an error.

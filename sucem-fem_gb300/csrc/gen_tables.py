@@ -18,7 +18,14 @@ off-diagonal weights symmetrised (K_pq + K_qp):
 
 * ``KC<o>[6][n][n]``     int_ref curl N_a,p curl N_b,q
 * ``KM<o>[6][n][n]``     int_ref N_a,p N_b,q
-* ``KF<o>[4][6][n][n]``  int over reference face f (parameter measure ds dt)
+* ``KT<o>[4][3][n][n]``  tangential face tensors of reference face f with
+                         edge vectors a = v1-v0, b = v2-v0 of the face:
+                         int (N_a.a)(N_b.a), int (N_a.a)(N_b.b)+(N_a.b)(N_b.a),
+                         int (N_a.b)(N_b.b) in the parameter measure ds dt.
+                         The physical ABC block of face f is then
+                         (|b|^2 KT[0] - (a.b) KT[1] + |a|^2 KT[2]) / |a x b|
+                         with a, b the physical face edge vectors (tangential
+                         components are exact, so off-face DOFs give exact 0).
 * ``NB<o>[n][3][10]``    monomial coefficients of N_a,p in
                          1,x,y,z,x^2,y^2,z^2,xy,xz,yz (point sources)
 """
@@ -226,9 +233,27 @@ def tables(order):
 
     KC = sym6(lambda a, b, p, q: int_tet(pmul(C[a][p], C[b][q])))
     KM = sym6(lambda a, b, p, q: int_tet(pmul(N[a][p], N[b][q])))
-    KF = [sym6(lambda a, b, p, q, f=f: int_face(pmul(N[a][p], N[b][q]), f)) for f in range(4)]
+    KT = []
+    for f in range(4):
+        va, vb, vc = (VERTS[i] for i in FACES[f])
+        ta = [vb[d] - va[d] for d in range(3)]
+        tb = [vc[d] - va[d] for d in range(3)]
+
+        def tang(a, t):
+            out = {}
+            for d in range(3):
+                if t[d]:
+                    out = padd(out, pscale(N[a][d], F(t[d])))
+            return out
+        Na = [tang(a, ta) for a in range(n)]
+        Nb = [tang(a, tb) for a in range(n)]
+        aa = [[int_face(pmul(Na[a], Na[b]), f) for b in range(n)] for a in range(n)]
+        ab = [[int_face(pmul(Na[a], Nb[b]), f) + int_face(pmul(Nb[a], Na[b]), f) for b in range(n)]
+              for a in range(n)]
+        bb = [[int_face(pmul(Nb[a], Nb[b]), f) for b in range(n)] for a in range(n)]
+        KT.append([aa, ab, bb])
     NB = [[[N[a][p].get(e, F(0)) for e in MONO10] for p in range(3)] for a in range(n)]
-    return KC, KM, KF, NB
+    return KC, KM, KT, NB
 
 
 def _fmt(x, depth):
@@ -242,11 +267,11 @@ def main(path):
     lines = ["// Generated by gen_tables.py: N1curl reference-element constants.",
              "// Do not edit; rerun the generator.", "#pragma once", ""]
     for order in (1, 2):
-        KC, KM, KF, NB = tables(order)
+        KC, KM, KT, NB = tables(order)
         n = len(NB)
         lines.append("static const double KC%d[6][%d][%d] = %s;" % (order, n, n, _fmt(KC, 0)))
         lines.append("static const double KM%d[6][%d][%d] = %s;" % (order, n, n, _fmt(KM, 0)))
-        lines.append("static const double KF%d[4][6][%d][%d] = %s;" % (order, n, n, _fmt(KF, 0)))
+        lines.append("static const double KT%d[4][3][%d][%d] = %s;" % (order, n, n, _fmt(KT, 0)))
         lines.append("static const double NB%d[%d][3][10] = %s;" % (order, n, _fmt(NB, 0)))
         lines.append("")
     with open(path, "w") as f:

@@ -1,7 +1,10 @@
 """GPU assembly parity against the FP64 oracle (through the C-ABI).
 
 Tolerances: per-entry error divided by the largest |entry| of its row
-(entries that cancel to ~0 have no meaningful relative error):
+(entries that cancel to ~0 have no meaningful relative error; rows whose
+entries are all round-off are scaled by 1e-6 of the matrix's largest entry
+instead; the ABC matrix B, whose mathematically-zero entries the oracle
+computes by cancellation of O(1) terms, is scaled by its largest entry):
   FP64 kernels  <= 1e-12
   FP32 kernels  <= 2e-6
 CSR pattern and DOF numbering are compared bit-exactly (CPU tests)."""
@@ -25,9 +28,10 @@ def _mesh(name):
     return fem.jitter_interior(coords, cells, 1 / 3, 0.2, seed=0), cells
 
 
-def _row_err(got, R):
+def _row_err(got, R, floor=1e-6):
     R = R.tocsr()
     rowmax = np.maximum.reduceat(np.abs(R.data), R.indptr[:-1])
+    rowmax = np.maximum(rowmax, floor * np.abs(R.data).max())
     scale = np.repeat(rowmax, np.diff(R.indptr))
     return np.max(np.abs(got - R.data) / scale)
 
@@ -61,7 +65,7 @@ def test_assembly_matches_oracle(rb, order, mesh):
     V = FunctionSpace(Mesh(coords, cells), order=order)
     got = _assemble(V, rb, eps, 1 / mu)
     for k, R in (("S", ref.S), ("T", ref.T), ("B", ref.B)):
-        assert _row_err(got[k], R) <= TOL[rb], k
+        assert _row_err(got[k], R, 1.0 if k == "B" else 1e-6) <= TOL[rb], k
 
 
 @pytest.mark.parametrize("rb", [8, 4])
