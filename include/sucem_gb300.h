@@ -41,6 +41,9 @@ typedef struct sucem_space sucem_space;
 
 int sucem_version(void);
 const char* sucem_last_error(void);
+/* Number of kernels the library has launched since it was loaded (all
+ * threads); used to report the kernel count of a timed region. */
+long long sucem_launch_count(void);
 
 /* Mesh + N1curl function space.  Replaces dolfin.FunctionSpace(mesh,
  * "Nedelec 1st kind H(curl)", order) and the sparsity pass of
@@ -68,6 +71,7 @@ int sucem_space_sizes(const sucem_space* sp, int64_t* out);
 #define SUCEM_COPY_EXT_MASK 7       /* uint8[nt] exterior-facet bit mask */
 #define SUCEM_COPY_CELL_EDGES 8     /* int32[nt*6] cell -> edge ids (UFC local order) */
 #define SUCEM_COPY_CELL_FACES 9     /* int32[nt*4] cell -> face ids (= facet numbering) */
+#define SUCEM_COPY_DOF_XYZ 10       /* double[n*3] DOF locations (edge midpoint / face centroid) */
 int sucem_space_copy(const sucem_space* sp, int what, void* host_dst);
 
 /* Copies the space to CUDA device `device` (idempotent). */
@@ -149,6 +153,57 @@ int sucem_compact_fill(const sucem_space* sp, int dtype, const void* vals,
  * complex128 [npts*ndof]. */
 int sucem_point_sources(const sucem_space* sp, const double* pts, const double* values, int npts,
                         int32_t* cells_out, double* contrib, void* stream);
+
+/* ---- vectors and general CSR (device arrays) ----
+ * The Krylov / refinement building blocks behind solve_sparse_system and the
+ * solver classes of sucemfem/Utilities/LinalgSolvers.py:239-322.
+ * spmv_csr: y = A x for any CSR with int32 indices.
+ * axpby: y = a*x + b*y, a and b complex (imaginary parts ignored for real
+ * dtypes; x may be NULL for y = b*y).
+ * dot: out[0..1] (device, double re/im) = sum conj(x)*y (conj=1) or x*y,
+ * accumulated in double in a fixed order; work = device scratch of
+ * sucem_vec_dot_work_bytes() bytes.
+ * convert: count reals between float and double arrays. */
+int sucem_spmv_csr(int64_t n, int64_t nnz, const int32_t* indptr, const int32_t* indices,
+                   int dtype, const void* vals, const void* x, void* y, void* stream);
+int sucem_vec_axpby(int64_t n, int dtype, double ar, double ai, const void* x, double br,
+                    double bi, void* y, void* stream);
+int64_t sucem_vec_dot_work_bytes(void);
+int sucem_vec_dot(int64_t n, int dtype, const void* x, const void* y, int conj, void* work,
+                  double* out, void* stream);
+int sucem_vec_convert(int64_t count, int dst_real_bytes, void* dst, int src_real_bytes,
+                      const void* src, void* stream);
+
+/* ---- multifrontal sparse LU (GPU) ----
+ * Replaces the reference's direct solves: dolfin.LUSolver(S - sigma*M)
+ * (sucemfem/ProblemConfigurations/EMVectorWaveEigenproblem.py:76-85),
+ * UMFPACKSolver / spsolve (sucemfem/Utilities/LinalgSolvers.py:262-277) and,
+ * used as a preconditioner, spilu (LinalgSolvers.py:118-121).
+ * analyse: host CSR pattern with symmetric structure (sorted columns) and
+ * n*3 DOF coordinates; builds a nested-dissection ordering and the front
+ * structure on the host.  factor: device values in CSR order (dtype
+ * SUCEM_F32/F64/C64/C128), no pivoting; pivots below pivot_tol*max|a_ij|
+ * are replaced (static pivoting, count via sucem_lu_perturbed).  solve:
+ * device b, x of n values in the factor's dtype or, for a single-precision
+ * factor, its double-precision twin (conversion on the fly). */
+typedef struct sucem_lu sucem_lu;
+int sucem_lu_analyse(int64_t n, const int32_t* indptr, const int32_t* indices, const double* xyz,
+                     int leaf_size, sucem_lu** out);
+/* Same analysis with the element-based nested dissection (preferred for FEM
+ * matrices): cell_dofs int32[nt*ndof_cell] (-1 for DOFs not in the matrix),
+ * cell_xyz double[nt*3] cell centroids.  Separators are interface surfaces
+ * between bisected cell sets. */
+int sucem_lu_analyse_cells(int64_t n, const int32_t* indptr, const int32_t* indices, int64_t nt,
+                           int ndof_cell, const int32_t* cell_dofs, const double* cell_xyz,
+                           int leaf_size, sucem_lu** out);
+void sucem_lu_destroy(sucem_lu* lu);
+/* out[7] = {n, nnz, tree nodes, tree levels, front arena entries, factor
+ *           multiply-adds, largest front} */
+int sucem_lu_info(const sucem_lu* lu, double* out);
+int sucem_lu_copy_perm(const sucem_lu* lu, int64_t* perm);
+int sucem_lu_factor(sucem_lu* lu, int dtype, const void* vals, double pivot_tol, void* stream);
+int sucem_lu_solve(sucem_lu* lu, int io_dtype, const void* b, void* x, void* stream);
+int sucem_lu_perturbed(sucem_lu* lu);
 
 #ifdef __cplusplus
 }

@@ -17,7 +17,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 
 CU = ["abi.cu", "assemble.cu", "linalg.cu"]
-CPP = ["space.cpp"]
+CPP = ["space.cpp", "mf_symbolic.cpp"]
 
 
 def _sources():

@@ -2,6 +2,7 @@
 // Declarations and the reference interfaces they replace: include/sucem_gb300.h.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -16,6 +17,8 @@
 
 namespace sucem {
 thread_local std::string g_last_error;
+static std::atomic<long long> g_launches{0};
+void count_launch(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
 int fail(const std::string& msg, int code) {
   g_last_error = msg;
@@ -55,7 +58,8 @@ void free_device_space(DeviceSpace* d) {
   void* ptrs[] = {d->cells,   d->xyz_hi,  d->xyz_lo,    d->xyz,           d->ext_mask,
                   d->ent_ptr, d->inc_cell, d->inc_rec,  d->indptr,        d->indices,
                   d->cell_dofs, d->boundary_dofs, d->kc_f, d->km_f, d->kt_f,
-                  d->kc_d,    d->km_d,    d->kt_d};
+                  d->kc_d,    d->km_d,    d->kt_d, d->bidx, d->g_f, d->g_d, d->h_f, d->h_d,
+                  d->kab_f, d->kab_d};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   cudaSetDevice(prev);
@@ -103,6 +107,18 @@ std::string upload_space(Space& s, int device) {
     flatten_tables<20>(KC2, KM2, KT2, kc, km, kf);
   std::vector<float> kcf(kc.begin(), kc.end()), kmf(km.begin(), km.end()),
       kff(kf.begin(), kf.end());
+  const int nd = s.ndof_cell;
+  std::vector<double> kab((size_t)nd * nd * 12);
+  for (int a = 0; a < nd; ++a)
+    for (int b = 0; b < nd; ++b)
+      for (int m = 0; m < 6; ++m) {
+        kab[((size_t)a * nd + b) * 12 + m] = kc[((size_t)m * nd + a) * nd + b];
+        kab[((size_t)a * nd + b) * 12 + 6 + m] = km[((size_t)m * nd + a) * nd + b];
+      }
+  std::vector<float> kabf(kab.begin(), kab.end());
+  std::vector<int32_t> bidx(s.nt);
+  int64_t nb = 0;
+  for (int64_t c = 0; c < s.nt; ++c) bidx[c] = s.ext_mask[c] ? (int32_t)nb++ : -1;
 #define UP(field, src, cnt)                                                            \
   do {                                                                                 \
     e = up(&d->field, src, cnt);                                                       \
@@ -130,6 +146,10 @@ std::string upload_space(Space& s, int device) {
   UP(kc_d, kc.data(), kc.size());
   UP(km_d, km.data(), km.size());
   UP(kt_d, kf.data(), kf.size());
+  UP(kab_f, kabf.data(), kabf.size());
+  UP(kab_d, kab.data(), kab.size());
+  UP(bidx, bidx.data(), bidx.size());
+  d->nb = nb;
 #undef UP
   d->n_boundary = (int64_t)s.boundary_dofs.size();
   s.dev = d;
@@ -147,6 +167,8 @@ extern "C" {
 int sucem_version(void) { return SUCEM_ABI_VERSION; }
 
 const char* sucem_last_error(void) { return sucem::g_last_error.c_str(); }
+
+long long sucem_launch_count(void) { return sucem::g_launches.load(); }
 
 int sucem_space_create(const double* coords, int64_t nv, const int64_t* cells, int64_t nt,
                        int order, sucem_space** out) {
@@ -208,6 +230,7 @@ int sucem_space_copy(const sucem_space* sp, int what, void* dst) {
     case SUCEM_COPY_EXT_MASK: return cp(s.ext_mask.data(), s.ext_mask.size());
     case SUCEM_COPY_CELL_EDGES: return cp(s.cell_edges.data(), s.cell_edges.size() * 4);
     case SUCEM_COPY_CELL_FACES: return cp(s.cell_faces.data(), s.cell_faces.size() * 4);
+    case SUCEM_COPY_DOF_XYZ: return cp(s.dof_xyz.data(), s.dof_xyz.size() * 8);
     default: return fail("unknown copy selector", SUCEM_ERR_ARG);
   }
 }
@@ -237,7 +260,7 @@ int sucem_assemble(const sucem_space* sp, int real_bytes, const void* eps_r,
                    const void* mu_r_inv, void* S, void* T, void* B, void* stream) {
   if (!sp) return fail("null space", SUCEM_ERR_ARG);
   if (real_bytes != 4 && real_bytes != 8) return fail("real_bytes must be 4 or 8", SUCEM_ERR_ARG);
-  const sucem::DeviceSpace* d = sp->s.dev;
+  sucem::DeviceSpace* d = sp->s.dev;
   if (!d) return fail("space is not on a device (call sucem_space_upload)", SUCEM_ERR_STATE);
   if (!S && !T && !B) return SUCEM_OK;
   sucem::AssembleArgs a;
@@ -257,7 +280,7 @@ int sucem_assemble_helmholtz(const sucem_space* sp, int real_bytes, const void* 
                              const void* mu_r_inv, double k0, void* A, void* stream) {
   if (!sp || !A) return fail("null argument", SUCEM_ERR_ARG);
   if (real_bytes != 4 && real_bytes != 8) return fail("real_bytes must be 4 or 8", SUCEM_ERR_ARG);
-  const sucem::DeviceSpace* d = sp->s.dev;
+  sucem::DeviceSpace* d = sp->s.dev;
   if (!d) return fail("space is not on a device (call sucem_space_upload)", SUCEM_ERR_STATE);
   sucem::AssembleArgs a;
   a.real_bytes = real_bytes;
@@ -275,7 +298,7 @@ int sucem_assemble_host(const sucem_space* sp, int real_bytes, const void* eps_r
                         const void* mu_r_inv_host, void* S_host, void* T_host, void* B_host) {
   if (!sp) return fail("null space", SUCEM_ERR_ARG);
   if (real_bytes != 4 && real_bytes != 8) return fail("real_bytes must be 4 or 8", SUCEM_ERR_ARG);
-  const sucem::DeviceSpace* d = sp->s.dev;
+  sucem::DeviceSpace* d = sp->s.dev;
   if (!d) return fail("space is not on a device (call sucem_space_upload)", SUCEM_ERR_STATE);
   const size_t cbytes = (size_t)d->nt * real_bytes, vbytes = (size_t)d->nnz * real_bytes;
   void *de = nullptr, *dm = nullptr, *dS = nullptr, *dT = nullptr, *dB = nullptr;

@@ -26,6 +26,16 @@ struct DeviceSpace {
   int32_t* cell_dofs = nullptr;   // nt*nd
   int32_t* boundary_dofs = nullptr;
   int64_t n_boundary = 0;
+  int32_t* bidx = nullptr;        // nt: index among cells with exterior facets, -1 otherwise
+  int64_t nb = 0;                 // number of cells with exterior facets
+  // per-cell coefficient scratch of the assembly (allocated on first use)
+  float* g_f = nullptr;           // nt*12
+  double* g_d = nullptr;
+  float* h_f = nullptr;           // nb*12
+  double* h_d = nullptr;
+  // reference tensors in the row kernel's layout [a][b][12] (KC m=0..5, KM m=0..5)
+  float* kab_f = nullptr;
+  double* kab_d = nullptr;
   // reference tensors [6][nd][nd] (curl, mass), [4][3][nd][nd] (face tangential)
   float* kc_f = nullptr;
   float* km_f = nullptr;
@@ -53,6 +63,6 @@ struct AssembleArgs {
   void* A = nullptr;
   double k0 = 0.0;
 };
-cudaError_t launch_assemble(const DeviceSpace& d, const AssembleArgs& a, cudaStream_t stream);
+cudaError_t launch_assemble(DeviceSpace& d, const AssembleArgs& a, cudaStream_t stream);
 
 }  // namespace sucem

@@ -14,6 +14,7 @@ namespace sucem {
 
 int fail(const std::string& msg, int code);
 int cuda_fail(cudaError_t e, const char* where);
+void count_launch(int k);
 
 namespace {
 
@@ -197,7 +198,129 @@ __global__ void compact_kernel(int64_t n, const int32_t* __restrict__ indptr,
   }
 }
 
+// ---- vector kernels ----
+template <typename R, bool CPLX>
+__global__ void axpby_kernel(int64_t n, double ar, double ai, const R* __restrict__ x, double br,
+                             double bi, R* __restrict__ y) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (!CPLX) {
+    const double xv = x ? (double)x[i] : 0.0;
+    const double yv = br != 0.0 ? (double)y[i] : 0.0;
+    y[i] = (R)(ar * xv + br * yv);
+  } else {
+    const double xr = x ? (double)x[2 * i] : 0.0, xi = x ? (double)x[2 * i + 1] : 0.0;
+    double yr = 0, yi = 0;
+    if (br != 0.0 || bi != 0.0) {
+      yr = (double)y[2 * i];
+      yi = (double)y[2 * i + 1];
+    }
+    y[2 * i] = (R)(ar * xr - ai * xi + br * yr - bi * yi);
+    y[2 * i + 1] = (R)(ar * xi + ai * xr + br * yi + bi * yr);
+  }
+}
+
+// partial sums of conj(x).y (or x.y) per block, in double precision
+template <typename R, bool CPLX>
+__global__ void dot_partial_kernel(int64_t n, const R* __restrict__ x, const R* __restrict__ y,
+                                   int conj, double2* __restrict__ partial) {
+  __shared__ double sr[32], si[32];
+  double ar = 0, ai = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (!CPLX) {
+      ar += (double)x[i] * (double)y[i];
+    } else {
+      const double xr = x[2 * i], xi = conj ? -(double)x[2 * i + 1] : (double)x[2 * i + 1];
+      const double yr = y[2 * i], yi = y[2 * i + 1];
+      ar += xr * yr - xi * yi;
+      ai += xr * yi + xi * yr;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    ar += __shfl_down_sync(~0u, ar, o);
+    ai += __shfl_down_sync(~0u, ai, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sr[w] = ar;
+    si[w] = ai;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    ar = l < nw ? sr[l] : 0.0;
+    ai = l < nw ? si[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      ar += __shfl_down_sync(~0u, ar, o);
+      ai += __shfl_down_sync(~0u, ai, o);
+    }
+    if (l == 0) partial[blockIdx.x] = make_double2(ar, ai);
+  }
+}
+
+// fixed-order sum of the block partials (deterministic)
+__global__ void dot_final_kernel(int nparts, const double2* __restrict__ partial,
+                                 double2* __restrict__ out) {
+  __shared__ double sr[32], si[32];
+  double ar = 0, ai = 0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+    ar += partial[i].x;
+    ai += partial[i].y;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    ar += __shfl_down_sync(~0u, ar, o);
+    ai += __shfl_down_sync(~0u, ai, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sr[w] = ar;
+    si[w] = ai;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    ar = l < nw ? sr[l] : 0.0;
+    ai = l < nw ? si[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      ar += __shfl_down_sync(~0u, ar, o);
+      ai += __shfl_down_sync(~0u, ai, o);
+    }
+    if (l == 0) *out = make_double2(ar, ai);
+  }
+}
+
+template <typename D, typename S>
+__global__ void convert_kernel(int64_t m, const S* __restrict__ src, D* __restrict__ dst) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) dst[i] = (D)src[i];
+}
+
 }  // namespace
+
+constexpr int kDotBlocks = 512;
+
+cudaError_t vec_dot(int64_t n, int dtype, const void* x, const void* y, int conj,
+                    double2* partial, double2* out, cudaStream_t s) {
+  const int threads = 256;
+  switch (dtype) {
+    case SUCEM_F32:
+      dot_partial_kernel<float, false><<<kDotBlocks, threads, 0, s>>>(n, (const float*)x, (const float*)y, conj, partial);
+      break;
+    case SUCEM_F64:
+      dot_partial_kernel<double, false><<<kDotBlocks, threads, 0, s>>>(n, (const double*)x, (const double*)y, conj, partial);
+      break;
+    case SUCEM_C64:
+      dot_partial_kernel<float, true><<<kDotBlocks, threads, 0, s>>>(n, (const float*)x, (const float*)y, conj, partial);
+      break;
+    case SUCEM_C128:
+      dot_partial_kernel<double, true><<<kDotBlocks, threads, 0, s>>>(n, (const double*)x, (const double*)y, conj, partial);
+      break;
+    default: return cudaErrorInvalidValue;
+  }
+  dot_final_kernel<<<1, 256, 0, s>>>(kDotBlocks, partial, out);
+  return cudaGetLastError();
+}
 
 cudaError_t spmv(const DeviceSpace& d, int dtype, const void* vals, const void* x, void* y,
                  cudaStream_t s) {
@@ -247,6 +370,7 @@ int sucem_apply_essential(const sucem_space* sp, int dtype, void* vals, const in
     default: return fail("essential rows: dtype must be F32 or F64", SUCEM_ERR_ARG);
   }
   cudaError_t e = cudaGetLastError();
+  sucem::count_launch(1);
   return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_apply_essential");
 }
 
@@ -256,7 +380,76 @@ int sucem_spmv(const sucem_space* sp, int dtype, const void* vals, const void* x
   if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
   if (!vals || !x || !y) return fail("null argument", SUCEM_ERR_ARG);
   cudaError_t e = sucem::spmv(*d, dtype, vals, x, y, (cudaStream_t)stream);
+  sucem::count_launch(1);
   return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_spmv");
+}
+
+int sucem_spmv_csr(int64_t n, int64_t nnz, const int32_t* indptr, const int32_t* indices,
+                   int dtype, const void* vals, const void* x, void* y, void* stream) {
+  if (!indptr || !indices || !vals || !x || !y) return fail("null argument", SUCEM_ERR_ARG);
+  cudaError_t e = sucem::spmv_raw(n, nnz, indptr, indices, dtype, vals, x, y, (cudaStream_t)stream);
+  sucem::count_launch(1);
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_spmv_csr");
+}
+
+int sucem_vec_axpby(int64_t n, int dtype, double ar, double ai, const void* x, double br,
+                    double bi, void* y, void* stream) {
+  if (!y) return fail("null output", SUCEM_ERR_ARG);
+  if (n == 0) return SUCEM_OK;
+  const int threads = 256;
+  const unsigned blocks = (unsigned)((n + threads - 1) / threads);
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (dtype) {
+    case SUCEM_F32:
+      sucem::axpby_kernel<float, false><<<blocks, threads, 0, s>>>(n, ar, ai, (const float*)x, br, bi, (float*)y);
+      break;
+    case SUCEM_F64:
+      sucem::axpby_kernel<double, false><<<blocks, threads, 0, s>>>(n, ar, ai, (const double*)x, br, bi, (double*)y);
+      break;
+    case SUCEM_C64:
+      sucem::axpby_kernel<float, true><<<blocks, threads, 0, s>>>(n, ar, ai, (const float*)x, br, bi, (float*)y);
+      break;
+    case SUCEM_C128:
+      sucem::axpby_kernel<double, true><<<blocks, threads, 0, s>>>(n, ar, ai, (const double*)x, br, bi, (double*)y);
+      break;
+    default: return fail("bad dtype", SUCEM_ERR_ARG);
+  }
+  cudaError_t e = cudaGetLastError();
+  sucem::count_launch(1);
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_vec_axpby");
+}
+
+int64_t sucem_vec_dot_work_bytes(void) { return (int64_t)sucem::kDotBlocks * 16; }
+
+int sucem_vec_dot(int64_t n, int dtype, const void* x, const void* y, int conj, void* work,
+                  double* out, void* stream) {
+  if (!x || !y || !work || !out) return fail("null argument", SUCEM_ERR_ARG);
+  cudaError_t e = sucem::vec_dot(n, dtype, x, y, conj, (double2*)work, (double2*)out,
+                                 (cudaStream_t)stream);
+  sucem::count_launch(2);
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_vec_dot");
+}
+
+int sucem_vec_convert(int64_t count, int dst_real_bytes, void* dst, int src_real_bytes,
+                      const void* src, void* stream) {
+  if (!dst || !src) return fail("null argument", SUCEM_ERR_ARG);
+  if (count == 0) return SUCEM_OK;
+  const int threads = 256;
+  const unsigned blocks = (unsigned)((count + threads - 1) / threads);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dst_real_bytes == 4 && src_real_bytes == 8)
+    sucem::convert_kernel<float, double><<<blocks, threads, 0, s>>>(count, (const double*)src, (float*)dst);
+  else if (dst_real_bytes == 8 && src_real_bytes == 4)
+    sucem::convert_kernel<double, float><<<blocks, threads, 0, s>>>(count, (const float*)src, (double*)dst);
+  else if (dst_real_bytes == src_real_bytes)
+    return cudaMemcpyAsync(dst, src, count * dst_real_bytes, cudaMemcpyDeviceToDevice, s) == cudaSuccess
+               ? SUCEM_OK
+               : fail("copy failed", SUCEM_ERR_CUDA);
+  else
+    return fail("real sizes must be 4 or 8", SUCEM_ERR_ARG);
+  cudaError_t e = cudaGetLastError();
+  sucem::count_launch(1);
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_vec_convert");
 }
 
 int sucem_combine(int64_t m, int real_bytes, double a, const void* X, double b, const void* Y,
@@ -279,6 +472,7 @@ int sucem_combine(int64_t m, int real_bytes, double a, const void* X, double b, 
   else
     return fail("real_bytes must be 4 or 8", SUCEM_ERR_ARG);
   cudaError_t e = cudaGetLastError();
+  sucem::count_launch(1);
   return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_combine");
 }
 
@@ -300,6 +494,7 @@ int sucem_compact_count(const sucem_space* sp, int dtype, const void* vals, int3
     return fail("compaction needs a complex dtype", SUCEM_ERR_ARG);
   sucem::scan_kernel<<<1, 1024, 0, s>>>(d->n, work, out_indptr);
   cudaError_t e = cudaGetLastError();
+  sucem::count_launch(2);
   return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_compact_count");
 }
 
@@ -322,6 +517,7 @@ int sucem_compact_fill(const sucem_space* sp, int dtype, const void* vals,
   else
     return fail("compaction needs a complex dtype", SUCEM_ERR_ARG);
   cudaError_t e = cudaGetLastError();
+  sucem::count_launch(1);
   return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_compact_fill");
 }
 

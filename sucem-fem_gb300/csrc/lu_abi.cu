@@ -1,0 +1,168 @@
+// C-ABI of the multifrontal sparse LU (declarations: include/sucem_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/sucem_gb300.h"
+#include "mf.h"
+
+namespace sucem {
+int fail(const std::string& msg, int code);
+int cuda_fail(cudaError_t e, const char* where);
+void count_launch(int k);
+
+// the numeric handle is defined next to its kernels
+struct MFHandle;
+MFHandle* mf_new();
+void mf_delete(MFHandle* h);
+MFSymbolic& mf_sym(MFHandle* h);
+
+namespace {
+
+template <typename R>
+__global__ void max_abs_kernel(int64_t m, const R* __restrict__ v, int stride,
+                               unsigned long long* __restrict__ out) {
+  // values are >= 0, so the IEEE bit pattern orders like an unsigned integer
+  double best = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double a = 0;
+    for (int c = 0; c < stride; ++c) a += (double)v[i * stride + c] * (double)v[i * stride + c];
+    best = fmax(best, sqrt(a));
+  }
+  for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_down_sync(~0u, best, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(best));
+}
+
+}  // namespace
+}  // namespace sucem
+
+struct sucem_lu {
+  sucem::MFHandle* h = nullptr;
+};
+
+using sucem::cuda_fail;
+using sucem::fail;
+
+extern "C" {
+
+int sucem_lu_analyse(int64_t n, const int32_t* indptr, const int32_t* indices, const double* xyz,
+                     int leaf_size, sucem_lu** out) {
+  if (!indptr || !indices || !xyz || !out) return fail("null argument", SUCEM_ERR_ARG);
+  *out = nullptr;
+  sucem_lu* lu = new (std::nothrow) sucem_lu();
+  if (!lu) return fail("out of host memory", SUCEM_ERR_MEMORY);
+  lu->h = sucem::mf_new();
+  std::string err;
+  try {
+    err = sucem::mf_analyse(sucem::mf_sym(lu->h), n, indptr, indices, xyz, leaf_size);
+  } catch (const std::bad_alloc&) {
+    err = "out of host memory";
+  }
+  if (!err.empty()) {
+    sucem::mf_delete(lu->h);
+    delete lu;
+    return fail(err, SUCEM_ERR_ARG);
+  }
+  *out = lu;
+  return SUCEM_OK;
+}
+
+int sucem_lu_analyse_cells(int64_t n, const int32_t* indptr, const int32_t* indices, int64_t nt,
+                           int ndof_cell, const int32_t* cell_dofs, const double* cell_xyz,
+                           int leaf_size, sucem_lu** out) {
+  if (!indptr || !indices || !cell_dofs || !cell_xyz || !out)
+    return fail("null argument", SUCEM_ERR_ARG);
+  *out = nullptr;
+  sucem_lu* lu = new (std::nothrow) sucem_lu();
+  if (!lu) return fail("out of host memory", SUCEM_ERR_MEMORY);
+  lu->h = sucem::mf_new();
+  std::string err;
+  try {
+    err = sucem::mf_analyse_cells(sucem::mf_sym(lu->h), n, indptr, indices, nt, ndof_cell,
+                                  cell_dofs, cell_xyz, leaf_size);
+  } catch (const std::bad_alloc&) {
+    err = "out of host memory";
+  }
+  if (!err.empty()) {
+    sucem::mf_delete(lu->h);
+    delete lu;
+    return fail(err, SUCEM_ERR_ARG);
+  }
+  *out = lu;
+  return SUCEM_OK;
+}
+
+void sucem_lu_destroy(sucem_lu* lu) {
+  if (!lu) return;
+  sucem::mf_delete(lu->h);
+  delete lu;
+}
+
+int sucem_lu_info(const sucem_lu* lu, double* out) {
+  if (!lu || !out) return fail("null argument", SUCEM_ERR_ARG);
+  const sucem::MFSymbolic& s = sucem::mf_sym(lu->h);
+  out[0] = (double)s.n;
+  out[1] = (double)s.nnz;
+  out[2] = (double)s.nodes.size();
+  out[3] = (double)(s.max_level + 1);
+  out[4] = (double)s.arena;
+  out[5] = s.flops;
+  out[6] = (double)s.max_front;
+  return SUCEM_OK;
+}
+
+int sucem_lu_copy_perm(const sucem_lu* lu, int64_t* perm) {
+  if (!lu || !perm) return fail("null argument", SUCEM_ERR_ARG);
+  const sucem::MFSymbolic& s = sucem::mf_sym(lu->h);
+  for (int64_t i = 0; i < s.n; ++i) perm[i] = s.perm[i];
+  return SUCEM_OK;
+}
+
+int sucem_lu_factor(sucem_lu* lu, int dtype, const void* vals, double pivot_tol, void* stream) {
+  if (!lu || !vals) return fail("null argument", SUCEM_ERR_ARG);
+  if (dtype < SUCEM_F32 || dtype > SUCEM_C128) return fail("bad dtype", SUCEM_ERR_ARG);
+  cudaStream_t st = (cudaStream_t)stream;
+  const sucem::MFSymbolic& s = sucem::mf_sym(lu->h);
+  // static pivot threshold relative to the largest |entry|
+  unsigned long long* dmax = nullptr;
+  cudaError_t e = cudaMalloc((void**)&dmax, sizeof(unsigned long long));
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_lu_factor");
+  e = cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), st);
+  const int stride = (dtype == SUCEM_C64 || dtype == SUCEM_C128) ? 2 : 1;
+  if (e == cudaSuccess) {
+    if (dtype == SUCEM_F32 || dtype == SUCEM_C64)
+      sucem::max_abs_kernel<float><<<256, 256, 0, st>>>(s.nnz, (const float*)vals, stride, dmax);
+    else
+      sucem::max_abs_kernel<double><<<256, 256, 0, st>>>(s.nnz, (const double*)vals, stride, dmax);
+    sucem::count_launch(1);
+    e = cudaGetLastError();
+  }
+  unsigned long long bits = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, dmax, sizeof(bits), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(dmax);
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_lu_factor");
+  double amax;
+  memcpy(&amax, &bits, sizeof(double));
+  const double tau = pivot_tol * (amax > 0 ? amax : 1.0);
+  e = sucem::mf_factor(*lu->h, dtype, vals, tau, st);
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_lu_factor");
+  return SUCEM_OK;
+}
+
+int sucem_lu_solve(sucem_lu* lu, int io_dtype, const void* b, void* x, void* stream) {
+  if (!lu || !b || !x) return fail("null argument", SUCEM_ERR_ARG);
+  cudaError_t e = sucem::mf_solve(*lu->h, io_dtype, b, x, (cudaStream_t)stream);
+  if (e == cudaErrorNotReady) return fail("factor before solving", SUCEM_ERR_STATE);
+  if (e == cudaErrorInvalidValue)
+    return fail("solve dtype must match the factor (or its double-precision twin)", SUCEM_ERR_ARG);
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_lu_solve");
+  return SUCEM_OK;
+}
+
+int sucem_lu_perturbed(sucem_lu* lu) { return lu ? sucem::mf_perturbed(*lu->h) : 0; }
+
+}  // extern "C"

@@ -1,0 +1,730 @@
+// Numeric multifrontal LU on the GPU (factor and solve), level by level
+// over the assembly tree built by mf_symbolic.cpp.  Scalars: float, double,
+// complex float (float2), complex double (double2).
+//
+// Factor: the arena of dense row-major fronts is zeroed, the matrix values
+// are scattered into it, then for every tree level (leaves first): the
+// children's Schur complements are added into their parents (extend-add,
+// one launch per child slot so no two writers meet), and every front of the
+// level is partially factorised with a blocked right-looking LU (panel
+// width 32): diagonal-block LU (one block per front), the two triangular
+// panel solves, and the trailing update, a batched register-tiled GEMM.
+// Solve: forward (unit-lower L) and backward (U) substitution level by
+// level; the off-diagonal block products are spread over many blocks.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+
+#include "../../include/sucem_gb300.h"
+#include "mf.h"
+
+namespace sucem {
+int fail(const std::string& msg, int code);
+int cuda_fail(cudaError_t e, const char* where);
+void count_launch(int k);
+
+namespace {
+
+constexpr int NB = 32;  // panel width
+
+// ---- scalar helpers ----
+__device__ __forceinline__ float s_zero(float) { return 0.f; }
+__device__ __forceinline__ double s_zero(double) { return 0.0; }
+__device__ __forceinline__ float2 s_zero(float2) { return make_float2(0.f, 0.f); }
+__device__ __forceinline__ double2 s_zero(double2) { return make_double2(0.0, 0.0); }
+
+__device__ __forceinline__ float s_fms(float c, float a, float b) { return fmaf(-a, b, c); }
+__device__ __forceinline__ double s_fms(double c, double a, double b) { return fma(-a, b, c); }
+__device__ __forceinline__ float2 s_fms(float2 c, float2 a, float2 b) {
+  c.x = fmaf(-a.x, b.x, c.x);
+  c.x = fmaf(a.y, b.y, c.x);
+  c.y = fmaf(-a.x, b.y, c.y);
+  c.y = fmaf(-a.y, b.x, c.y);
+  return c;
+}
+__device__ __forceinline__ double2 s_fms(double2 c, double2 a, double2 b) {
+  c.x = fma(-a.x, b.x, c.x);
+  c.x = fma(a.y, b.y, c.x);
+  c.y = fma(-a.x, b.y, c.y);
+  c.y = fma(-a.y, b.x, c.y);
+  return c;
+}
+__device__ __forceinline__ float s_add(float a, float b) { return a + b; }
+__device__ __forceinline__ double s_add(double a, double b) { return a + b; }
+__device__ __forceinline__ float2 s_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 s_add(double2 a, double2 b) {
+  return make_double2(a.x + b.x, a.y + b.y);
+}
+__device__ __forceinline__ float s_div(float a, float b) { return a / b; }
+__device__ __forceinline__ double s_div(double a, double b) { return a / b; }
+__device__ __forceinline__ float2 s_div(float2 a, float2 b) {
+  const float d = b.x * b.x + b.y * b.y;
+  return make_float2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+__device__ __forceinline__ double2 s_div(double2 a, double2 b) {
+  const double d = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+__device__ __forceinline__ double s_abs(float a) { return fabsf(a); }
+__device__ __forceinline__ double s_abs(double a) { return fabs(a); }
+__device__ __forceinline__ double s_abs(float2 a) { return hypotf(a.x, a.y); }
+__device__ __forceinline__ double s_abs(double2 a) { return hypot(a.x, a.y); }
+__device__ __forceinline__ float s_real(float, double v) { return (float)v; }
+__device__ __forceinline__ double s_real(double, double v) { return v; }
+__device__ __forceinline__ float2 s_real(float2, double v) { return make_float2((float)v, 0.f); }
+__device__ __forceinline__ double2 s_real(double2, double v) { return make_double2(v, 0.0); }
+__device__ __forceinline__ void s_atomic_sub(float* p, float v) { atomicAdd(p, -v); }
+__device__ __forceinline__ void s_atomic_sub(double* p, double v) { atomicAdd(p, -v); }
+__device__ __forceinline__ void s_atomic_sub(float2* p, float2 v) {
+  atomicAdd(&p->x, -v.x);
+  atomicAdd(&p->y, -v.y);
+}
+__device__ __forceinline__ void s_atomic_sub(double2* p, double2 v) {
+  atomicAdd(&p->x, -v.x);
+  atomicAdd(&p->y, -v.y);
+}
+template <typename S>
+__device__ __forceinline__ S s_shfl_down(S v, int o);
+template <>
+__device__ __forceinline__ float s_shfl_down(float v, int o) { return __shfl_down_sync(~0u, v, o); }
+template <>
+__device__ __forceinline__ double s_shfl_down(double v, int o) { return __shfl_down_sync(~0u, v, o); }
+template <>
+__device__ __forceinline__ float2 s_shfl_down(float2 v, int o) {
+  return make_float2(__shfl_down_sync(~0u, v.x, o), __shfl_down_sync(~0u, v.y, o));
+}
+template <>
+__device__ __forceinline__ double2 s_shfl_down(double2 v, int o) {
+  return make_double2(__shfl_down_sync(~0u, v.x, o), __shfl_down_sync(~0u, v.y, o));
+}
+template <typename S>
+__device__ __forceinline__ S s_shfl(S v, int src);
+template <>
+__device__ __forceinline__ float s_shfl(float v, int s) { return __shfl_sync(~0u, v, s); }
+template <>
+__device__ __forceinline__ double s_shfl(double v, int s) { return __shfl_sync(~0u, v, s); }
+template <>
+__device__ __forceinline__ float2 s_shfl(float2 v, int s) {
+  return make_float2(__shfl_sync(~0u, v.x, s), __shfl_sync(~0u, v.y, s));
+}
+template <>
+__device__ __forceinline__ double2 s_shfl(double2 v, int s) {
+  return make_double2(__shfl_sync(~0u, v.x, s), __shfl_sync(~0u, v.y, s));
+}
+
+// ---- per-node device metadata ----
+struct DNode {
+  int64_t off;  // front offset in the arena
+  int64_t start;
+  int32_t f, k;
+  int64_t u_off;   // offset of U (new indices) in d_U
+  int64_t ea_off;  // offset of the extend-add map in d_ea
+  int32_t parent;
+  int32_t child_slot;  // 0 or 1: position among the parent's children
+};
+
+// ---- factor kernels ----
+template <typename S>
+__global__ void scatter_kernel(int64_t m, const int32_t* __restrict__ src,
+                               const int64_t* __restrict__ dst, const S* __restrict__ vals,
+                               S* __restrict__ arena) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) arena[dst[i]] = vals[src[i]];
+}
+
+// children (of nodes in this level) with the given child slot add their
+// Schur complement into the parent front; one block row per (child, row)
+template <typename S>
+__global__ void extend_add_kernel(const int32_t* __restrict__ kids, int nkids,
+                                  const DNode* __restrict__ nodes, const int32_t* __restrict__ ea,
+                                  S* __restrict__ arena) {
+  const int ci = blockIdx.y;
+  if (ci >= nkids) return;
+  const DNode c = nodes[kids[ci]];
+  const int u = c.f - c.k;
+  if (u <= 0 || c.parent < 0) return;
+  const DNode p = nodes[c.parent];
+  const int32_t* map = ea + c.ea_off;
+  for (int r = blockIdx.x; r < u; r += gridDim.x) {
+    const S* src = arena + c.off + (int64_t)(c.k + r) * c.f + c.k;
+    S* dst = arena + p.off + (int64_t)map[r] * p.f;
+    for (int j = threadIdx.x; j < u; j += blockDim.x) {
+      S* d = dst + map[j];
+      *d = s_add(*d, src[j]);
+    }
+  }
+}
+
+// LU (no pivoting, static pivot replacement) of the nb x nb diagonal block
+template <typename S>
+__global__ void diag_lu_kernel(const int32_t* __restrict__ list, int count,
+                               const DNode* __restrict__ nodes, S* __restrict__ arena, int p0,
+                               double tau, int* __restrict__ n_perturbed) {
+  __shared__ S D[NB][NB + 1];
+  const int fi = blockIdx.x;
+  if (fi >= count) return;
+  const DNode nd = nodes[list[fi]];
+  const int nb = min(NB, nd.k - p0);
+  if (nb <= 0) return;
+  S* base = arena + nd.off + (int64_t)p0 * nd.f + p0;
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    const int r = t / nb, c = t % nb;
+    D[r][c] = base[(int64_t)r * nd.f + c];
+  }
+  __syncthreads();
+  for (int i = 0; i < nb; ++i) {
+    if (threadIdx.x == 0 && s_abs(D[i][i]) < tau) {
+      D[i][i] = s_real(D[i][i], tau);
+      atomicAdd(n_perturbed, 1);
+    }
+    __syncthreads();
+    for (int r = i + 1 + threadIdx.x; r < nb; r += blockDim.x) D[r][i] = s_div(D[r][i], D[i][i]);
+    __syncthreads();
+    const int w = nb - i - 1;
+    for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
+      const int r = i + 1 + t / w, c = i + 1 + t % w;
+      D[r][c] = s_fms(D[r][c], D[r][i], D[i][c]);
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    const int r = t / nb, c = t % nb;
+    base[(int64_t)r * nd.f + c] = D[r][c];
+  }
+}
+
+// panel solves: rows below the diagonal block (X U11 = A, thread per row)
+// and columns right of it (L11 X = A, thread per column); 128 per block
+template <typename S>
+__global__ void panel_trsm_kernel(const int32_t* __restrict__ list, int count,
+                                  const DNode* __restrict__ nodes, S* __restrict__ arena, int p0) {
+  __shared__ S D[NB][NB + 1];
+  __shared__ S T[128][NB + 1];
+  const int fi = blockIdx.y;
+  if (fi >= count) return;
+  const DNode nd = nodes[list[fi]];
+  const int nb = min(NB, nd.k - p0);
+  if (nb <= 0) return;
+  const int rest = nd.f - p0 - nb;
+  if (rest <= 0) return;
+  const int tiles = (rest + 127) / 128;
+  int tile = blockIdx.x;
+  const bool rows = tile < tiles;
+  if (!rows) tile -= tiles;
+  if (tile >= tiles) return;
+  S* base = arena + nd.off + (int64_t)p0 * nd.f + p0;
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) D[t / nb][t % nb] = base[(int64_t)(t / nb) * nd.f + t % nb];
+  const int first = p0 + nb + tile * 128;
+  const int cnt = min(128, nd.f - first);
+  if (rows) {
+    // load cnt rows x nb columns (coalesced along the row)
+    for (int t = threadIdx.x; t < cnt * nb; t += blockDim.x) {
+      const int r = t / nb, c = t % nb;
+      T[r][c] = arena[nd.off + (int64_t)(first + r) * nd.f + p0 + c];
+    }
+    __syncthreads();
+    if (threadIdx.x < cnt) {
+      const int r = threadIdx.x;
+      for (int j = 0; j < nb; ++j) {
+        S x = T[r][j];
+        for (int i = 0; i < j; ++i) x = s_fms(x, T[r][i], D[i][j]);
+        T[r][j] = s_div(x, D[j][j]);
+      }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < cnt * nb; t += blockDim.x) {
+      const int r = t / nb, c = t % nb;
+      arena[nd.off + (int64_t)(first + r) * nd.f + p0 + c] = T[r][c];
+    }
+  } else {
+    __syncthreads();
+    if (threadIdx.x < cnt) {
+      const int col = first + threadIdx.x;
+      S* colp = arena + nd.off + (int64_t)p0 * nd.f + col;
+      S x[NB];
+#pragma unroll
+      for (int i = 0; i < NB; ++i)
+        if (i < nb) x[i] = colp[(int64_t)i * nd.f];
+#pragma unroll
+      for (int i = 0; i < NB; ++i) {
+        if (i >= nb) break;
+#pragma unroll
+        for (int j = 0; j < NB; ++j)
+          if (j < i) x[i] = s_fms(x[i], D[i][j], x[j]);
+      }
+#pragma unroll
+      for (int i = 0; i < NB; ++i)
+        if (i < nb) colp[(int64_t)i * nd.f] = x[i];
+    }
+  }
+}
+
+// trailing update C -= Lpanel * Upanel over the (f-p0-nb)^2 block,
+// 64x64 tile per block, 4x4 outputs per thread
+template <typename S>
+__global__ void __launch_bounds__(256) gemm_update_kernel(const int32_t* __restrict__ list,
+                                                          int count,
+                                                          const DNode* __restrict__ nodes,
+                                                          S* __restrict__ arena, int p0) {
+  __shared__ S As[NB][64 + 1];  // As[t][i] = L[i][t]
+  __shared__ S Bs[NB][64];      // Bs[t][j] = U[t][j]
+  const int fi = blockIdx.y;
+  if (fi >= count) return;
+  const DNode nd = nodes[list[fi]];
+  const int nb = min(NB, nd.k - p0);
+  if (nb <= 0) return;
+  const int lo = p0 + nb;
+  const int rest = nd.f - lo;
+  if (rest <= 0) return;
+  const int tpd = (rest + 63) / 64;
+  if ((int)blockIdx.x >= tpd * tpd) return;
+  const int ti = blockIdx.x / tpd, tj = blockIdx.x % tpd;
+  const int i0 = lo + ti * 64, j0 = lo + tj * 64;
+  S* F = arena + nd.off;
+  for (int t = threadIdx.x; t < 64 * NB; t += 256) {
+    const int i = t / NB, c = t % NB;
+    As[c][i] = (i0 + i < nd.f && c < nb) ? F[(int64_t)(i0 + i) * nd.f + p0 + c] : s_zero(S());
+    const int r = t / 64, j = t % 64;
+    Bs[r][j] = (j0 + j < nd.f && r < nb) ? F[(int64_t)(p0 + r) * nd.f + j0 + j] : s_zero(S());
+  }
+  __syncthreads();
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  S acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = s_zero(S());
+  for (int t = 0; t < nb; ++t) {
+    S av[4], bv[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) av[a] = As[t][ty + 16 * a];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) bv[b] = Bs[t][tx + 16 * b];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] = s_fms(acc[a][b], av[a], bv[b]);
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int i = i0 + ty + 16 * a;
+    if (i >= nd.f) continue;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int j = j0 + tx + 16 * b;
+      if (j >= nd.f) continue;
+      S* c = F + (int64_t)i * nd.f + j;
+      *c = s_add(*c, acc[a][b]);
+    }
+  }
+}
+
+// ---- solve kernels (x in the new ordering) ----
+// forward: y_V = L11^-1 y_V (unit lower), one block per front
+template <typename S>
+__global__ void fwd_trsv_kernel(const int32_t* __restrict__ list, int count,
+                                const DNode* __restrict__ nodes, const S* __restrict__ arena,
+                                S* __restrict__ x) {
+  const int fi = blockIdx.x;
+  if (fi >= count) return;
+  const DNode nd = nodes[list[fi]];
+  const S* F = arena + nd.off;
+  S* y = x + nd.start;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int b0 = 0; b0 < nd.k; b0 += 32) {
+    // subtract the contributions of the solved rows [0, b0) from rows of this block
+    if (b0 > 0) {
+      for (int r = b0 + warp; r < min(b0 + 32, nd.k); r += nw) {
+        S acc = s_zero(S());
+        for (int j = lane; j < b0; j += 32) acc = s_fms(acc, F[(int64_t)r * nd.f + j], y[j]);
+        for (int o = 16; o > 0; o >>= 1) acc = s_add(acc, s_shfl_down(acc, o));
+        if (lane == 0) y[r] = s_add(y[r], acc);
+      }
+      __syncthreads();
+    }
+    if (warp == 0) {
+      const int r = b0 + lane;
+      S v = r < nd.k ? y[r] : s_zero(S());
+      const int m = min(32, nd.k - b0);
+      for (int j = 0; j < m; ++j) {
+        const S yj = s_shfl(v, j);
+        if (lane > j && r < nd.k) v = s_fms(v, F[(int64_t)r * nd.f + b0 + j], yj);
+      }
+      if (r < nd.k) y[r] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// forward update of the ancestors: x[U[r]] -= L21[r,:] . y_V (warp per row)
+template <typename S>
+__global__ void fwd_gemv_kernel(const int32_t* __restrict__ list, int count,
+                                const DNode* __restrict__ nodes, const int32_t* __restrict__ U,
+                                const S* __restrict__ arena, S* __restrict__ x) {
+  const int fi = blockIdx.y;
+  if (fi >= count) return;
+  const DNode nd = nodes[list[fi]];
+  const int u = nd.f - nd.k;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const S* y = x + nd.start;
+  for (int r = warp; r < u; r += nwarps) {
+    const S* row = arena + nd.off + (int64_t)(nd.k + r) * nd.f;
+    S acc = s_zero(S());
+    for (int j = lane; j < nd.k; j += 32) acc = s_fms(acc, row[j], y[j]);
+    for (int o = 16; o > 0; o >>= 1) acc = s_add(acc, s_shfl_down(acc, o));
+    if (lane == 0) s_atomic_sub(&x[U[nd.u_off + r]], s_fms(s_zero(S()), acc, s_real(S(), 1.0)));
+  }
+}
+
+// backward: y_V -= U12 . x_U (warp per row)
+template <typename S>
+__global__ void bwd_gemv_kernel(const int32_t* __restrict__ list, int count,
+                                const DNode* __restrict__ nodes, const int32_t* __restrict__ U,
+                                const S* __restrict__ arena, S* __restrict__ x) {
+  const int fi = blockIdx.y;
+  if (fi >= count) return;
+  const DNode nd = nodes[list[fi]];
+  const int u = nd.f - nd.k;
+  if (u <= 0) return;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int32_t* Ui = U + nd.u_off;
+  for (int r = warp; r < nd.k; r += nwarps) {
+    const S* row = arena + nd.off + (int64_t)r * nd.f + nd.k;
+    S acc = s_zero(S());
+    for (int j = lane; j < u; j += 32) acc = s_fms(acc, row[j], x[Ui[j]]);
+    for (int o = 16; o > 0; o >>= 1) acc = s_add(acc, s_shfl_down(acc, o));
+    if (lane == 0) x[nd.start + r] = s_add(x[nd.start + r], acc);
+  }
+}
+
+// backward: x_V = U11^-1 y_V (upper, non-unit), one block per front
+template <typename S>
+__global__ void bwd_trsv_kernel(const int32_t* __restrict__ list, int count,
+                                const DNode* __restrict__ nodes, const S* __restrict__ arena,
+                                S* __restrict__ x) {
+  const int fi = blockIdx.x;
+  if (fi >= count) return;
+  const DNode nd = nodes[list[fi]];
+  const S* F = arena + nd.off;
+  S* y = x + nd.start;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int nblk = (nd.k + 31) / 32;
+  for (int bi = nblk - 1; bi >= 0; --bi) {
+    const int b0 = bi * 32, b1 = min(b0 + 32, nd.k);
+    if (b1 < nd.k) {
+      for (int r = b0 + warp; r < b1; r += nw) {
+        S acc = s_zero(S());
+        for (int j = b1 + lane; j < nd.k; j += 32) acc = s_fms(acc, F[(int64_t)r * nd.f + j], y[j]);
+        for (int o = 16; o > 0; o >>= 1) acc = s_add(acc, s_shfl_down(acc, o));
+        if (lane == 0) y[r] = s_add(y[r], acc);
+      }
+      __syncthreads();
+    }
+    if (warp == 0) {
+      const int r = b0 + lane;
+      S v = r < b1 ? y[r] : s_zero(S());
+      for (int j = b1 - 1; j >= b0; --j) {
+        if (r == j) v = s_div(v, F[(int64_t)r * nd.f + r]);
+        const S xj = s_shfl(v, j - b0);
+        if (r < j) v = s_fms(v, F[(int64_t)r * nd.f + j], xj);
+      }
+      if (r < b1) y[r] = v;
+    }
+    __syncthreads();
+  }
+}
+
+template <typename S, typename T>
+__global__ void permute_in_kernel(int64_t n, const int64_t* __restrict__ perm,
+                                  const T* __restrict__ b, S* __restrict__ x);
+template <typename S, typename T>
+__global__ void permute_out_kernel(int64_t n, const int64_t* __restrict__ perm,
+                                   const S* __restrict__ x, T* __restrict__ out);
+
+__device__ __forceinline__ void cvt(float& d, float s) { d = s; }
+__device__ __forceinline__ void cvt(float& d, double s) { d = (float)s; }
+__device__ __forceinline__ void cvt(double& d, float s) { d = s; }
+__device__ __forceinline__ void cvt(double& d, double s) { d = s; }
+__device__ __forceinline__ void cvt(float2& d, float2 s) { d = s; }
+__device__ __forceinline__ void cvt(float2& d, double2 s) { d = make_float2((float)s.x, (float)s.y); }
+__device__ __forceinline__ void cvt(double2& d, float2 s) { d = make_double2(s.x, s.y); }
+__device__ __forceinline__ void cvt(double2& d, double2 s) { d = s; }
+
+template <typename S, typename T>
+__global__ void permute_in_kernel(int64_t n, const int64_t* __restrict__ perm,
+                                  const T* __restrict__ b, S* __restrict__ x) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) cvt(x[i], b[perm[i]]);
+}
+template <typename S, typename T>
+__global__ void permute_out_kernel(int64_t n, const int64_t* __restrict__ perm,
+                                   const S* __restrict__ x, T* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) cvt(out[perm[i]], x[i]);
+}
+
+}  // namespace
+
+// ---- host object ----
+struct MFLevel {
+  std::vector<int32_t> nodes_by_k;  // node ids sorted by k descending
+  std::vector<int32_t> kids[2];     // children by slot
+  int max_k = 0, max_rest = 0, max_u = 0;
+  int32_t* d_nodes = nullptr;
+  int32_t* d_kids[2] = {nullptr, nullptr};
+  std::vector<int> k_sorted;        // k of nodes_by_k
+};
+
+struct MFDevice {
+  int device = -1;
+  int dtype = -1;                   // SUCEM_F32 ...
+  size_t elem = 0;
+  void* arena = nullptr;
+  DNode* d_nodes = nullptr;
+  int32_t* d_U = nullptr;
+  int32_t* d_ea = nullptr;
+  int32_t* d_src = nullptr;
+  int64_t* d_dst = nullptr;
+  int64_t* d_perm = nullptr;
+  void* d_x = nullptr;              // solve work vector (new ordering)
+  int* d_flag = nullptr;            // perturbed pivot count
+  std::vector<MFLevel> levels;
+  bool factored = false;
+  int perturbed = 0;
+};
+
+struct MFHandle {
+  MFSymbolic sym;
+  MFDevice dev;
+};
+
+namespace {
+
+size_t elem_size(int dtype) {
+  switch (dtype) {
+    case SUCEM_F32: return 4;
+    case SUCEM_F64: return 8;
+    case SUCEM_C64: return 8;
+    case SUCEM_C128: return 16;
+  }
+  return 0;
+}
+
+template <typename T>
+cudaError_t upv(T** d, const std::vector<T>& h) {
+  *d = nullptr;
+  if (h.empty()) return cudaSuccess;
+  cudaError_t e = cudaMalloc((void**)d, h.size() * sizeof(T));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+void free_dev(MFDevice& d) {
+  void* ptrs[] = {d.arena, d.d_nodes, d.d_U, d.d_ea, d.d_src, d.d_dst, d.d_perm, d.d_x, d.d_flag};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (auto& L : d.levels) {
+    if (L.d_nodes) cudaFree(L.d_nodes);
+    for (int s = 0; s < 2; ++s)
+      if (L.d_kids[s]) cudaFree(L.d_kids[s]);
+  }
+  d = MFDevice();
+}
+
+cudaError_t setup_device(MFHandle& h, int dtype) {
+  MFDevice& d = h.dev;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (d.device == dev && d.dtype == dtype) return cudaSuccess;
+  free_dev(d);
+  d.device = dev;
+  d.dtype = dtype;
+  d.elem = elem_size(dtype);
+  const MFSymbolic& s = h.sym;
+  std::vector<DNode> dn(s.nodes.size());
+  std::vector<int32_t> U;
+  for (size_t i = 0; i < s.nodes.size(); ++i) {
+    const MFNode& nd = s.nodes[i];
+    dn[i].off = nd.front_off;
+    dn[i].start = nd.start;
+    dn[i].f = (int32_t)nd.f;
+    dn[i].k = (int32_t)nd.k;
+    dn[i].u_off = (int64_t)U.size();
+    for (int64_t u : nd.U) U.push_back((int32_t)u);
+    dn[i].ea_off = nd.ea_off;
+    dn[i].parent = nd.parent;
+    dn[i].child_slot = 0;
+  }
+  for (size_t i = 0; i < s.nodes.size(); ++i)
+    for (size_t c = 0; c < s.nodes[i].children.size(); ++c) dn[s.nodes[i].children[c]].child_slot = (int)c;
+  d.levels.assign(s.max_level + 1, MFLevel());
+  for (size_t i = 0; i < s.nodes.size(); ++i) {
+    const MFNode& nd = s.nodes[i];
+    MFLevel& L = d.levels[nd.level];
+    L.nodes_by_k.push_back((int32_t)i);
+    for (size_t c = 0; c < nd.children.size() && c < 2; ++c) L.kids[c].push_back(nd.children[c]);
+  }
+  cudaError_t e = cudaSuccess;
+  for (auto& L : d.levels) {
+    std::sort(L.nodes_by_k.begin(), L.nodes_by_k.end(),
+              [&](int32_t a, int32_t b) { return s.nodes[a].k > s.nodes[b].k; });
+    for (int32_t i : L.nodes_by_k) {
+      L.k_sorted.push_back((int)s.nodes[i].k);
+      L.max_k = std::max<int>(L.max_k, (int)s.nodes[i].k);
+      L.max_rest = std::max<int>(L.max_rest, (int)s.nodes[i].f);
+      L.max_u = std::max<int>(L.max_u, (int)(s.nodes[i].f - s.nodes[i].k));
+    }
+    if (e == cudaSuccess) e = upv(&L.d_nodes, L.nodes_by_k);
+    for (int c = 0; c < 2; ++c)
+      if (e == cudaSuccess) e = upv(&L.d_kids[c], L.kids[c]);
+  }
+  if (e == cudaSuccess) e = upv(&d.d_nodes, dn);
+  if (e == cudaSuccess) e = upv(&d.d_U, U);
+  if (e == cudaSuccess) e = upv(&d.d_ea, s.ea_map);
+  if (e == cudaSuccess) e = upv(&d.d_src, s.scat_src);
+  if (e == cudaSuccess) e = upv(&d.d_dst, s.scat_dst);
+  if (e == cudaSuccess) e = upv(&d.d_perm, s.perm);
+  if (e == cudaSuccess) e = cudaMalloc(&d.arena, (size_t)std::max<int64_t>(s.arena, 1) * d.elem);
+  if (e == cudaSuccess) e = cudaMalloc(&d.d_x, (size_t)std::max<int64_t>(s.n, 1) * d.elem);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&d.d_flag, sizeof(int));
+  if (e != cudaSuccess) free_dev(d);
+  return e;
+}
+
+template <typename S>
+cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st) {
+  MFDevice& d = h.dev;
+  const MFSymbolic& s = h.sym;
+  S* arena = (S*)d.arena;
+  cudaError_t e = cudaMemsetAsync(arena, 0, (size_t)s.arena * sizeof(S), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.d_flag, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  const int64_t m = (int64_t)s.scat_src.size();
+  if (m > 0) {
+    scatter_kernel<S><<<(unsigned)((m + 255) / 256), 256, 0, st>>>(m, d.d_src, d.d_dst,
+                                                                   (const S*)vals, arena);
+    count_launch(1);
+  }
+  for (size_t lv = 0; lv < d.levels.size(); ++lv) {
+    const MFLevel& L = d.levels[lv];
+    for (int c = 0; c < 2; ++c) {
+      const int nk = (int)L.kids[c].size();
+      if (nk == 0) continue;
+      dim3 grid(64, nk);
+      extend_add_kernel<S><<<grid, 128, 0, st>>>(L.d_kids[c], nk, d.d_nodes, d.d_ea, arena);
+      count_launch(1);
+    }
+    for (int p0 = 0; p0 < L.max_k; p0 += NB) {
+      // active fronts: prefix of the k-descending list with k > p0
+      int cnt = 0;
+      while (cnt < (int)L.k_sorted.size() && L.k_sorted[cnt] > p0) ++cnt;
+      if (cnt == 0) break;
+      diag_lu_kernel<S><<<cnt, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0, tau, d.d_flag);
+      count_launch(1);
+      const int rest = std::max(0, L.max_rest - p0 - 1);
+      const int tiles = (rest + 127) / 128;
+      if (tiles > 0) {
+        dim3 g1(2 * tiles, cnt);
+        panel_trsm_kernel<S><<<g1, 128, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0);
+        const int tpd = (rest + 63) / 64;
+        dim3 g2(tpd * tpd, cnt);
+        gemm_update_kernel<S><<<g2, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0);
+        count_launch(2);
+      }
+    }
+  }
+  return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t solve_t(MFHandle& h, cudaStream_t st) {
+  MFDevice& d = h.dev;
+  S* x = (S*)d.d_x;
+  const S* arena = (const S*)d.arena;
+  for (size_t lv = 0; lv < d.levels.size(); ++lv) {
+    const MFLevel& L = d.levels[lv];
+    const int cnt = (int)L.nodes_by_k.size();
+    fwd_trsv_kernel<S><<<cnt, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x);
+    count_launch(1);
+    if (L.max_u > 0) {
+      dim3 g(std::max(1, std::min(64, (L.max_u + 255) / 256)), cnt);
+      fwd_gemv_kernel<S><<<g, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x);
+      count_launch(1);
+    }
+  }
+  for (int lv = (int)d.levels.size() - 1; lv >= 0; --lv) {
+    const MFLevel& L = d.levels[lv];
+    const int cnt = (int)L.nodes_by_k.size();
+    if (L.max_u > 0) {
+      dim3 g(std::max(1, std::min(64, (L.max_k + 255) / 256)), cnt);
+      bwd_gemv_kernel<S><<<g, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x);
+      count_launch(1);
+    }
+    bwd_trsv_kernel<S><<<cnt, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x);
+    count_launch(1);
+  }
+  return cudaGetLastError();
+}
+
+template <typename S, typename T>
+cudaError_t solve_io(MFHandle& h, const void* b, void* xout, cudaStream_t st) {
+  const int64_t n = h.sym.n;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  permute_in_kernel<S, T><<<blocks, 256, 0, st>>>(n, h.dev.d_perm, (const T*)b, (S*)h.dev.d_x);
+  cudaError_t e = solve_t<S>(h, st);
+  if (e != cudaSuccess) return e;
+  permute_out_kernel<S, T><<<blocks, 256, 0, st>>>(n, h.dev.d_perm, (const S*)h.dev.d_x, (T*)xout);
+  count_launch(2);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t mf_factor(MFHandle& h, int dtype, const void* vals, double tau, cudaStream_t st) {
+  cudaError_t e = setup_device(h, dtype);
+  if (e != cudaSuccess) return e;
+  switch (dtype) {
+    case SUCEM_F32: e = factor_t<float>(h, vals, tau, st); break;
+    case SUCEM_F64: e = factor_t<double>(h, vals, tau, st); break;
+    case SUCEM_C64: e = factor_t<float2>(h, vals, tau, st); break;
+    case SUCEM_C128: e = factor_t<double2>(h, vals, tau, st); break;
+    default: return cudaErrorInvalidValue;
+  }
+  h.dev.factored = e == cudaSuccess;
+  return e;
+}
+
+// b and x may have the factor's precision or the matching double precision
+cudaError_t mf_solve(MFHandle& h, int io_dtype, const void* b, void* x, cudaStream_t st) {
+  if (!h.dev.factored) return cudaErrorNotReady;
+  const int f = h.dev.dtype;
+  if (f == SUCEM_F32 && io_dtype == SUCEM_F32) return solve_io<float, float>(h, b, x, st);
+  if (f == SUCEM_F32 && io_dtype == SUCEM_F64) return solve_io<float, double>(h, b, x, st);
+  if (f == SUCEM_F64 && io_dtype == SUCEM_F64) return solve_io<double, double>(h, b, x, st);
+  if (f == SUCEM_C64 && io_dtype == SUCEM_C64) return solve_io<float2, float2>(h, b, x, st);
+  if (f == SUCEM_C64 && io_dtype == SUCEM_C128) return solve_io<float2, double2>(h, b, x, st);
+  if (f == SUCEM_C128 && io_dtype == SUCEM_C128) return solve_io<double2, double2>(h, b, x, st);
+  return cudaErrorInvalidValue;
+}
+
+int mf_perturbed(MFHandle& h) {
+  int v = 0;
+  if (h.dev.d_flag) cudaMemcpy(&v, h.dev.d_flag, sizeof(int), cudaMemcpyDeviceToHost);
+  return v;
+}
+
+void mf_free(MFHandle& h) { free_dev(h.dev); }
+
+MFHandle* mf_new() { return new MFHandle(); }
+void mf_delete(MFHandle* h) {
+  if (!h) return;
+  free_dev(h->dev);
+  delete h;
+}
+MFSymbolic& mf_sym(MFHandle* h) { return h->sym; }
+
+}  // namespace sucem

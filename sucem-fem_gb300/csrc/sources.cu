@@ -20,6 +20,7 @@
 namespace sucem {
 int fail(const std::string& msg, int code);
 int cuda_fail(cudaError_t e, const char* where);
+void count_launch(int k);
 
 namespace {
 
@@ -146,5 +147,6 @@ extern "C" int sucem_point_sources(const sucem_space* sp, const double* pts,
     evaluate_kernel<20><<<eb, threads, 0, s>>>(d->nt, d->cells, d->xyz, pts, values, npts, cells_out,
                                                contrib);
   e = cudaGetLastError();
+  count_launch(2);
   return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_point_sources");
 }

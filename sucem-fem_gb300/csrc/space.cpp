@@ -237,6 +237,21 @@ std::string build_space(Space& s, const double* coords, int64_t nv, const int64_
       std::copy(ent_cols.begin() + ent_col_ptr[k], ent_cols.begin() + ent_col_ptr[k + 1],
                 s.indices.begin() + s.indptr[dpe * k + j]);
 
+  // ---- DOF locations (used by the nested-dissection ordering) ----
+  s.dof_xyz.assign(s.n * 3, 0.0);
+  for (int64_t e = 0; e < s.ne; ++e)
+    for (int j = 0; j < dpe; ++j)
+      for (int d = 0; d < 3; ++d)
+        s.dof_xyz[(dpe * e + j) * 3 + d] =
+            0.5 * (s.coords[s.edges[2 * e] * 3 + d] + s.coords[s.edges[2 * e + 1] * 3 + d]);
+  if (order == 2)
+    for (int64_t f = 0; f < s.nf; ++f)
+      for (int j = 0; j < 2; ++j)
+        for (int d = 0; d < 3; ++d)
+          s.dof_xyz[(2 * s.ne + 2 * f + j) * 3 + d] =
+              (s.coords[s.faces[3 * f] * 3 + d] + s.coords[s.faces[3 * f + 1] * 3 + d] +
+               s.coords[s.faces[3 * f + 2] * 3 + d]) / 3.0;
+
   // ---- boundary DOFs (closure of the exterior facets) ----
   {
     std::vector<uint8_t> mark(s.n, 0);

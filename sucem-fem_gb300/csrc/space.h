@@ -48,6 +48,7 @@ struct Space {
   int rec_bytes = 8;
 
   std::vector<int32_t> boundary_dofs;  // closure of the exterior facets, sorted
+  std::vector<double> dof_xyz;         // n*3: edge midpoint / face centroid of each DOF
 
   DeviceSpace* dev = nullptr;
 };

@@ -13,7 +13,7 @@ SUCEM_OK = 0
 ERR_ARG, ERR_MEMORY, ERR_CUDA, ERR_STATE, ERR_NOCONV, ERR_BREAKDOWN = -1, -2, -3, -4, -5, -6
 
 COPY = dict(indptr=0, indices=1, cell_dofs=2, boundary_dofs=3, edges=4, faces=5, cells=6, ext_mask=7,
-            cell_edges=8, cell_faces=9)
+            cell_edges=8, cell_faces=9, dof_xyz=10)
 DEV = dict(indptr=0, indices=1, cell_dofs=2, boundary_dofs=3)
 
 _lib = None
@@ -34,6 +34,7 @@ class SolverError(RuntimeError):
 _SIGS = [
     ("sucem_version", ctypes.c_int, []),
     ("sucem_last_error", ctypes.c_char_p, []),
+    ("sucem_launch_count", ctypes.c_longlong, []),
     ("sucem_space_create", ctypes.c_int,
      [c_vp, ctypes.c_int64, c_vp, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(c_vp)]),
     ("sucem_space_destroy", None, [c_vp]),

@@ -97,6 +97,10 @@ class FunctionSpace:
         return self._copy("ext_mask", self.nt, np.uint8)
 
     @property
+    def dof_xyz(self):
+        return self._copy("dof_xyz", (self.n, 3), np.float64)
+
+    @property
     def cell_edges(self):
         return self._copy("cell_edges", (self.nt, 6), np.int32)
 

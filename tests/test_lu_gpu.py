@@ -1,0 +1,86 @@
+"""GPU multifrontal LU against scipy's sparse direct solve (the oracle side
+of the reference's UMFPACK/LUSolver calls).  Tolerances: relative residual
+of the single-precision factor solve < 1e-4 (one solve) and < 1e-12 after
+double-precision refinement; double-precision factor < 1e-11."""
+import numpy as np
+import pytest
+import scipy.sparse.linalg as spl
+
+from oracle import fem
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(order, n=(4, 3, 3), driven=True):
+    coords, cells = fem.box_mesh(1.0, 0.8, 0.6, *n)
+    rng = np.random.default_rng(1)
+    eps = rng.uniform(1, 4, len(cells))
+    A = fem.assemble(coords, cells, order, eps_r=eps)
+    if driven:
+        L = fem.lhs_matrix(A.S, A.T, A.B, 299792458 / 0.7)
+    else:
+        L = (A.S - 1.0 * A.T)
+    return coords, cells, L.tocsr(), A
+
+
+def _space(coords, cells, order):
+    from sucemfem.mesh import Mesh
+    from sucemfem.space import FunctionSpace
+    return FunctionSpace(Mesh(coords, cells), order=order)
+
+
+def _values_on_pattern(V, M):
+    """Values of scipy matrix M on the space's CSR pattern."""
+    M = M.tocsr()
+    out = np.zeros(V.nnz, dtype=M.dtype)
+    rows = np.repeat(np.arange(V.n), np.diff(V.indptr))
+    out[:] = np.asarray(M[rows, V.indices]).ravel()
+    return out
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("dtype", ["c64", "c128"])
+@pytest.mark.parametrize("ordering", ["cells", "dofs"])
+def test_lu_driven(order, dtype, ordering):
+    import torch
+    from sucemfem import _device
+    from sucemfem.lu import SparseLU
+    coords, cells, L, _ = _problem(order)
+    V = _space(coords, cells, order)
+    vals = _values_on_pattern(V, L)
+    if ordering == "cells":
+        lu = SparseLU(V.indptr, V.indices, leaf_size=32,
+                      cells=(V.cell_dofs, coords[V.cells].mean(1)))
+    else:
+        lu = SparseLU(V.indptr, V.indices, V.dof_xyz, leaf_size=32)
+    assert sorted(lu.perm()) == list(range(V.n))
+    tdt = torch.complex64 if dtype == "c64" else torch.complex128
+    dv = torch.as_tensor(vals, device=_device.device()).to(tdt)
+    lu.factor(dv, dtype)
+    b = np.random.default_rng(0).standard_normal(V.n) + 1j * np.random.default_rng(1).standard_normal(V.n)
+    db = torch.as_tensor(b, device=_device.device())
+    x = lu.solve(db if dtype == "c128" else db).cpu().numpy()
+    res = np.linalg.norm(L @ x - b) / np.linalg.norm(b)
+    assert res < (1e-4 if dtype == "c64" else 1e-11), res
+    xr = spl.spsolve(L.tocsc(), b)
+    assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < (1e-3 if dtype == "c64" else 1e-9)
+    assert lu.perturbed() == 0
+
+
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_lu_real_indefinite(dtype):
+    import torch
+    from sucemfem import _device
+    from sucemfem.lu import SparseLU
+    coords, cells = fem.box_mesh(1.0, 0.5, 0.75, 4, 2, 3)
+    A = fem.assemble(coords, cells, 1, with_abc=False)
+    V = _space(coords, cells, 1)
+    M = (A.S - 1.3 * A.T).tocsr()
+    vals = M.data.copy()  # oracle pattern == space pattern (bit-exact)
+    lu = SparseLU(V.indptr, V.indices, leaf_size=16, cells=(V.cell_dofs, coords[V.cells].mean(1)))
+    tdt = torch.float32 if dtype == "f32" else torch.float64
+    lu.factor(torch.as_tensor(vals, device=_device.device()).to(tdt), dtype)
+    b = np.random.default_rng(0).standard_normal(V.n)
+    x = lu.solve(torch.as_tensor(b, device=_device.device())).cpu().numpy()
+    res = np.linalg.norm(M @ x - b) / np.linalg.norm(b)
+    assert res < (1e-3 if dtype == "f32" else 1e-11), res

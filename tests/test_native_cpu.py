@@ -16,7 +16,8 @@ HEADER = os.path.join(ROOT, "include", "sucem_gb300.h")
 
 def _declared():
     txt = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+(sucem_\w+)\s*\(", txt, re.M)))
+    return sorted(set(re.findall(
+        r"^\s*(?:int|void|const char\*|int64_t|long long)\s+(sucem_\w+)\s*\(", txt, re.M)))
 
 
 def test_library_exports_every_declared_symbol():
