@@ -144,6 +144,20 @@ int sucem_compact_fill(const sucem_space* sp, int dtype, const void* vals,
                        const int32_t* out_indptr, int32_t* out_indices, void* out_vals,
                        void* stream);
 
+/* Allocation-free form of sucem_compact_count; no counterpart in the
+ * reference.  For callers that cannot allocate device memory when they need
+ * the compaction (for example a serving loop that reserved its whole HBM
+ * budget for resident problems, or a host whose device memory belongs to
+ * another allocator): the per-row count scratch is a fixed array inside the
+ * library (4 MiB, held on every GPU that loads the library until exit), so
+ * no work buffer is passed and nothing is allocated.  Limit: at most 2^20
+ * rows; larger matrices get SUCEM_ERR_ARG with a message.  The first call on
+ * a device looks up the array's device address (make that first call before
+ * any stream capture).  Every call shares the one array: calls that overlap
+ * on the GPU (other streams, other threads) race and must be serialised. */
+int sucem_compact_count_noalloc(const sucem_space* sp, int dtype, const void* vals,
+                                int32_t* out_indptr, void* stream);
+
 /* Point current sources: locate each point (lowest-index cell whose closure
  * contains it) and evaluate N_i(p) . value for the ndof basis functions of
  * that cell.  Replaces calc_pointsource_contrib

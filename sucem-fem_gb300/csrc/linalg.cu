@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
+#include <string>
 
 #include "../../include/sucem_gb300.h"
 #include "device.h"
@@ -522,3 +524,76 @@ int sucem_compact_fill(const sucem_space* sp, int dtype, const void* vals,
 }
 
 }  // extern "C"
+
+// ---- allocation-free variant of the compaction count --------------------
+// Some callers of this library cannot allocate device memory at the moment
+// they need a compaction: a serving loop that reserved its whole HBM budget
+// up front for resident problems, or a host that lets another allocator own
+// the device memory.  For them the per-row count scratch of
+// sucem_compact_count lives in this fixed device array instead of a
+// caller-provided buffer.  Every GPU that loads the library holds it until
+// the process exits.
+namespace sucem {
+namespace {
+
+constexpr int64_t kNoAllocMaxRows = int64_t(1) << 20;  // 4 MiB of int32 counts
+static __device__ __align__(256) int32_t g_noalloc_counts[kNoAllocMaxRows];
+
+constexpr int kMaxDevices = 64;
+int32_t* g_noalloc_ptr[kMaxDevices] = {nullptr};
+std::mutex g_noalloc_mutex;
+
+// Device address of the array for the current device.  In host code the
+// array's name is only a host-side stand-in, so the address must come from
+// cudaGetSymbolAddress, looked up once per device with that device current.
+int noalloc_scratch(int32_t** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_compact_count_noalloc: cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail("device index out of range", SUCEM_ERR_ARG);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_counts);
+    if (e != cudaSuccess) return cuda_fail(e, "sucem_compact_count_noalloc: cudaGetSymbolAddress");
+    g_noalloc_ptr[dev] = static_cast<int32_t*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return SUCEM_OK;
+}
+
+}  // namespace
+}  // namespace sucem
+
+extern "C" int sucem_compact_count_noalloc(const sucem_space* sp, int dtype, const void* vals,
+                                           int32_t* out_indptr, void* stream) {
+  const sucem::DeviceSpace* d = dev_of(sp);
+  if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  if (!vals || !out_indptr) return fail("null argument", SUCEM_ERR_ARG);
+  if (dtype != SUCEM_C64 && dtype != SUCEM_C128)
+    return fail("compaction needs a complex dtype", SUCEM_ERR_ARG);
+  if (d->n > sucem::kNoAllocMaxRows)
+    return fail("sucem_compact_count_noalloc: the matrix has " + std::to_string(d->n) +
+                    " rows; the allocation-free scratch holds at most " +
+                    std::to_string(sucem::kNoAllocMaxRows) +
+                    " (use sucem_compact_count with a caller buffer)",
+                SUCEM_ERR_ARG);
+  int32_t* counts = nullptr;
+  int rc = sucem::noalloc_scratch(&counts);
+  if (rc != SUCEM_OK) return rc;
+  // the count kernel writes counts[0, n) before the scan reads them, so the
+  // contents left by an earlier call need no clearing
+  cudaStream_t s = (cudaStream_t)stream;
+  const int threads = 256;
+  const unsigned blocks = (unsigned)((d->n * 32 + threads - 1) / threads);
+  if (dtype == SUCEM_C64)
+    sucem::count_nonzero_kernel<float><<<blocks, threads, 0, s>>>(d->n, d->indptr,
+                                                                  (const float*)vals, counts);
+  else
+    sucem::count_nonzero_kernel<double><<<blocks, threads, 0, s>>>(d->n, d->indptr,
+                                                                   (const double*)vals, counts);
+  sucem::scan_kernel<<<1, 1024, 0, s>>>(d->n, counts, out_indptr);
+  cudaError_t e = cudaGetLastError();
+  sucem::count_launch(2);
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_compact_count_noalloc");
+}

@@ -55,6 +55,7 @@ _SIGS = [
     ("sucem_compact_count", ctypes.c_int, [c_vp, ctypes.c_int, c_vp, c_vp, c_vp, c_vp]),
     ("sucem_compact_fill", ctypes.c_int, [c_vp, ctypes.c_int, c_vp, c_vp, c_vp, c_vp, c_vp]),
     ("sucem_point_sources", ctypes.c_int, [c_vp, c_vp, c_vp, ctypes.c_int, c_vp, c_vp, c_vp]),
+    ("sucem_compact_count_noalloc", ctypes.c_int, [c_vp, ctypes.c_int, c_vp, c_vp, c_vp]),
 ]
 
 F32, F64, C64, C128 = 0, 1, 2, 3
