@@ -188,6 +188,23 @@ int sucem_vec_dot(int64_t n, int dtype, const void* x, const void* y, int conj, 
 int sucem_vec_convert(int64_t count, int dst_real_bytes, void* dst, int src_real_bytes,
                       const void* src, void* stream);
 
+/* Segmented (batched) double vectors for the batched Lanczos of
+ * DefaultEigenSolver.solve_problem (EMVectorWaveEigenproblem.py:61-105,
+ * ARPACK's inner products and updates): independent problems are stacked,
+ * segment s covering [seg_ptr[s], seg_ptr[s+1]).
+ * seg_dot: out[j*nseg + s] = X_j . y over segment s, X_j = X + j*ldx.
+ * seg_axpy: y_i = b[s] y_i + sum_j a[j*nseg + s] X_j,i (b NULL = 1);
+ * seg_of: int32[n] segment of every entry. */
+int sucem_seg_dot(int nseg, const int64_t* seg_ptr, const double* X, int64_t ldx, int nvec,
+                  const double* y, double* out, void* stream);
+/* dst[i] = src[idx[i]] (elements of 4, 8 or 16 bytes): extracts the values
+ * of a sub-matrix (e.g. the PEC-free DOFs) from a CSR value array. */
+int sucem_gather(int64_t m, int elem_bytes, const int64_t* idx, const void* src, void* dst,
+                 void* stream);
+int sucem_seg_axpy(int nseg, const int64_t* seg_ptr, int64_t n, const int32_t* seg_of,
+                   const double* X, int64_t ldx, int nvec, const double* a, const double* b,
+                   double* y, void* stream);
+
 /* ---- multifrontal sparse LU (GPU) ----
  * Replaces the reference's direct solves: dolfin.LUSolver(S - sigma*M)
  * (sucemfem/ProblemConfigurations/EMVectorWaveEigenproblem.py:76-85),

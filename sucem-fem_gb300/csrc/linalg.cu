@@ -292,6 +292,50 @@ __global__ void dot_final_kernel(int nparts, const double2* __restrict__ partial
   }
 }
 
+// segmented dot products of real double vectors: out[s] = sum_{i in seg s} x_i y_i
+// one block per segment, fixed-order reduction
+__global__ void seg_dot_kernel(int nseg, const int64_t* __restrict__ seg, const double* __restrict__ x,
+                               const double* __restrict__ y, int64_t ldx, int nvec,
+                               double* __restrict__ out) {
+  // blockIdx.x = segment, blockIdx.y = vector index j: out[j*nseg + s] = x_j . y
+  __shared__ double sh[32];
+  const int s = blockIdx.x, j = blockIdx.y;
+  if (s >= nseg || j >= nvec) return;
+  const double* xj = x + (int64_t)j * ldx;
+  double a = 0;
+  for (int64_t i = seg[s] + threadIdx.x; i < seg[s + 1]; i += blockDim.x) a += xj[i] * y[i];
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(~0u, a, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = a;
+  __syncthreads();
+  if (w == 0) {
+    a = l < (int)(blockDim.x >> 5) ? sh[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(~0u, a, o);
+    if (l == 0) out[(int64_t)j * nseg + s] = a;
+  }
+}
+
+// y_i = b[s] * y_i + sum_j a[j*nseg + s] * x_j,i for i in segment s
+__global__ void seg_axpy_kernel(int nseg, const int64_t* __restrict__ seg, int64_t n,
+                                const int32_t* __restrict__ seg_of, const double* __restrict__ x,
+                                int64_t ldx, int nvec, const double* __restrict__ a,
+                                const double* __restrict__ b, double* __restrict__ y) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int s = seg_of[i];
+  double v = b ? b[s] * y[i] : y[i];
+  for (int j = 0; j < nvec; ++j) v += a[(int64_t)j * nseg + s] * x[(int64_t)j * ldx + i];
+  y[i] = v;
+}
+
+// dst[i] = src[idx[i]] for 8-byte or 16-byte elements
+template <typename T>
+__global__ void gather_kernel(int64_t m, const int64_t* __restrict__ idx, const T* __restrict__ src,
+                              T* __restrict__ dst) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) dst[i] = src[idx[i]];
+}
+
 template <typename D, typename S>
 __global__ void convert_kernel(int64_t m, const S* __restrict__ src, D* __restrict__ dst) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -430,6 +474,50 @@ int sucem_vec_dot(int64_t n, int dtype, const void* x, const void* y, int conj, 
                                  (cudaStream_t)stream);
   sucem::count_launch(2);
   return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_vec_dot");
+}
+
+int sucem_gather(int64_t m, int elem_bytes, const int64_t* idx, const void* src, void* dst,
+                 void* stream) {
+  if (!idx || !src || !dst) return fail("null argument", SUCEM_ERR_ARG);
+  if (m == 0) return SUCEM_OK;
+  const unsigned blocks = (unsigned)((m + 255) / 256);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (elem_bytes == 4)
+    sucem::gather_kernel<float><<<blocks, 256, 0, s>>>(m, idx, (const float*)src, (float*)dst);
+  else if (elem_bytes == 8)
+    sucem::gather_kernel<double><<<blocks, 256, 0, s>>>(m, idx, (const double*)src, (double*)dst);
+  else if (elem_bytes == 16)
+    sucem::gather_kernel<double2><<<blocks, 256, 0, s>>>(m, idx, (const double2*)src, (double2*)dst);
+  else
+    return fail("element size must be 4, 8 or 16 bytes", SUCEM_ERR_ARG);
+  cudaError_t e = cudaGetLastError();
+  sucem::count_launch(1);
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_gather");
+}
+
+int sucem_seg_dot(int nseg, const int64_t* seg_ptr, const double* X, int64_t ldx, int nvec,
+                  const double* y, double* out, void* stream) {
+  if (!seg_ptr || !X || !y || !out) return fail("null argument", SUCEM_ERR_ARG);
+  if (nseg <= 0 || nvec <= 0) return SUCEM_OK;
+  if (nvec > 65535) return fail("too many vectors", SUCEM_ERR_ARG);
+  dim3 grid((unsigned)nseg, (unsigned)nvec);
+  sucem::seg_dot_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(nseg, seg_ptr, X, y, ldx, nvec, out);
+  cudaError_t e = cudaGetLastError();
+  sucem::count_launch(1);
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_seg_dot");
+}
+
+int sucem_seg_axpy(int nseg, const int64_t* seg_ptr, int64_t n, const int32_t* seg_of,
+                   const double* X, int64_t ldx, int nvec, const double* a, const double* b,
+                   double* y, void* stream) {
+  if (!seg_ptr || !seg_of || !y || (nvec > 0 && (!X || !a))) return fail("null argument", SUCEM_ERR_ARG);
+  if (n == 0) return SUCEM_OK;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  sucem::seg_axpy_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(nseg, seg_ptr, n, seg_of, X, ldx,
+                                                                   nvec, a, b, y);
+  cudaError_t e = cudaGetLastError();
+  sucem::count_launch(1);
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_seg_axpy");
 }
 
 int sucem_vec_convert(int64_t count, int dst_real_bytes, void* dst, int src_real_bytes,
