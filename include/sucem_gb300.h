@@ -211,7 +211,8 @@ int sucem_seg_axpy(int nseg, const int64_t* seg_ptr, int64_t n, const int32_t* s
  * UMFPACKSolver / spsolve (sucemfem/Utilities/LinalgSolvers.py:262-277) and,
  * used as a preconditioner, spilu (LinalgSolvers.py:118-121).
  * analyse: host CSR pattern with symmetric structure (sorted columns) and
- * n*3 DOF coordinates; builds a nested-dissection ordering and the front
+ * n*3 DOF coordinates (NULL: breadth-first-distance pseudo-coordinates of
+ * the matrix graph); builds a nested-dissection ordering and the front
  * structure on the host.  factor: device values in CSR order (dtype
  * SUCEM_F32/F64/C64/C128), no pivoting; pivots below pivot_tol*max|a_ij|
  * are replaced (static pivoting, count via sucem_lu_perturbed).  solve:

@@ -50,7 +50,7 @@ extern "C" {
 
 int sucem_lu_analyse(int64_t n, const int32_t* indptr, const int32_t* indices, const double* xyz,
                      int leaf_size, sucem_lu** out) {
-  if (!indptr || !indices || !xyz || !out) return fail("null argument", SUCEM_ERR_ARG);
+  if (!indptr || !indices || !out) return fail("null argument", SUCEM_ERR_ARG);
   *out = nullptr;
   sucem_lu* lu = new (std::nothrow) sucem_lu();
   if (!lu) return fail("out of host memory", SUCEM_ERR_MEMORY);

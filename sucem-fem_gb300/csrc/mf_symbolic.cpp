@@ -214,9 +214,88 @@ std::string mf_analyse_cells(MFSymbolic& sym, int64_t n, const int32_t* indptr,
   return mf_finish(sym, n, indptr, indices, std::move(store.order), std::move(store.nodes));
 }
 
+// Pseudo-coordinates for a matrix without geometry: breadth-first distances
+// from three far-apart vertices of each connected component (components
+// are laid out one after another along the first axis).
+static void graph_coordinates(int64_t n, const int32_t* indptr, const int32_t* indices,
+                              std::vector<double>& xyz) {
+  xyz.assign(n * 3, 0.0);
+  std::vector<int64_t> dist(n, -1), comp_nodes, queue;
+  std::vector<char> seen(n, 0);
+  double offset = 0;
+  auto bfs = [&](int64_t src, std::vector<int64_t>& d) {
+    for (int64_t v : comp_nodes) d[v] = -1;
+    queue.clear();
+    queue.push_back(src);
+    d[src] = 0;
+    int64_t far = src;
+    for (size_t h = 0; h < queue.size(); ++h) {
+      const int64_t v = queue[h];
+      if (d[v] > d[far]) far = v;
+      for (int32_t q = indptr[v]; q < indptr[v + 1]; ++q) {
+        const int64_t w = indices[q];
+        if (d[w] < 0) {
+          d[w] = d[v] + 1;
+          queue.push_back(w);
+        }
+      }
+    }
+    return far;
+  };
+  for (int64_t s = 0; s < n; ++s) {
+    if (seen[s]) continue;
+    // collect the component
+    comp_nodes.clear();
+    comp_nodes.push_back(s);
+    seen[s] = 1;
+    for (size_t h = 0; h < comp_nodes.size(); ++h) {
+      const int64_t v = comp_nodes[h];
+      for (int32_t q = indptr[v]; q < indptr[v + 1]; ++q)
+        if (!seen[indices[q]]) {
+          seen[indices[q]] = 1;
+          comp_nodes.push_back(indices[q]);
+        }
+    }
+    std::vector<int64_t>& d = dist;
+    const int64_t a = bfs(s, d);
+    const int64_t b = bfs(a, d);
+    std::vector<int64_t> d1(comp_nodes.size());
+    for (size_t i = 0; i < comp_nodes.size(); ++i) d1[i] = d[comp_nodes[i]];
+    const int64_t c = bfs(b, d);
+    std::vector<int64_t> d2(comp_nodes.size());
+    int64_t best = s;
+    int64_t bestv = -1;
+    for (size_t i = 0; i < comp_nodes.size(); ++i) {
+      d2[i] = d[comp_nodes[i]];
+      const int64_t mv = std::min(d1[i], d2[i]);
+      if (mv > bestv) {
+        bestv = mv;
+        best = comp_nodes[i];
+      }
+    }
+    (void)c;
+    bfs(best, d);
+    double span = 0;
+    for (size_t i = 0; i < comp_nodes.size(); ++i) {
+      const int64_t v = comp_nodes[i];
+      xyz[3 * v] = offset + (double)d1[i];
+      xyz[3 * v + 1] = (double)d2[i];
+      xyz[3 * v + 2] = (double)d[v];
+      span = std::max(span, (double)d1[i]);
+    }
+    offset += span + 2.0;
+  }
+}
+
 std::string mf_analyse(MFSymbolic& sym, int64_t n, const int32_t* indptr, const int32_t* indices,
-                       const double* xyz, int leaf_size) {
+                       const double* xyz_in, int leaf_size) {
   if (n <= 0) return "empty matrix";
+  std::vector<double> pseudo;
+  const double* xyz = xyz_in;
+  if (!xyz) {
+    graph_coordinates(n, indptr, indices, pseudo);
+    xyz = pseudo.data();
+  }
   ND nd;
   nd.indptr = indptr;
   nd.indices = indices;

@@ -44,7 +44,8 @@ class SparseLU:
             call("sucem_lu_analyse_cells", self.n, ptr(ip), ptr(ix), len(cd), cd.shape[1], ptr(cd),
                  ptr(cx), int(leaf_size), ctypes.byref(h))
         else:
-            xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(self.n, 3)
+            if xyz is not None:
+                xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(self.n, 3)
             call("sucem_lu_analyse", self.n, ptr(ip), ptr(ix), ptr(xyz), int(leaf_size),
                  ctypes.byref(h))
         self._h = h
