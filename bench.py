@@ -380,8 +380,38 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_kernel_case(args):
+    """Small single-kernel cases for profiling (no JSON contract): 'factor'
+    runs warmup+steps complex64 LU factorisations of the driven matrix,
+    'assemble' the fused FP32 assembly, at --cubes^3 and --order."""
+    import torch
+    from sucemfem import _device
+    from sucemfem._native import call, ptr
+    from sucemfem.solvers import lu_for_space
+    from sucemfem.space import FunctionSpace
+    dev = _device.device()
+    mesh, eps, k0 = workload(args.cubes)
+    V = FunctionSpace(mesh, order=args.order)
+    h = V.upload()
+    d_eps = torch.as_tensor(eps, dtype=torch.float32, device=dev)
+    A = torch.empty(V.nnz, dtype=torch.complex64, device=dev)
+    sp = _device.stream_ptr()
+    lu = lu_for_space(V) if args.only == "factor" else None
+    for _ in range(args.warmup + args.steps):
+        call("sucem_assemble_helmholtz", h, 4, ptr(d_eps), None, float(k0), ptr(A), sp)
+        if lu is not None:
+            lu.factor(A, "c64")
+    torch.cuda.synchronize()
+    print(json.dumps({"case": args.only, "cubes": args.cubes, "order": args.order, "n": V.n,
+                      "nnz": V.nnz, "runs": args.warmup + args.steps}))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--only", default="solve", choices=["solve", "factor", "assemble"],
+                    help="profiling cases: factor / assemble at --cubes, --order")
+    ap.add_argument("--cubes", type=int, default=N_CUBES)
+    ap.add_argument("--order", type=int, default=ORDER)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
@@ -395,6 +425,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.only != "solve":
+        run_kernel_case(args)
     else:
         run_gpu(args)
 

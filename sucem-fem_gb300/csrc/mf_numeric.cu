@@ -322,9 +322,35 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(const int32_t* __restr
 }
 
 // ---- solve kernels (x in the new ordering) ----
+// acc - sum_{j in [lo,hi)} row[j] * y[j] over the lanes of a warp, four
+// independent partial sums so four loads per lane are in flight; the result
+// is complete in lane 0.  IDX: y is gathered through idx (y[idx[j]]).
+template <typename S, bool IDX>
+__device__ __forceinline__ S warp_row_dot(const S* __restrict__ row, const S* __restrict__ y,
+                                          const int32_t* __restrict__ idx, int lo, int hi,
+                                          int lane) {
+  S a0 = s_zero(S()), a1 = s_zero(S()), a2 = s_zero(S()), a3 = s_zero(S());
+  int j = lo + lane;
+  for (; j + 96 < hi; j += 128) {
+    const S r0 = row[j], r1 = row[j + 32], r2 = row[j + 64], r3 = row[j + 96];
+    const S y0 = IDX ? y[idx[j]] : y[j];
+    const S y1 = IDX ? y[idx[j + 32]] : y[j + 32];
+    const S y2 = IDX ? y[idx[j + 64]] : y[j + 64];
+    const S y3 = IDX ? y[idx[j + 96]] : y[j + 96];
+    a0 = s_fms(a0, r0, y0);
+    a1 = s_fms(a1, r1, y1);
+    a2 = s_fms(a2, r2, y2);
+    a3 = s_fms(a3, r3, y3);
+  }
+  for (; j < hi; j += 32) a0 = s_fms(a0, row[j], IDX ? y[idx[j]] : y[j]);
+  S acc = s_add(s_add(a0, a1), s_add(a2, a3));
+  for (int o = 16; o > 0; o >>= 1) acc = s_add(acc, s_shfl_down(acc, o));
+  return acc;
+}
+
 // forward: y_V = L11^-1 y_V (unit lower), one block per front
 template <typename S>
-__global__ void fwd_trsv_kernel(const int32_t* __restrict__ list, int count,
+__global__ void __launch_bounds__(1024) fwd_trsv_kernel(const int32_t* __restrict__ list, int count,
                                 const DNode* __restrict__ nodes, const S* __restrict__ arena,
                                 S* __restrict__ x) {
   const int fi = blockIdx.x;
@@ -337,9 +363,7 @@ __global__ void fwd_trsv_kernel(const int32_t* __restrict__ list, int count,
     // subtract the contributions of the solved rows [0, b0) from rows of this block
     if (b0 > 0) {
       for (int r = b0 + warp; r < min(b0 + 32, nd.k); r += nw) {
-        S acc = s_zero(S());
-        for (int j = lane; j < b0; j += 32) acc = s_fms(acc, F[(int64_t)r * nd.f + j], y[j]);
-        for (int o = 16; o > 0; o >>= 1) acc = s_add(acc, s_shfl_down(acc, o));
+        const S acc = warp_row_dot<S, false>(F + (int64_t)r * nd.f, y, nullptr, 0, b0, lane);
         if (lane == 0) y[r] = s_add(y[r], acc);
       }
       __syncthreads();
@@ -372,9 +396,7 @@ __global__ void fwd_gemv_kernel(const int32_t* __restrict__ list, int count,
   const S* y = x + nd.start;
   for (int r = warp; r < u; r += nwarps) {
     const S* row = arena + nd.off + (int64_t)(nd.k + r) * nd.f;
-    S acc = s_zero(S());
-    for (int j = lane; j < nd.k; j += 32) acc = s_fms(acc, row[j], y[j]);
-    for (int o = 16; o > 0; o >>= 1) acc = s_add(acc, s_shfl_down(acc, o));
+    const S acc = warp_row_dot<S, false>(row, y, nullptr, 0, nd.k, lane);
     if (lane == 0) s_atomic_sub(&x[U[nd.u_off + r]], s_fms(s_zero(S()), acc, s_real(S(), 1.0)));
   }
 }
@@ -394,16 +416,14 @@ __global__ void bwd_gemv_kernel(const int32_t* __restrict__ list, int count,
   const int32_t* Ui = U + nd.u_off;
   for (int r = warp; r < nd.k; r += nwarps) {
     const S* row = arena + nd.off + (int64_t)r * nd.f + nd.k;
-    S acc = s_zero(S());
-    for (int j = lane; j < u; j += 32) acc = s_fms(acc, row[j], x[Ui[j]]);
-    for (int o = 16; o > 0; o >>= 1) acc = s_add(acc, s_shfl_down(acc, o));
+    const S acc = warp_row_dot<S, true>(row, x, Ui, 0, u, lane);
     if (lane == 0) x[nd.start + r] = s_add(x[nd.start + r], acc);
   }
 }
 
 // backward: x_V = U11^-1 y_V (upper, non-unit), one block per front
 template <typename S>
-__global__ void bwd_trsv_kernel(const int32_t* __restrict__ list, int count,
+__global__ void __launch_bounds__(1024) bwd_trsv_kernel(const int32_t* __restrict__ list, int count,
                                 const DNode* __restrict__ nodes, const S* __restrict__ arena,
                                 S* __restrict__ x) {
   const int fi = blockIdx.x;
@@ -417,9 +437,7 @@ __global__ void bwd_trsv_kernel(const int32_t* __restrict__ list, int count,
     const int b0 = bi * 32, b1 = min(b0 + 32, nd.k);
     if (b1 < nd.k) {
       for (int r = b0 + warp; r < b1; r += nw) {
-        S acc = s_zero(S());
-        for (int j = b1 + lane; j < nd.k; j += 32) acc = s_fms(acc, F[(int64_t)r * nd.f + j], y[j]);
-        for (int o = 16; o > 0; o >>= 1) acc = s_add(acc, s_shfl_down(acc, o));
+        const S acc = warp_row_dot<S, false>(F + (int64_t)r * nd.f, y, nullptr, b1, nd.k, lane);
         if (lane == 0) y[r] = s_add(y[r], acc);
       }
       __syncthreads();
@@ -648,10 +666,11 @@ cudaError_t solve_t(MFHandle& h, cudaStream_t st) {
   for (size_t lv = 0; lv < d.levels.size(); ++lv) {
     const MFLevel& L = d.levels[lv];
     const int cnt = (int)L.nodes_by_k.size();
-    fwd_trsv_kernel<S><<<cnt, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x);
+    fwd_trsv_kernel<S><<<cnt, 1024, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x);
     count_launch(1);
     if (L.max_u > 0) {
-      dim3 g(std::max(1, std::min(64, (L.max_u + 255) / 256)), cnt);
+      // one warp per row of L21
+      dim3 g(std::max(1, std::min(256, (L.max_u + 7) / 8)), cnt);
       fwd_gemv_kernel<S><<<g, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x);
       count_launch(1);
     }
@@ -660,11 +679,11 @@ cudaError_t solve_t(MFHandle& h, cudaStream_t st) {
     const MFLevel& L = d.levels[lv];
     const int cnt = (int)L.nodes_by_k.size();
     if (L.max_u > 0) {
-      dim3 g(std::max(1, std::min(64, (L.max_k + 255) / 256)), cnt);
+      dim3 g(std::max(1, std::min(256, (L.max_k + 7) / 8)), cnt);
       bwd_gemv_kernel<S><<<g, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x);
       count_launch(1);
     }
-    bwd_trsv_kernel<S><<<cnt, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x);
+    bwd_trsv_kernel<S><<<cnt, 1024, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x);
     count_launch(1);
   }
   return cudaGetLastError();
