@@ -406,10 +406,38 @@ def run_kernel_case(args):
                       "nnz": V.nnz, "runs": args.warmup + args.steps}))
 
 
+def run_serve(args):
+    """Serving workload (Poisson arrivals of driven ABC solves, divisions
+    log-uniform, order 1/2 at 50/50, 1-6 wavelengths per box, complex64 LU +
+    FP64 refinement to 1e-8) through the continuous-batching server, and the
+    same requests one at a time on the plain FP64 path."""
+    from sucemfem.serving import SolveServer, make_request_stream
+    reqs = make_request_stream(args.serve_requests, args.serve_rate,
+                               cubes=(6, args.serve_max_cubes), seed=0)
+    srv = SolveServer(slots=args.serve_slots, tol=1e-8)
+    res = srv.run(reqs, realtime=True)
+    n64 = min(len(reqs), args.serve_fp64_sample)
+    one = SolveServer(slots=1, precision="fp64", tol=1e-8)
+    one.run(reqs[:n64], realtime=False)
+    print(json.dumps({
+        "case": "serve", "requests": len(reqs), "rate_per_s": args.serve_rate,
+        "cubes": [6, args.serve_max_cubes], "slots": args.serve_slots,
+        "server": srv.stats,
+        "max_residual": max(r.residual for r in res if r.status == "ok"),
+        "fp64_one_at_a_time": {"requests": n64, "solves_per_s": one.stats["solves_per_s"],
+                               "p50_ms": one.stats["p50_ms"]},
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", default="solve", choices=["solve", "factor", "assemble"],
-                    help="profiling cases: factor / assemble at --cubes, --order")
+    ap.add_argument("--only", default="solve", choices=["solve", "factor", "assemble", "serve"],
+                    help="profiling cases: factor / assemble at --cubes, --order; serve")
+    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-max-cubes", type=int, default=16)
+    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-fp64-sample", type=int, default=20)
     ap.add_argument("--cubes", type=int, default=N_CUBES)
     ap.add_argument("--order", type=int, default=ORDER)
     ap.add_argument("--gpus", type=int, default=1)
@@ -425,6 +453,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.only == "serve":
+        run_serve(args)
     elif args.only != "solve":
         run_kernel_case(args)
     else:

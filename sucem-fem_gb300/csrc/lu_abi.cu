@@ -19,24 +19,6 @@ MFHandle* mf_new();
 void mf_delete(MFHandle* h);
 MFSymbolic& mf_sym(MFHandle* h);
 
-namespace {
-
-template <typename R>
-__global__ void max_abs_kernel(int64_t m, const R* __restrict__ v, int stride,
-                               unsigned long long* __restrict__ out) {
-  // values are >= 0, so the IEEE bit pattern orders like an unsigned integer
-  double best = 0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    double a = 0;
-    for (int c = 0; c < stride; ++c) a += (double)v[i * stride + c] * (double)v[i * stride + c];
-    best = fmax(best, sqrt(a));
-  }
-  for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_down_sync(~0u, best, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(best));
-}
-
-}  // namespace
 }  // namespace sucem
 
 struct sucem_lu {
@@ -125,30 +107,9 @@ int sucem_lu_factor(sucem_lu* lu, int dtype, const void* vals, double pivot_tol,
   if (!lu || !vals) return fail("null argument", SUCEM_ERR_ARG);
   if (dtype < SUCEM_F32 || dtype > SUCEM_C128) return fail("bad dtype", SUCEM_ERR_ARG);
   cudaStream_t st = (cudaStream_t)stream;
-  const sucem::MFSymbolic& s = sucem::mf_sym(lu->h);
-  // static pivot threshold relative to the largest |entry|
-  unsigned long long* dmax = nullptr;
-  cudaError_t e = cudaMalloc((void**)&dmax, sizeof(unsigned long long));
-  if (e != cudaSuccess) return cuda_fail(e, "sucem_lu_factor");
-  e = cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), st);
-  const int stride = (dtype == SUCEM_C64 || dtype == SUCEM_C128) ? 2 : 1;
-  if (e == cudaSuccess) {
-    if (dtype == SUCEM_F32 || dtype == SUCEM_C64)
-      sucem::max_abs_kernel<float><<<256, 256, 0, st>>>(s.nnz, (const float*)vals, stride, dmax);
-    else
-      sucem::max_abs_kernel<double><<<256, 256, 0, st>>>(s.nnz, (const double*)vals, stride, dmax);
-    sucem::count_launch(1);
-    e = cudaGetLastError();
-  }
-  unsigned long long bits = 0;
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&bits, dmax, sizeof(bits), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  cudaFree(dmax);
-  if (e != cudaSuccess) return cuda_fail(e, "sucem_lu_factor");
-  double amax;
-  memcpy(&amax, &bits, sizeof(double));
-  const double tau = pivot_tol * (amax > 0 ? amax : 1.0);
-  e = sucem::mf_factor(*lu->h, dtype, vals, tau, st);
+  // the pivot threshold pivot_tol * max|a_ij| is formed on the device, so a
+  // factorisation is fully asynchronous on its stream
+  cudaError_t e = sucem::mf_factor(*lu->h, dtype, vals, pivot_tol, st);
   if (e != cudaSuccess) return cuda_fail(e, "sucem_lu_factor");
   return SUCEM_OK;
 }

@@ -157,17 +157,37 @@ __global__ void extend_add_kernel(const int32_t* __restrict__ kids, int nkids,
   }
 }
 
-// LU (no pivoting, static pivot replacement) of the nb x nb diagonal block
+// largest |a_ij| of the values (non-negative doubles order like their bits)
+__device__ __forceinline__ double mag2(float v) { return (double)v * v; }
+__device__ __forceinline__ double mag2(double v) { return v * v; }
+__device__ __forceinline__ double mag2(float2 v) { return (double)v.x * v.x + (double)v.y * v.y; }
+__device__ __forceinline__ double mag2(double2 v) { return v.x * v.x + v.y * v.y; }
+template <typename S>
+__global__ void max_abs_kernel(int64_t m, const S* __restrict__ v,
+                               unsigned long long* __restrict__ out) {
+  double best = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x)
+    best = fmax(best, mag2(v[i]));
+  for (int o = 16; o > 0; o >>= 1) best = fmax(best, __shfl_down_sync(~0u, best, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(sqrt(best)));
+}
+
+// LU (no pivoting, static pivot replacement) of the nb x nb diagonal block;
+// pivots below rel_tol * max|a_ij| are replaced by that value
 template <typename S>
 __global__ void diag_lu_kernel(const int32_t* __restrict__ list, int count,
                                const DNode* __restrict__ nodes, S* __restrict__ arena, int p0,
-                               double tau, int* __restrict__ n_perturbed) {
+                               const unsigned long long* __restrict__ amax, double rel_tol,
+                               int* __restrict__ n_perturbed) {
   __shared__ S D[NB][NB + 1];
   const int fi = blockIdx.x;
   if (fi >= count) return;
   const DNode nd = nodes[list[fi]];
   const int nb = min(NB, nd.k - p0);
   if (nb <= 0) return;
+  const double am = __longlong_as_double((long long)*amax);
+  const double tau = rel_tol * (am > 0 ? am : 1.0);
   S* base = arena + nd.off + (int64_t)p0 * nd.f + p0;
   for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
     const int r = t / nb, c = t % nb;
@@ -608,7 +628,7 @@ cudaError_t setup_device(MFHandle& h, int dtype) {
   if (e == cudaSuccess) e = upv(&d.d_perm, s.perm);
   if (e == cudaSuccess) e = cudaMalloc(&d.arena, (size_t)std::max<int64_t>(s.arena, 1) * d.elem);
   if (e == cudaSuccess) e = cudaMalloc(&d.d_x, (size_t)std::max<int64_t>(s.n, 1) * d.elem);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&d.d_flag, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&d.d_flag, 16);
   if (e != cudaSuccess) free_dev(d);
   return e;
 }
@@ -619,8 +639,12 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
   const MFSymbolic& s = h.sym;
   S* arena = (S*)d.arena;
   cudaError_t e = cudaMemsetAsync(arena, 0, (size_t)s.arena * sizeof(S), st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d.d_flag, 0, sizeof(int), st);
+  // d_flag[0]: perturbed-pivot count; d_flag[2..3]: max |a_ij| (as bits)
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.d_flag, 0, 16, st);
   if (e != cudaSuccess) return e;
+  unsigned long long* amax = reinterpret_cast<unsigned long long*>(d.d_flag + 2);
+  max_abs_kernel<S><<<256, 256, 0, st>>>(s.nnz, (const S*)vals, amax);
+  count_launch(1);
   const int64_t m = (int64_t)s.scat_src.size();
   if (m > 0) {
     scatter_kernel<S><<<(unsigned)((m + 255) / 256), 256, 0, st>>>(m, d.d_src, d.d_dst,
@@ -641,7 +665,8 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
       int cnt = 0;
       while (cnt < (int)L.k_sorted.size() && L.k_sorted[cnt] > p0) ++cnt;
       if (cnt == 0) break;
-      diag_lu_kernel<S><<<cnt, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0, tau, d.d_flag);
+      diag_lu_kernel<S><<<cnt, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0, amax, tau,
+                                             d.d_flag);
       count_launch(1);
       const int rest = std::max(0, L.max_rest - p0 - 1);
       const int tiles = (rest + 127) / 128;
