@@ -406,6 +406,164 @@ def run_kernel_case(args):
                       "nnz": V.nnz, "runs": args.warmup + args.steps}))
 
 
+def jittered_box(n, frac=0.2, seed=0):
+    """Unit box of n^3 cubes x 6 tets with every interior vertex moved by
+    U(-frac*h, frac*h) per coordinate (h = 1/n)."""
+    from sucemfem.mesh import BoxMesh, Mesh
+    m = BoxMesh(1.0, 1.0, 1.0, n, n, n)
+    x = m.coordinates().copy()
+    interior = np.all((x > 1e-12) & (x < 1 - 1e-12), axis=1)
+    d = np.random.default_rng(seed).uniform(-frac / n, frac / n, size=x.shape)
+    x[interior] += d[interior]
+    return Mesh(x, m.cells())
+
+
+def run_precision(args):
+    """Large-mesh precision case: jittered 60^3 box (1,296,000 tets), orders 1
+    and 2: per-entry FP32-vs-FP64 error of S, T, B; fused FP32 assembly
+    throughput against the HBM roofline (outputs far larger than L2);
+    order-1 FP32 LU + FP64 FGMRES solve to 1e-8; and, on the 40^3 order-1
+    box, the FP32+refinement solution against the plain FP64 GPU solution."""
+    import torch
+    from sucemfem import _device
+    from sucemfem._native import call, ptr
+    from sucemfem.solvers import DrivenSolver
+    from sucemfem.space import FunctionSpace
+    dev = _device.device()
+    hbm, _, peak_kind = measured_peaks()
+    out = {"case": "precision", "cubes": args.cubes}
+    mesh = jittered_box(args.cubes)
+    eps = np.random.default_rng(1).uniform(1.0, 4.0, mesh.num_cells())
+    k0 = 2 * np.pi / WAVELENGTH
+    for order in (1, 2):
+        V = FunctionSpace(mesh, order=order)
+        h = V.upload()
+        ip = torch.as_tensor(V.indptr, device=dev)
+        rows = torch.repeat_interleave(torch.arange(V.n, device=dev), ip[1:] - ip[:-1])
+        errs = {}
+        for name in ("S", "T", "B"):
+            v = {}
+            for rb in (8, 4):
+                dt = torch.float64 if rb == 8 else torch.float32
+                bufs = {k: torch.empty(V.nnz, dtype=dt, device=dev) if k == name else None for k in "STB"}
+                de = torch.as_tensor(eps, dtype=dt, device=dev)
+                call("sucem_assemble", h, rb, ptr(de), None, ptr(bufs["S"]), ptr(bufs["T"]),
+                     ptr(bufs["B"]), _device.stream_ptr())
+                v[rb] = bufs[name].double()
+                del bufs
+            a = v[8].abs()
+            rowmax = torch.zeros(V.n, dtype=torch.float64, device=dev).scatter_reduce(
+                0, rows, a, reduce="amax")
+            floor = (1.0 if name == "B" else 1e-6) * a.max()
+            scale = torch.maximum(rowmax[rows], floor)
+            e = (v[4] - v[8]).abs() / scale
+            errs[name] = {"max": float(e.max()), "median": float(e.median())}
+            del v, a, e, scale
+        d_eps = torch.as_tensor(eps, dtype=torch.float32, device=dev)
+        A = torch.empty(V.nnz, dtype=torch.complex64, device=dev)
+        times = []
+        for i in range(3 + 10):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            call("sucem_assemble_helmholtz", h, 4, ptr(d_eps), None, float(k0), ptr(A),
+                 _device.stream_ptr())
+            e1.record()
+            torch.cuda.synchronize()
+            if i >= 3:
+                times.append(e0.elapsed_time(e1))
+        ms = statistics.mean(times)
+        gbs = assembly_bytes(V) / (ms * 1e-3) / 1e9
+        out["order%d" % order] = {
+            "n_dofs": V.n, "nnz": V.nnz, "fp32_vs_fp64_entry_error": errs,
+            "assembly": {"ms": ms, "elems_per_s": V.nt / (ms * 1e-3), "achieved_gbs": gbs,
+                         "frac_of_hbm": gbs / hbm, "peak_source": peak_kind}}
+        del A, rows, ip
+        if order == 1:
+            from sucemfem.Sources.point_source import evaluate_point_sources
+            Z0 = 4e-7 * np.pi * C0
+            _, dofs, con = evaluate_point_sources(V, np.array([[0.5, 0.5, 0.5]]), np.array([[0, 0, 1.0]]))
+            b = np.zeros(V.n, dtype=np.complex128)
+            b[dofs[0]] += -1j * k0 * Z0 * con[0]
+            ds = DrivenSolver(V, eps_r=eps)
+            t0 = time.perf_counter()
+            x, info = ds.solve(k0, b, precision="fp32-ir", tol=1e-8)
+            torch.cuda.synchronize()
+            out["order1"]["solve_fp32_ir"] = {"seconds": time.perf_counter() - t0,
+                                              "iterations": info["iterations"],
+                                              "residual": info["residual"],
+                                              "lu_arena_gb": ds.lu.info["arena"] * 8 / 1e9,
+                                              "lu_tflop": ds.lu.info["flops"] * 8 / 1e12}
+            del ds, x
+        del V
+        torch.cuda.empty_cache()
+    # solution error vs the FP64 GPU path on a size where the FP64 LU is cheap
+    small = jittered_box(args.precision_solve_cubes)
+    eps_s = np.random.default_rng(2).uniform(1.0, 4.0, small.num_cells())
+    from sucemfem.Sources.point_source import evaluate_point_sources
+    Vs = FunctionSpace(small, order=1)
+    Z0 = 4e-7 * np.pi * C0
+    _, dofs, con = evaluate_point_sources(Vs, np.array([[0.5, 0.5, 0.5]]), np.array([[0, 0, 1.0]]))
+    b = np.zeros(Vs.n, dtype=np.complex128)
+    b[dofs[0]] += -1j * k0 * Z0 * con[0]
+    ds = DrivenSolver(Vs, eps_r=eps_s)
+    x32, i32 = ds.solve(k0, b, precision="fp32-ir", tol=1e-8)
+    x64, i64 = ds.solve(k0, b, precision="fp64", tol=1e-12)
+    out["solution_vs_fp64"] = {"cubes": args.precision_solve_cubes, "order": 1, "n_dofs": Vs.n,
+                               "rel_error": float(torch.linalg.norm(x32 - x64) / torch.linalg.norm(x64)),
+                               "fp32_ir_residual": i32["residual"], "fp64_residual": i64["residual"],
+                               "fp32_ir_s": i32["seconds"], "fp64_s": i64["seconds"]}
+    print(json.dumps(out))
+
+
+def run_eigen_batch(args):
+    """Batched cavities: 256 PEC boxes, sides U[0.3,1.5] m, divisions U{4..24}
+    per axis, order 1, eps_r U[1,4] per cell; one space, one assembly launch,
+    one LU of the stacked problem, one batched shift-invert Lanczos for the 6
+    smallest k^2 above sigma=1 of every cavity (FP32 LU, FP64 Lanczos/RR)."""
+    import torch
+    from sucemfem import _device
+    from sucemfem._native import call, ptr
+    from sucemfem.eigen import BatchedShiftInvertLanczos
+    from sucemfem.mesh import BoxMesh, Mesh
+    from sucemfem.space import FunctionSpace
+    dev = _device.device()
+    rng = np.random.default_rng(0)
+    ncav = args.cavities
+    coords, cells, seg_cells, off, x0 = [], [], [], 0, 0.0
+    for k in range(ncav):
+        L = rng.uniform(0.3, 1.5, 3)
+        n = rng.integers(4, 25, 3)
+        m = BoxMesh(L[0], L[1], L[2], int(n[0]), int(n[1]), int(n[2]), origin=(x0, 0.0, 0.0))
+        x0 += L[0] + 0.5
+        coords.append(m.coordinates())
+        cells.append(m.cells() + off)
+        off += len(m.coordinates())
+        seg_cells.append(np.full(m.num_cells(), k))
+    t0 = time.perf_counter()
+    V = FunctionSpace(Mesh(np.concatenate(coords), np.concatenate(cells)), order=1)
+    seg_cells = np.concatenate(seg_cells)
+    dof_seg = np.zeros(V.n, dtype=np.int64)
+    dof_seg[V.cell_dofs.ravel()] = np.repeat(seg_cells, 6)
+    eps = rng.uniform(1.0, 4.0, V.nt)
+    t_host = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    S = torch.empty(V.nnz, dtype=torch.float64, device=dev)
+    T = torch.empty_like(S)
+    d_eps = torch.as_tensor(eps, device=dev)
+    call("sucem_assemble", V.upload(), 8, ptr(d_eps), None, ptr(S), ptr(T), None, _device.stream_ptr())
+    sol = BatchedShiftInvertLanczos(V, S, T, V.boundary_dofs, 1.0, dof_segment=dof_seg)
+    t2 = time.perf_counter()
+    k2, Z = sol.solve(6)
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    print(json.dumps({"case": "eigen-batch", "cavities": ncav, "tets": V.nt, "n_dofs": V.n,
+                      "host_build_s": t_host, "setup_s": t2 - t1, "solve_s": t3 - t2,
+                      "cavity_solves_per_s": ncav / (t3 - t1),
+                      "lanczos_steps": sol.stats.get("m"), "lu_arena_gb": sol.lu.info["arena"] * 4 / 1e9,
+                      "k2_first_cavity": [float(v) for v in np.sort(k2[0])]}))
+
+
 def run_serve(args):
     """Serving workload (Poisson arrivals of driven ABC solves, divisions
     log-uniform, order 1/2 at 50/50, 1-6 wavelengths per box, complex64 LU +
@@ -431,8 +589,11 @@ def run_serve(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", default="solve", choices=["solve", "factor", "assemble", "serve"],
-                    help="profiling cases: factor / assemble at --cubes, --order; serve")
+    ap.add_argument("--only", default="solve",
+                    choices=["solve", "factor", "assemble", "serve", "precision", "eigen-batch"],
+                    help="profiling cases: factor / assemble at --cubes, --order; serve; precision")
+    ap.add_argument("--precision-solve-cubes", type=int, default=30)
+    ap.add_argument("--cavities", type=int, default=256)
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-max-cubes", type=int, default=16)
@@ -455,6 +616,10 @@ def main():
         run_reference(args)
     elif args.only == "serve":
         run_serve(args)
+    elif args.only == "precision":
+        run_precision(args)
+    elif args.only == "eigen-batch":
+        run_eigen_batch(args)
     elif args.only != "solve":
         run_kernel_case(args)
     else:
