@@ -8,11 +8,11 @@
 //     for cells with exterior facets, 3 tangential coefficients per facet.
 //  2. assemble_rows_kernel: one warp owns one mesh entity (an edge, or for
 //     order 2 also a face) and therefore the dofs_per_entity CSR rows that
-//     share its column list.  The warp's lanes sweep the flattened
-//     (incident cell, entity row, cell column) triples, contract the cell
-//     coefficients with the reference tensors held in shared memory, and
-//     add the value into the entity's rows (shared-memory accumulators,
-//     indexed by the precomputed column slot).  Each CSR value is then
+//     share its column list.  Lanes map to the columns of the incident
+//     cells (order 2: one cell per step; order 1: five), contract the cell
+//     coefficients with the reference tensors held in shared memory for
+//     the entity's rows, and add the values into shared-memory row
+//     accumulators at the precomputed column slots.  Each CSR value is then
 //     written exactly once with coalesced stores: no zero-fill pass, no
 //     atomics and a fixed summation order (bit-reproducible run to run).
 //
@@ -206,13 +206,14 @@ __device__ __forceinline__ void load12<double>(const double* p, double out[12]) 
 // ORDER: 1 or 2.  WITH_B: accumulate the ABC matrix.  MODE 0: separate
 // real outputs; MODE 1: fused complex A = S - k0^2 T + j k0 B.
 //
-// The warp sweeps the entity's (incident cell k, cell column b) pairs 32 at
-// a time; each lane computes both rows of its pair.  32 consecutive pairs
-// span at most NC = 32/ND + 2 incident cells, so pair (k, b) adds into
-// accumulator copy k % NC: within one sweep step two lanes that share a copy
-// belong to the same cell and hit distinct column slots, so plain
-// shared-memory read-add-write is race free.  The copies are summed in a
-// fixed order when the rows are written, so results are bit-reproducible.
+// One warp per entity.  Its lanes take ICH = 32/ND incident cells at a time
+// (order 2: one cell, lane b = cell column b; order 1: five cells x six
+// columns).  Each lane contracts the cell's coefficients with the reference
+// tensors for the entity's rows and adds the result into its accumulator
+// copy (copy = which of the ICH cells of the step it handles).  Within a copy
+// the columns of one cell are distinct slots, so plain shared-memory
+// read-add-write is race free; copies are summed in a fixed order when the
+// rows are written, so results are bit-reproducible.
 template <int ORDER, typename Real, bool WITH_B, int MODE>
 __global__ void __launch_bounds__(kWarps * 32)
     assemble_rows_kernel(RowPtrs p, const Real* __restrict__ gcell, const Real* __restrict__ hcell,
@@ -221,7 +222,7 @@ __global__ void __launch_bounds__(kWarps * 32)
   constexpr int ND = ORDER == 1 ? 6 : 20;
   constexpr int DPE = ORDER == 1 ? 1 : 2;
   constexpr int REC = ORDER == 1 ? 8 : 24;
-  constexpr int NC = 32 / ND + 2;
+  constexpr int ICH = 32 / ND;                 // incident cells per sweep step
   // accumulated matrices: mode 0 -> S, T (, B); mode 1 -> Re A, Im A
   constexpr int NMAT = MODE == 1 ? 2 : (WITH_B ? 3 : 2);
   constexpr int KSZ = ND * ND * 12;
@@ -231,13 +232,16 @@ __global__ void __launch_bounds__(kWarps * 32)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int R = p.max_row;
   const int copy_len = DPE * NMAT * R;        // one copy: [DPE][NMAT][R]
-  const int acc_len = NC * copy_len;
-  Real* acc = sK + KSZ + warp * acc_len;      // [NC][DPE][NMAT][R]
+  const int acc_len = ICH * copy_len;
+  Real* acc = sK + KSZ + warp * acc_len;      // [ICH][DPE][NMAT][R]
 
   for (int i = threadIdx.x; i < KSZ; i += blockDim.x) sK[i] = kab[i];
   for (int i = lane; i < acc_len; i += 32) acc[i] = Real(0);
   __syncthreads();
   const Real k0sq = k0 * k0;
+  const int sub = lane / ND, b = lane - sub * ND;   // cell of the step, cell column
+  const bool lane_on = sub < ICH;
+  Real* my_copy = acc + (lane_on ? sub : 0) * copy_len;
 
   const int64_t nwarps = (int64_t)gridDim.x * kWarps;
   for (int64_t e = (int64_t)blockIdx.x * kWarps + warp; e < p.n_ent; e += nwarps) {
@@ -245,13 +249,9 @@ __global__ void __launch_bounds__(kWarps * 32)
     const int64_t r0 = (int64_t)DPE * e;
     const int off = __ldg(&p.indptr[r0]);
     const int L = __ldg(&p.indptr[r0 + 1]) - off;
-    const int total = (i1 - i0) * ND;
-    for (int t0 = 0; t0 < total; t0 += 32) {
-      const int t = t0 + lane;
-      if (t < total) {
-        const int k = t / ND;
-        const int b = t - k * ND;
-        const int inc = i0 + k;
+    for (int k0i = i0; k0i < i1; k0i += ICH) {
+      const int inc = k0i + sub;
+      if (lane_on && inc < i1) {
         const int c = __ldg(&p.inc_cell[inc]);
         const uint8_t* rec = p.inc_rec + (int64_t)inc * REC;
         const int le = __ldg(rec);
@@ -263,7 +263,6 @@ __global__ void __launch_bounds__(kWarps * 32)
           hb = __ldg(&p.bidx[c]);
           if (hb >= 0) mask = __ldg(&p.ext_mask[c]);
         }
-        Real* cp = acc + (k % NC) * copy_len + slot;
 #pragma unroll
         for (int j = 0; j < DPE; ++j) {
           const int a = DPE * le + j;
@@ -275,9 +274,16 @@ __global__ void __launch_bounds__(kWarps * 32)
             s = fma(g[m], kk[m], s);
             tm = fma(g[6 + m], kk[6 + m], tm);
           }
-          Real bv = 0;
+          Real* ar = my_copy + j * NMAT * R + slot;
+          if (MODE == 1) {
+            ar[0] += s - k0sq * tm;
+          } else {
+            ar[0] += s;
+            ar[R] += tm;
+          }
           if (WITH_B && hb >= 0) {
             const Real* hh = hcell + (int64_t)hb * 12;
+            Real bv = 0;
 #pragma unroll
             for (int f = 0; f < 4; ++f) {
               if (!(mask >> f & 1)) continue;
@@ -285,15 +291,10 @@ __global__ void __launch_bounds__(kWarps * 32)
               for (int m = 0; m < 3; ++m)
                 bv = fma(__ldg(&hh[f * 3 + m]), __ldg(&kt[((f * 3 + m) * ND + a) * ND + b]), bv);
             }
-          }
-          Real* ar = cp + j * NMAT * R;
-          if (MODE == 1) {
-            ar[0] += s - k0sq * tm;
-            if (WITH_B && hb >= 0) ar[R] += k0 * bv;
-          } else {
-            ar[0] += s;
-            ar[R] += tm;
-            if (WITH_B && hb >= 0) ar[2 * R] += bv;
+            if (MODE == 1)
+              ar[R] += k0 * bv;
+            else
+              ar[2 * R] += bv;
           }
         }
       }
@@ -308,7 +309,7 @@ __global__ void __launch_bounds__(kWarps * 32)
 #pragma unroll
         for (int q = 0; q < NMAT; ++q) v[q] = 0;
 #pragma unroll
-        for (int cc = 0; cc < NC; ++cc) {
+        for (int cc = 0; cc < ICH; ++cc) {
           Real* ar = acc + cc * copy_len + j * NMAT * R + col;
 #pragma unroll
           for (int q = 0; q < NMAT; ++q) {
@@ -354,7 +355,7 @@ cudaError_t launch_t(DeviceSpace& d, const AssembleArgs& a, cudaStream_t stream)
   constexpr int ND = ORDER == 1 ? 6 : 20;
   constexpr int DPE = ORDER == 1 ? 1 : 2;
   constexpr int NMAT = MODE == 1 ? 2 : (WITH_B ? 3 : 2);
-  constexpr int NC = 32 / ND + 2;
+  constexpr int ICH = 32 / ND;
   Real *g = nullptr, *h = nullptr;
   cudaError_t err = ensure_scratch<Real>(d, &g, &h);
   if (err != cudaSuccess) return err;
@@ -377,7 +378,7 @@ cudaError_t launch_t(DeviceSpace& d, const AssembleArgs& a, cudaStream_t stream)
   p.n_ent = d.n_ent;
   p.max_row = d.max_row;
   const size_t smem =
-      sizeof(Real) * ((size_t)ND * ND * 12 + (size_t)kWarps * NC * DPE * NMAT * d.max_row);
+      sizeof(Real) * ((size_t)ND * ND * 12 + (size_t)kWarps * ICH * DPE * NMAT * d.max_row);
   auto kern = assemble_rows_kernel<ORDER, Real, WITH_B, MODE>;
   err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;

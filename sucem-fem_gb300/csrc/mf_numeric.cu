@@ -7,7 +7,7 @@
 // children's Schur complements are added into their parents (extend-add,
 // one launch per child slot so no two writers meet), and every front of the
 // level is partially factorised with a blocked right-looking LU (panel
-// width 32): diagonal-block LU (one block per front), the two triangular
+// width 64, 32 for complex double): diagonal-block LU (one block per front), the two triangular
 // panel solves, and the trailing update, a batched register-tiled GEMM.
 // Solve: forward (unit-lower L) and backward (U) substitution level by
 // level; the off-diagonal block products are spread over many blocks.
@@ -27,7 +27,6 @@ void count_launch(int k);
 
 namespace {
 
-constexpr int NB = 32;  // panel width
 
 // ---- scalar helpers ----
 __device__ __forceinline__ float s_zero(float) { return 0.f; }
@@ -175,16 +174,16 @@ __global__ void max_abs_kernel(int64_t m, const S* __restrict__ v,
 
 // LU (no pivoting, static pivot replacement) of the nb x nb diagonal block;
 // pivots below rel_tol * max|a_ij| are replaced by that value
-template <typename S>
+template <typename S, int NBT>
 __global__ void diag_lu_kernel(const int32_t* __restrict__ list, int count,
                                const DNode* __restrict__ nodes, S* __restrict__ arena, int p0,
                                const unsigned long long* __restrict__ amax, double rel_tol,
                                int* __restrict__ n_perturbed) {
-  __shared__ S D[NB][NB + 1];
+  __shared__ S D[NBT][NBT + 1];
   const int fi = blockIdx.x;
   if (fi >= count) return;
   const DNode nd = nodes[list[fi]];
-  const int nb = min(NB, nd.k - p0);
+  const int nb = min(NBT, nd.k - p0);
   if (nb <= 0) return;
   const double am = __longlong_as_double((long long)*amax);
   const double tau = rel_tol * (am > 0 ? am : 1.0);
@@ -216,30 +215,33 @@ __global__ void diag_lu_kernel(const int32_t* __restrict__ list, int count,
 }
 
 // panel solves: rows below the diagonal block (X U11 = A, thread per row)
-// and columns right of it (L11 X = A, thread per column); 128 per block
-template <typename S>
+// and columns right of it (L11 X = A, thread per column); TR per block.
+// Dynamic shared memory: D[NBT][NBT+1] then T[TR][NBT+1].
+template <typename S, int NBT, int TR>
 __global__ void panel_trsm_kernel(const int32_t* __restrict__ list, int count,
                                   const DNode* __restrict__ nodes, S* __restrict__ arena, int p0) {
-  __shared__ S D[NB][NB + 1];
-  __shared__ S T[128][NB + 1];
+  extern __shared__ __align__(16) unsigned char trsm_smem[];
+  S(*D)[NBT + 1] = reinterpret_cast<S(*)[NBT + 1]>(trsm_smem);
+  S(*T)[NBT + 1] = reinterpret_cast<S(*)[NBT + 1]>(trsm_smem + sizeof(S) * NBT * (NBT + 1));
   const int fi = blockIdx.y;
   if (fi >= count) return;
   const DNode nd = nodes[list[fi]];
-  const int nb = min(NB, nd.k - p0);
+  const int nb = min(NBT, nd.k - p0);
   if (nb <= 0) return;
   const int rest = nd.f - p0 - nb;
   if (rest <= 0) return;
-  const int tiles = (rest + 127) / 128;
+  const int tiles = (rest + TR - 1) / TR;
   int tile = blockIdx.x;
   const bool rows = tile < tiles;
   if (!rows) tile -= tiles;
   if (tile >= tiles) return;
   S* base = arena + nd.off + (int64_t)p0 * nd.f + p0;
-  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) D[t / nb][t % nb] = base[(int64_t)(t / nb) * nd.f + t % nb];
-  const int first = p0 + nb + tile * 128;
-  const int cnt = min(128, nd.f - first);
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x)
+    D[t / nb][t % nb] = base[(int64_t)(t / nb) * nd.f + t % nb];
+  const int first = p0 + nb + tile * TR;
+  const int cnt = min(TR, nd.f - first);
   if (rows) {
-    // load cnt rows x nb columns (coalesced along the row)
+    // cnt rows x nb columns (coalesced along the row)
     for (int t = threadIdx.x; t < cnt * nb; t += blockDim.x) {
       const int r = t / nb, c = t % nb;
       T[r][c] = arena[nd.off + (int64_t)(first + r) * nd.f + p0 + c];
@@ -259,41 +261,43 @@ __global__ void panel_trsm_kernel(const int32_t* __restrict__ list, int count,
       arena[nd.off + (int64_t)(first + r) * nd.f + p0 + c] = T[r][c];
     }
   } else {
+    // nb rows x cnt columns, stored transposed: T[col][i]
+    for (int t = threadIdx.x; t < cnt * nb; t += blockDim.x) {
+      const int i = t / cnt, c = t % cnt;
+      T[c][i] = arena[nd.off + (int64_t)(p0 + i) * nd.f + first + c];
+    }
     __syncthreads();
     if (threadIdx.x < cnt) {
-      const int col = first + threadIdx.x;
-      S* colp = arena + nd.off + (int64_t)p0 * nd.f + col;
-      S x[NB];
-#pragma unroll
-      for (int i = 0; i < NB; ++i)
-        if (i < nb) x[i] = colp[(int64_t)i * nd.f];
-#pragma unroll
-      for (int i = 0; i < NB; ++i) {
-        if (i >= nb) break;
-#pragma unroll
-        for (int j = 0; j < NB; ++j)
-          if (j < i) x[i] = s_fms(x[i], D[i][j], x[j]);
+      const int c = threadIdx.x;
+      for (int i = 1; i < nb; ++i) {
+        S x = T[c][i];
+        for (int j = 0; j < i; ++j) x = s_fms(x, D[i][j], T[c][j]);
+        T[c][i] = x;
       }
-#pragma unroll
-      for (int i = 0; i < NB; ++i)
-        if (i < nb) colp[(int64_t)i * nd.f] = x[i];
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < cnt * nb; t += blockDim.x) {
+      const int i = t / cnt, c = t % cnt;
+      arena[nd.off + (int64_t)(p0 + i) * nd.f + first + c] = T[c][i];
     }
   }
 }
 
 // trailing update C -= Lpanel * Upanel over the (f-p0-nb)^2 block,
-// 64x64 tile per block, 4x4 outputs per thread
-template <typename S>
+// 64x64 tile per block, 4x4 outputs per thread, K = nb <= NBT.
+// Dynamic shared memory: As[NBT][65] (As[t][i] = L[i][t]) then Bs[NBT][64].
+template <typename S, int NBT>
 __global__ void __launch_bounds__(256) gemm_update_kernel(const int32_t* __restrict__ list,
                                                           int count,
                                                           const DNode* __restrict__ nodes,
                                                           S* __restrict__ arena, int p0) {
-  __shared__ S As[NB][64 + 1];  // As[t][i] = L[i][t]
-  __shared__ S Bs[NB][64];      // Bs[t][j] = U[t][j]
+  extern __shared__ __align__(16) unsigned char gemm_smem[];
+  S(*As)[65] = reinterpret_cast<S(*)[65]>(gemm_smem);
+  S(*Bs)[64] = reinterpret_cast<S(*)[64]>(gemm_smem + sizeof(S) * NBT * 65);
   const int fi = blockIdx.y;
   if (fi >= count) return;
   const DNode nd = nodes[list[fi]];
-  const int nb = min(NB, nd.k - p0);
+  const int nb = min(NBT, nd.k - p0);
   if (nb <= 0) return;
   const int lo = p0 + nb;
   const int rest = nd.f - lo;
@@ -303,8 +307,8 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(const int32_t* __restr
   const int ti = blockIdx.x / tpd, tj = blockIdx.x % tpd;
   const int i0 = lo + ti * 64, j0 = lo + tj * 64;
   S* F = arena + nd.off;
-  for (int t = threadIdx.x; t < 64 * NB; t += 256) {
-    const int i = t / NB, c = t % NB;
+  for (int t = threadIdx.x; t < 64 * NBT; t += 256) {
+    const int i = t / NBT, c = t % NBT;
     As[c][i] = (i0 + i < nd.f && c < nb) ? F[(int64_t)(i0 + i) * nd.f + p0 + c] : s_zero(S());
     const int r = t / 64, j = t % 64;
     Bs[r][j] = (j0 + j < nd.f && r < nb) ? F[(int64_t)(p0 + r) * nd.f + j0 + j] : s_zero(S());
@@ -316,6 +320,17 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(const int32_t* __restr
   for (int a = 0; a < 4; ++a)
 #pragma unroll
     for (int b = 0; b < 4; ++b) acc[a][b] = s_zero(S());
+  // issue the C loads early; they are consumed after the contraction
+  S cv[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int i = i0 + ty + 16 * a;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int j = j0 + tx + 16 * b;
+      cv[a][b] = (i < nd.f && j < nd.f) ? F[(int64_t)i * nd.f + j] : s_zero(S());
+    }
+  }
   for (int t = 0; t < nb; ++t) {
     S av[4], bv[4];
 #pragma unroll
@@ -335,8 +350,7 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(const int32_t* __restr
     for (int b = 0; b < 4; ++b) {
       const int j = j0 + tx + 16 * b;
       if (j >= nd.f) continue;
-      S* c = F + (int64_t)i * nd.f + j;
-      *c = s_add(*c, acc[a][b]);
+      F[(int64_t)i * nd.f + j] = s_add(cv[a][b], acc[a][b]);
     }
   }
 }
@@ -635,6 +649,19 @@ cudaError_t setup_device(MFHandle& h, int dtype) {
 
 template <typename S>
 cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st) {
+  // panel width 64 (32 for complex double, whose tiles would not fit)
+  constexpr int NBT = sizeof(S) <= 8 ? 64 : 32;
+  constexpr int TR = NBT == 64 ? 64 : 128;
+  const size_t trsm_smem = sizeof(S) * (size_t)(NBT + TR) * (NBT + 1);
+  const size_t gemm_smem = sizeof(S) * (size_t)NBT * (65 + 64);
+  {
+    cudaError_t ea = cudaFuncSetAttribute(panel_trsm_kernel<S, NBT, TR>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trsm_smem);
+    if (ea == cudaSuccess)
+      ea = cudaFuncSetAttribute(gemm_update_kernel<S, NBT>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem);
+    if (ea != cudaSuccess) return ea;
+  }
   MFDevice& d = h.dev;
   const MFSymbolic& s = h.sym;
   S* arena = (S*)d.arena;
@@ -660,22 +687,22 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
       extend_add_kernel<S><<<grid, 128, 0, st>>>(L.d_kids[c], nk, d.d_nodes, d.d_ea, arena);
       count_launch(1);
     }
-    for (int p0 = 0; p0 < L.max_k; p0 += NB) {
+    for (int p0 = 0; p0 < L.max_k; p0 += NBT) {
       // active fronts: prefix of the k-descending list with k > p0
       int cnt = 0;
       while (cnt < (int)L.k_sorted.size() && L.k_sorted[cnt] > p0) ++cnt;
       if (cnt == 0) break;
-      diag_lu_kernel<S><<<cnt, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0, amax, tau,
-                                             d.d_flag);
+      diag_lu_kernel<S, NBT><<<cnt, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0, amax,
+                                                  tau, d.d_flag);
       count_launch(1);
       const int rest = std::max(0, L.max_rest - p0 - 1);
-      const int tiles = (rest + 127) / 128;
+      const int tiles = (rest + TR - 1) / TR;
       if (tiles > 0) {
         dim3 g1(2 * tiles, cnt);
-        panel_trsm_kernel<S><<<g1, 128, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0);
+        panel_trsm_kernel<S, NBT, TR><<<g1, TR, trsm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0);
         const int tpd = (rest + 63) / 64;
         dim3 g2(tpd * tpd, cnt);
-        gemm_update_kernel<S><<<g2, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0);
+        gemm_update_kernel<S, NBT><<<g2, 256, gemm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0);
         count_launch(2);
       }
     }

@@ -141,23 +141,28 @@ class BatchedShiftInvertLanczos:
         dev = _device.device()
         nseg, n = self.nseg, self.n
         sizes = np.diff(self.seg_ptr_h)
-        m = int(max(2 * nev + 1, ncv or 0, nev + 20))
-        m = int(min(m, sizes.min()))
-        for attempt in range(maxiter):
-            res = self._lanczos(nev, m, seed)
-            if res is not None:
-                break
+        m0 = int(min(max(2 * nev + 1, ncv or 0, nev + 20), sizes.min()))
+        checkpoints = []
+        m = m0
+        for _ in range(maxiter):
+            checkpoints.append(m)
             if m >= sizes.min():
-                raise RuntimeError("Lanczos did not converge with the full space")
+                break
             m = int(min(2 * m, sizes.min()))
-        Y, theta = res
+        res = self._lanczos(nev, checkpoints, seed)
+        if res is None:
+            raise RuntimeError("Lanczos did not converge within %d steps" % checkpoints[-1])
+        Y, theta, m = res
         k2, Z = self._rayleigh_ritz(Y, nev)
-        self.stats.update(m=m, attempts=attempt + 1, theta=theta)
+        self.stats.update(m=m, theta=theta)
         return k2, Z
 
-    def _lanczos(self, nev, m, seed):
+    def _lanczos(self, nev, checkpoints, seed):
+        """One Lanczos run extended through the checkpoints until the nev
+        wanted Ritz values of every segment have converged."""
         dev = _device.device()
         nseg, n = self.nseg, self.n
+        m = checkpoints[-1]
         Vb = torch.empty((m + 1, n), dtype=torch.float64, device=dev)
         g = torch.Generator(device="cpu").manual_seed(seed)
         Vb[0].copy_(torch.rand(n, generator=g, dtype=torch.float64) - 0.5)
@@ -185,11 +190,19 @@ class BatchedShiftInvertLanczos:
             inv = torch.as_tensor(np.where(b > 0, 1.0 / np.maximum(b, 1e-300), 0.0), device=dev)
             Vb[j + 1].zero_()
             self._segaxpy(w, 1, inv, torch.zeros(nseg, dtype=torch.float64, device=dev), Vb[j + 1])
-        # Ritz values per segment, convergence check
+            if j + 1 in checkpoints:
+                done = self._ritz(nev, j + 1, alpha, beta, Vb)
+                if done is not None:
+                    return done[0], done[1], j + 1
+        return None
+
+    def _ritz(self, nev, m, alpha, beta, Vb):
+        """Ritz values per segment after m steps; None unless all converged."""
+        nseg, n = self.nseg, self.n
         coef = np.zeros((m, nseg * nev))
         thetas = np.zeros((nseg, nev))
         for s in range(nseg):
-            th, Sv = sla.eigh_tridiagonal(alpha[s], beta[s, :m - 1])
+            th, Sv = sla.eigh_tridiagonal(alpha[s, :m], beta[s, :m - 1])
             idx = np.argsort(th)[::-1][:nev]           # largest mu = smallest k^2 above sigma
             resid = np.abs(beta[s, m - 1] * Sv[m - 1, idx])
             if np.any(resid > 1e-8 * np.maximum(np.abs(th[idx]), 1e-300)):
@@ -198,6 +211,7 @@ class BatchedShiftInvertLanczos:
             for i, q in enumerate(idx):
                 coef[:, i * nseg + s] = Sv[:, q]
         # Ritz vectors Y_i = sum_j coef[j, i] v_j (per segment)
+        dev = Vb.device
         Y = torch.zeros((nev, n), dtype=torch.float64, device=dev)
         zeros = torch.zeros(nseg, dtype=torch.float64, device=dev)
         for i in range(nev):
