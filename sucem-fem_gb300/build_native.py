@@ -63,7 +63,7 @@ def build(verbose=False, force=False):
             if o.strip():
                 print(o)
     tmp = OUT + ".tmp"
-    _run([NVCC] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", tmp] + objs)
+    _run([NVCC] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", tmp] + objs + ["-lcublas"])
     os.replace(tmp, OUT)
     return OUT
 

@@ -20,6 +20,10 @@
 #include "../../include/sucem_gb300.h"
 #include "mf.h"
 
+#include <cublas_v2.h>
+
+#include <type_traits>
+
 namespace sucem {
 int fail(const std::string& msg, int code);
 int cuda_fail(cudaError_t e, const char* where);
@@ -27,6 +31,11 @@ void count_launch(int k);
 
 namespace {
 
+
+// levels with at most this many fronts update them with cuBLAS (see blas_update)
+constexpr int kBlasFronts = 16;
+template <typename S>
+constexpr bool kSinglePrecision = std::is_same<S, float>::value || std::is_same<S, float2>::value;
 
 // ---- scalar helpers ----
 __device__ __forceinline__ float s_zero(float) { return 0.f; }
@@ -547,6 +556,9 @@ struct MFDevice {
   std::vector<MFLevel> levels;
   bool factored = false;
   int perturbed = 0;
+  // cuBLAS handle for the single-precision Schur updates of the top levels
+  cublasHandle_t blas = nullptr;
+  cublasComputeType_t blas_compute = CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
 };
 
 struct MFHandle {
@@ -584,7 +596,44 @@ void free_dev(MFDevice& d) {
     for (int s = 0; s < 2; ++s)
       if (L.d_kids[s]) cudaFree(L.d_kids[s]);
   }
+  if (d.blas) cublasDestroy(d.blas);
   d = MFDevice();
+}
+
+// Trailing update of one large front by cuBLAS (a plain GEMM): in the
+// row-major front, C[lo:, lo:] -= L[lo:, p0:p0+nb] U[p0:p0+nb, lo:], i.e. in
+// cuBLAS's column-major view C^T -= U^T L^T with leading dimension f.  The
+// single-precision product runs with FP32-accurate BF16x9 emulation on the
+// tensor cores when cuBLAS offers it for the type, else plain FP32.
+template <typename S>
+cudaError_t blas_update(MFDevice& d, S* F, int64_t f, int p0, int nb, cudaStream_t st) {
+  const int64_t lo = p0 + nb, rest = f - lo;
+  if (rest <= 0) return cudaSuccess;
+  if (!d.blas) {
+    if (cublasCreate(&d.blas) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+  }
+  cublasSetStream(d.blas, st);
+  const bool cplx = sizeof(S) == 8;
+  const cudaDataType_t t = cplx ? CUDA_C_32F : CUDA_R_32F;
+  const float2 am1 = make_float2(-1.f, 0.f), one = make_float2(1.f, 0.f);
+  const void* alpha = &am1;
+  const void* beta = &one;
+  const S* A = F + p0 * f + lo;  // U block
+  const S* B = F + lo * f + p0;  // L block
+  S* C = F + lo * f + lo;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    cublasStatus_t s = cublasGemmEx(d.blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, (int)rest, nb,
+                                    alpha, A, t, (int)f, B, t, (int)f, beta, C, t, (int)f,
+                                    d.blas_compute, CUBLAS_GEMM_DEFAULT);
+    if (s == CUBLAS_STATUS_SUCCESS) {
+      count_launch(1);
+      return cudaSuccess;
+    }
+    if (s != CUBLAS_STATUS_NOT_SUPPORTED || d.blas_compute == CUBLAS_COMPUTE_32F)
+      return cudaErrorUnknown;
+    d.blas_compute = CUBLAS_COMPUTE_32F;
+  }
+  return cudaErrorUnknown;
 }
 
 cudaError_t setup_device(MFHandle& h, int dtype) {
@@ -678,6 +727,14 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
                                                                    (const S*)vals, arena);
     count_launch(1);
   }
+  // SUCEM_LU_PROFILE=1 prints the device time of every tree level (stderr)
+  const bool prof = getenv("SUCEM_LU_PROFILE") != nullptr;
+  cudaEvent_t ev[2];
+  if (prof) {
+    cudaEventCreate(&ev[0]);
+    cudaEventCreate(&ev[1]);
+    cudaEventRecord(ev[0], st);
+  }
   for (size_t lv = 0; lv < d.levels.size(); ++lv) {
     const MFLevel& L = d.levels[lv];
     for (int c = 0; c < 2; ++c) {
@@ -700,12 +757,37 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
       if (tiles > 0) {
         dim3 g1(2 * tiles, cnt);
         panel_trsm_kernel<S, NBT, TR><<<g1, TR, trsm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0);
-        const int tpd = (rest + 63) / 64;
-        dim3 g2(tpd * tpd, cnt);
-        gemm_update_kernel<S, NBT><<<g2, 256, gemm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0);
-        count_launch(2);
+        count_launch(1);
+        if (kSinglePrecision<S> && cnt <= kBlasFronts) {
+          // few large fronts: one cuBLAS GEMM per front
+          for (int q = 0; q < cnt; ++q) {
+            const MFNode& nd = s.nodes[L.nodes_by_k[q]];
+            const int nbq = (int)std::min<int64_t>(NBT, nd.k - p0);
+            e = blas_update<S>(d, arena + nd.front_off, nd.f, p0, nbq, st);
+            if (e != cudaSuccess) return e;
+          }
+        } else {
+          const int tpd = (rest + 63) / 64;
+          dim3 g2(tpd * tpd, cnt);
+          gemm_update_kernel<S, NBT><<<g2, 256, gemm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena,
+                                                                  p0);
+          count_launch(1);
+        }
       }
     }
+    if (prof) {
+      cudaEventRecord(ev[1], st);
+      cudaEventSynchronize(ev[1]);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev[0], ev[1]);
+      fprintf(stderr, "[sucem lu] level %zu fronts %zu max_k %d max_f %d  %.3f ms\n", lv,
+              L.nodes_by_k.size(), L.max_k, L.max_rest, ms);
+      cudaEventRecord(ev[0], st);
+    }
+  }
+  if (prof) {
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
   }
   return cudaGetLastError();
 }
