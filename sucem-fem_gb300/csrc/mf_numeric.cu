@@ -59,6 +59,34 @@ __device__ __forceinline__ double2 s_fms(double2 c, double2 a, double2 b) {
   c.y = fma(-a.y, b.x, c.y);
   return c;
 }
+__device__ __forceinline__ float s_one(float) { return 1.f; }
+__device__ __forceinline__ double s_one(double) { return 1.0; }
+__device__ __forceinline__ float2 s_one(float2) { return make_float2(1.f, 0.f); }
+__device__ __forceinline__ double2 s_one(double2) { return make_double2(1.0, 0.0); }
+__device__ __forceinline__ float s_mul(float a, float b) { return a * b; }
+__device__ __forceinline__ double s_mul(double a, double b) { return a * b; }
+__device__ __forceinline__ float2 s_mul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 s_mul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float s_fma(float c, float a, float b) { return fmaf(a, b, c); }
+__device__ __forceinline__ double s_fma(double c, double a, double b) { return fma(a, b, c); }
+__device__ __forceinline__ float2 s_fma(float2 c, float2 a, float2 b) {
+  c.x = fmaf(a.x, b.x, c.x);
+  c.x = fmaf(-a.y, b.y, c.x);
+  c.y = fmaf(a.x, b.y, c.y);
+  c.y = fmaf(a.y, b.x, c.y);
+  return c;
+}
+__device__ __forceinline__ double2 s_fma(double2 c, double2 a, double2 b) {
+  c.x = fma(a.x, b.x, c.x);
+  c.x = fma(-a.y, b.y, c.x);
+  c.y = fma(a.x, b.y, c.y);
+  c.y = fma(a.y, b.x, c.y);
+  return c;
+}
 __device__ __forceinline__ float s_add(float a, float b) { return a + b; }
 __device__ __forceinline__ double s_add(double a, double b) { return a + b; }
 __device__ __forceinline__ float2 s_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -182,12 +210,16 @@ __global__ void max_abs_kernel(int64_t m, const S* __restrict__ v,
 }
 
 // LU (no pivoting, static pivot replacement) of the nb x nb diagonal block;
-// pivots below rel_tol * max|a_ij| are replaced by that value
+// pivots below rel_tol * max|a_ij| are replaced by that value.  16 x 16
+// threads, each owning the rows ty + 16a and columns tx + 16b of the block
+// (padded with the identity beyond nb), two barriers per pivot step.
 template <typename S, int NBT>
-__global__ void diag_lu_kernel(const int32_t* __restrict__ list, int count,
-                               const DNode* __restrict__ nodes, S* __restrict__ arena, int p0,
-                               const unsigned long long* __restrict__ amax, double rel_tol,
-                               int* __restrict__ n_perturbed) {
+__global__ void __launch_bounds__(256) diag_lu_kernel(const int32_t* __restrict__ list,
+                                                      int count, const DNode* __restrict__ nodes,
+                                                      S* __restrict__ arena, int p0,
+                                                      const unsigned long long* __restrict__ amax,
+                                                      double rel_tol, int* __restrict__ n_perturbed) {
+  constexpr int RB = NBT / 16;
   __shared__ S D[NBT][NBT + 1];
   const int fi = blockIdx.x;
   if (fi >= count) return;
@@ -197,41 +229,67 @@ __global__ void diag_lu_kernel(const int32_t* __restrict__ list, int count,
   const double am = __longlong_as_double((long long)*amax);
   const double tau = rel_tol * (am > 0 ? am : 1.0);
   S* base = arena + nd.off + (int64_t)p0 * nd.f + p0;
-  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
-    const int r = t / nb, c = t % nb;
-    D[r][c] = base[(int64_t)r * nd.f + c];
+  const S zero = s_zero(S()), one = s_one(S());
+  for (int t = threadIdx.x; t < NBT * NBT; t += 256) {
+    const int r = t / NBT, c = t % NBT;
+    D[r][c] = (r < nb && c < nb) ? base[(int64_t)r * nd.f + c] : (r == c ? one : zero);
   }
   __syncthreads();
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
   for (int i = 0; i < nb; ++i) {
-    if (threadIdx.x == 0 && s_abs(D[i][i]) < tau) {
-      D[i][i] = s_real(D[i][i], tau);
+    S piv = D[i][i];
+    const bool pert = s_abs(piv) < tau;
+    if (pert) piv = s_real(piv, tau);
+    S l[RB], u[RB];
+#pragma unroll
+    for (int a = 0; a < RB; ++a) {
+      const int r = ty + 16 * a;
+      l[a] = r > i ? s_div(D[r][i], piv) : zero;
+    }
+#pragma unroll
+    for (int b = 0; b < RB; ++b) u[b] = D[i][tx + 16 * b];
+    __syncthreads();
+    if (threadIdx.x == 0 && pert) {
+      D[i][i] = piv;
       atomicAdd(n_perturbed, 1);
     }
-    __syncthreads();
-    for (int r = i + 1 + threadIdx.x; r < nb; r += blockDim.x) D[r][i] = s_div(D[r][i], D[i][i]);
-    __syncthreads();
-    const int w = nb - i - 1;
-    for (int t = threadIdx.x; t < w * w; t += blockDim.x) {
-      const int r = i + 1 + t / w, c = i + 1 + t % w;
-      D[r][c] = s_fms(D[r][c], D[r][i], D[i][c]);
+#pragma unroll
+    for (int a = 0; a < RB; ++a) {
+      const int r = ty + 16 * a;
+      if (r <= i) continue;
+#pragma unroll
+      for (int b = 0; b < RB; ++b) {
+        const int c = tx + 16 * b;
+        if (c > i)
+          D[r][c] = s_fms(D[r][c], l[a], u[b]);
+        else if (c == i)
+          D[r][c] = l[a];
+      }
     }
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+  for (int t = threadIdx.x; t < nb * nb; t += 256) {
     const int r = t / nb, c = t % nb;
     base[(int64_t)r * nd.f + c] = D[r][c];
   }
 }
 
-// panel solves: rows below the diagonal block (X U11 = A, thread per row)
-// and columns right of it (L11 X = A, thread per column); TR per block.
-// Dynamic shared memory: D[NBT][NBT+1] then T[TR][NBT+1].
-template <typename S, int NBT, int TR>
-__global__ void panel_trsm_kernel(const int32_t* __restrict__ list, int count,
-                                  const DNode* __restrict__ nodes, S* __restrict__ arena, int p0) {
+// panel solves by substitution: rows below the diagonal block
+// (X U11 = A21, non-unit upper) and columns right of it (L11 X = A12, unit
+// lower), 64 rows (or columns) per block.  Four lanes share a row: lane q
+// holds the entries q, q+4, ... in registers; at step j the owner of entry j
+// finishes it and hands it to the other three by a shuffle, so no block
+// barrier is needed inside the substitution.
+// Dynamic shared memory: D[NBT][NBT+1] (the factored block) then T[64][NBT+1].
+template <typename S, int NBT>
+__global__ void __launch_bounds__(256) panel_trsm_kernel(const int32_t* __restrict__ list,
+                                                         int count,
+                                                         const DNode* __restrict__ nodes,
+                                                         S* __restrict__ arena, int p0) {
+  constexpr int CPT = NBT / 4;
   extern __shared__ __align__(16) unsigned char trsm_smem[];
   S(*D)[NBT + 1] = reinterpret_cast<S(*)[NBT + 1]>(trsm_smem);
-  S(*T)[NBT + 1] = reinterpret_cast<S(*)[NBT + 1]>(trsm_smem + sizeof(S) * NBT * (NBT + 1));
+  S(*T)[NBT + 1] = D + NBT;
   const int fi = blockIdx.y;
   if (fi >= count) return;
   const DNode nd = nodes[list[fi]];
@@ -239,55 +297,70 @@ __global__ void panel_trsm_kernel(const int32_t* __restrict__ list, int count,
   if (nb <= 0) return;
   const int rest = nd.f - p0 - nb;
   if (rest <= 0) return;
-  const int tiles = (rest + TR - 1) / TR;
+  const int tiles = (rest + 63) / 64;
   int tile = blockIdx.x;
   const bool rows = tile < tiles;
   if (!rows) tile -= tiles;
   if (tile >= tiles) return;
-  S* base = arena + nd.off + (int64_t)p0 * nd.f + p0;
-  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x)
-    D[t / nb][t % nb] = base[(int64_t)(t / nb) * nd.f + t % nb];
-  const int first = p0 + nb + tile * TR;
-  const int cnt = min(TR, nd.f - first);
+  const int first = p0 + nb + tile * 64;
+  const int cnt = min(64, nd.f - first);
+  S* F = arena + nd.off;
+  const S zero = s_zero(S()), one = s_one(S());
+  for (int t = threadIdx.x; t < NBT * NBT; t += 256) {
+    const int r = t / NBT, c = t % NBT;
+    D[r][c] = (r < nb && c < nb) ? F[(int64_t)(p0 + r) * nd.f + p0 + c] : (r == c ? one : zero);
+  }
   if (rows) {
-    // cnt rows x nb columns (coalesced along the row)
-    for (int t = threadIdx.x; t < cnt * nb; t += blockDim.x) {
-      const int r = t / nb, c = t % nb;
-      T[r][c] = arena[nd.off + (int64_t)(first + r) * nd.f + p0 + c];
-    }
-    __syncthreads();
-    if (threadIdx.x < cnt) {
-      const int r = threadIdx.x;
-      for (int j = 0; j < nb; ++j) {
-        S x = T[r][j];
-        for (int i = 0; i < j; ++i) x = s_fms(x, T[r][i], D[i][j]);
-        T[r][j] = s_div(x, D[j][j]);
-      }
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < cnt * nb; t += blockDim.x) {
-      const int r = t / nb, c = t % nb;
-      arena[nd.off + (int64_t)(first + r) * nd.f + p0 + c] = T[r][c];
+    for (int t = threadIdx.x; t < 64 * NBT; t += 256) {
+      const int r = t / NBT, c = t % NBT;
+      T[r][c] = (r < cnt && c < nb) ? F[(int64_t)(first + r) * nd.f + p0 + c] : zero;
     }
   } else {
-    // nb rows x cnt columns, stored transposed: T[col][i]
-    for (int t = threadIdx.x; t < cnt * nb; t += blockDim.x) {
-      const int i = t / cnt, c = t % cnt;
-      T[c][i] = arena[nd.off + (int64_t)(p0 + i) * nd.f + first + c];
+    for (int t = threadIdx.x; t < NBT * 64; t += 256) {
+      const int m = t / 64, c = t % 64;
+      T[c][m] = (m < nb && c < cnt) ? F[(int64_t)(p0 + m) * nd.f + first + c] : zero;
     }
-    __syncthreads();
-    if (threadIdx.x < cnt) {
-      const int c = threadIdx.x;
-      for (int i = 1; i < nb; ++i) {
-        S x = T[c][i];
-        for (int j = 0; j < i; ++j) x = s_fms(x, D[i][j], T[c][j]);
-        T[c][i] = x;
-      }
+  }
+  __syncthreads();
+  const int r = threadIdx.x >> 2, q = threadIdx.x & 3;
+  const int lane = threadIdx.x & 31, grp = lane & ~3;
+  S v[CPT];
+#pragma unroll
+  for (int s = 0; s < CPT; ++s) v[s] = T[r][q + 4 * s];
+  if (rows) {
+    // x_j = (a_j - sum_{i<j} x_i U_ij) / U_jj, right-looking over j
+#pragma unroll
+    for (int j = 0; j < NBT; ++j) {
+      if (j >= nb) break;
+      if (q == (j & 3)) v[j >> 2] = s_div(v[j >> 2], D[j][j]);
+      const S xj = s_shfl(v[j >> 2], grp | (j & 3));
+#pragma unroll
+      for (int s = (j >> 2); s < CPT; ++s)
+        if (q + 4 * s > j) v[s] = s_fms(v[s], xj, D[j][q + 4 * s]);
     }
-    __syncthreads();
-    for (int t = threadIdx.x; t < cnt * nb; t += blockDim.x) {
-      const int i = t / cnt, c = t % cnt;
-      arena[nd.off + (int64_t)(p0 + i) * nd.f + first + c] = T[c][i];
+  } else {
+    // x_i = a_i - sum_{m<i} L_im x_m (unit diagonal)
+#pragma unroll
+    for (int m = 0; m < NBT; ++m) {
+      if (m >= nb) break;
+      const S xm = s_shfl(v[m >> 2], grp | (m & 3));
+#pragma unroll
+      for (int s = (m >> 2); s < CPT; ++s)
+        if (q + 4 * s > m) v[s] = s_fms(v[s], D[q + 4 * s][m], xm);
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < CPT; ++s) T[r][q + 4 * s] = v[s];
+  __syncthreads();
+  if (rows) {
+    for (int t = threadIdx.x; t < 64 * NBT; t += 256) {
+      const int rr = t / NBT, c = t % NBT;
+      if (rr < cnt && c < nb) F[(int64_t)(first + rr) * nd.f + p0 + c] = T[rr][c];
+    }
+  } else {
+    for (int t = threadIdx.x; t < NBT * 64; t += 256) {
+      const int m = t / 64, c = t % 64;
+      if (m < nb && c < cnt) F[(int64_t)(p0 + m) * nd.f + first + c] = T[c][m];
     }
   }
 }
@@ -315,6 +388,9 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(const int32_t* __restr
   if ((int)blockIdx.x >= tpd * tpd) return;
   const int ti = blockIdx.x / tpd, tj = blockIdx.x % tpd;
   const int i0 = lo + ti * 64, j0 = lo + tj * 64;
+  // the (k,f) x (k,f) Schur block is updated once, after all panels, by
+  // schur_update_kernel with the full K = k (see factor_t)
+  if (i0 >= nd.k && j0 >= nd.k) return;
   S* F = arena + nd.off;
   for (int t = threadIdx.x; t < 64 * NBT; t += 256) {
     const int i = t / NBT, c = t % NBT;
@@ -337,7 +413,8 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(const int32_t* __restr
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
       const int j = j0 + tx + 16 * b;
-      cv[a][b] = (i < nd.f && j < nd.f) ? F[(int64_t)i * nd.f + j] : s_zero(S());
+      cv[a][b] = (i < nd.f && j < nd.f && (i < nd.k || j < nd.k)) ? F[(int64_t)i * nd.f + j]
+                                                                 : s_zero(S());
     }
   }
   for (int t = 0; t < nb; ++t) {
@@ -358,8 +435,70 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(const int32_t* __restr
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
       const int j = j0 + tx + 16 * b;
-      if (j >= nd.f) continue;
+      if (j >= nd.f || (i >= nd.k && j >= nd.k)) continue;
       F[(int64_t)i * nd.f + j] = s_add(cv[a][b], acc[a][b]);
+    }
+  }
+}
+
+// Schur block of a front, F[k:f, k:f] -= F[k:f, 0:k] F[0:k, k:f], once after
+// the pivot panels: one 64x64 tile per block, K = k in chunks of KC
+// (dynamic shared memory As[KC][65], Bs[KC][64]).
+template <typename S, int KC>
+__global__ void __launch_bounds__(256) schur_update_kernel(const int32_t* __restrict__ list,
+                                                           int count,
+                                                           const DNode* __restrict__ nodes,
+                                                           S* __restrict__ arena) {
+  extern __shared__ __align__(16) unsigned char schur_smem[];
+  S(*As)[65] = reinterpret_cast<S(*)[65]>(schur_smem);
+  S(*Bs)[64] = reinterpret_cast<S(*)[64]>(schur_smem + sizeof(S) * KC * 65);
+  const int fi = blockIdx.y;
+  if (fi >= count) return;
+  const DNode nd = nodes[list[fi]];
+  const int u = nd.f - nd.k;
+  if (u <= 0 || nd.k <= 0) return;
+  const int tpd = (u + 63) / 64;
+  if ((int)blockIdx.x >= tpd * tpd) return;
+  const int i0 = nd.k + (blockIdx.x / tpd) * 64, j0 = nd.k + (blockIdx.x % tpd) * 64;
+  S* F = arena + nd.off;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  S acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = s_zero(S());
+  for (int kc = 0; kc < nd.k; kc += KC) {
+    const int kn = min(KC, nd.k - kc);
+    __syncthreads();
+    for (int t = threadIdx.x; t < 64 * KC; t += 256) {
+      const int i = t / KC, c = t % KC;
+      As[c][i] = (i0 + i < nd.f && c < kn) ? F[(int64_t)(i0 + i) * nd.f + kc + c] : s_zero(S());
+      const int r = t / 64, j = t % 64;
+      Bs[r][j] = (j0 + j < nd.f && r < kn) ? F[(int64_t)(kc + r) * nd.f + j0 + j] : s_zero(S());
+    }
+    __syncthreads();
+    for (int t = 0; t < kn; ++t) {
+      S av[4], bv[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) av[a] = As[t][ty + 16 * a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) bv[b] = Bs[t][tx + 16 * b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = s_fms(acc[a][b], av[a], bv[b]);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int i = i0 + ty + 16 * a;
+    if (i >= nd.f) continue;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int j = j0 + tx + 16 * b;
+      if (j >= nd.f) continue;
+      S* c = F + (int64_t)i * nd.f + j;
+      *c = s_add(*c, acc[a][b]);
     }
   }
 }
@@ -391,11 +530,14 @@ __device__ __forceinline__ S warp_row_dot(const S* __restrict__ row, const S* __
   return acc;
 }
 
-// forward: y_V = L11^-1 y_V (unit lower), one block per front
+// forward: y_V = L11^-1 y_V (unit lower), one block per front, 32 rows at a
+// time: the rows' products with the solved part (a warp per row), then the
+// 32 x 32 diagonal tile, staged in shared memory, by one warp
 template <typename S>
 __global__ void __launch_bounds__(1024) fwd_trsv_kernel(const int32_t* __restrict__ list, int count,
                                 const DNode* __restrict__ nodes, const S* __restrict__ arena,
                                 S* __restrict__ x) {
+  __shared__ S Dt[32][33];
   const int fi = blockIdx.x;
   if (fi >= count) return;
   const DNode nd = nodes[list[fi]];
@@ -403,23 +545,26 @@ __global__ void __launch_bounds__(1024) fwd_trsv_kernel(const int32_t* __restric
   S* y = x + nd.start;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int b0 = 0; b0 < nd.k; b0 += 32) {
+    const int m = min(32, nd.k - b0);
+    for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) {
+      const int i = t >> 5, j = t & 31;
+      Dt[i][j] = (i < m && j < i) ? F[(int64_t)(b0 + i) * nd.f + b0 + j] : s_zero(S());
+    }
     // subtract the contributions of the solved rows [0, b0) from rows of this block
     if (b0 > 0) {
-      for (int r = b0 + warp; r < min(b0 + 32, nd.k); r += nw) {
+      for (int r = b0 + warp; r < b0 + m; r += nw) {
         const S acc = warp_row_dot<S, false>(F + (int64_t)r * nd.f, y, nullptr, 0, b0, lane);
         if (lane == 0) y[r] = s_add(y[r], acc);
       }
-      __syncthreads();
     }
+    __syncthreads();
     if (warp == 0) {
-      const int r = b0 + lane;
-      S v = r < nd.k ? y[r] : s_zero(S());
-      const int m = min(32, nd.k - b0);
+      S v = lane < m ? y[b0 + lane] : s_zero(S());
       for (int j = 0; j < m; ++j) {
         const S yj = s_shfl(v, j);
-        if (lane > j && r < nd.k) v = s_fms(v, F[(int64_t)r * nd.f + b0 + j], yj);
+        if (lane > j) v = s_fms(v, Dt[lane][j], yj);
       }
-      if (r < nd.k) y[r] = v;
+      if (lane < m) y[b0 + lane] = v;
     }
     __syncthreads();
   }
@@ -464,11 +609,13 @@ __global__ void bwd_gemv_kernel(const int32_t* __restrict__ list, int count,
   }
 }
 
-// backward: x_V = U11^-1 y_V (upper, non-unit), one block per front
+// backward: x_V = U11^-1 y_V (upper, non-unit), one block per front, 32
+// rows at a time from the bottom, the diagonal tile staged in shared memory
 template <typename S>
 __global__ void __launch_bounds__(1024) bwd_trsv_kernel(const int32_t* __restrict__ list, int count,
                                 const DNode* __restrict__ nodes, const S* __restrict__ arena,
                                 S* __restrict__ x) {
+  __shared__ S Dt[32][33];
   const int fi = blockIdx.x;
   if (fi >= count) return;
   const DNode nd = nodes[list[fi]];
@@ -477,23 +624,27 @@ __global__ void __launch_bounds__(1024) bwd_trsv_kernel(const int32_t* __restric
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int nblk = (nd.k + 31) / 32;
   for (int bi = nblk - 1; bi >= 0; --bi) {
-    const int b0 = bi * 32, b1 = min(b0 + 32, nd.k);
+    const int b0 = bi * 32, b1 = min(b0 + 32, nd.k), m = b1 - b0;
+    for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) {
+      const int i = t >> 5, j = t & 31;
+      Dt[i][j] = (i < m && j < m && j >= i) ? F[(int64_t)(b0 + i) * nd.f + b0 + j]
+                                            : s_zero(S());
+    }
     if (b1 < nd.k) {
       for (int r = b0 + warp; r < b1; r += nw) {
         const S acc = warp_row_dot<S, false>(F + (int64_t)r * nd.f, y, nullptr, b1, nd.k, lane);
         if (lane == 0) y[r] = s_add(y[r], acc);
       }
-      __syncthreads();
     }
+    __syncthreads();
     if (warp == 0) {
-      const int r = b0 + lane;
-      S v = r < b1 ? y[r] : s_zero(S());
-      for (int j = b1 - 1; j >= b0; --j) {
-        if (r == j) v = s_div(v, F[(int64_t)r * nd.f + r]);
-        const S xj = s_shfl(v, j - b0);
-        if (r < j) v = s_fms(v, F[(int64_t)r * nd.f + j], xj);
+      S v = lane < m ? y[b0 + lane] : s_zero(S());
+      for (int j = m - 1; j >= 0; --j) {
+        if (lane == j) v = s_div(v, Dt[j][j]);
+        const S xj = s_shfl(v, j);
+        if (lane < j) v = s_fms(v, Dt[lane][j], xj);
       }
-      if (r < b1) y[r] = v;
+      if (lane < m) y[b0 + lane] = v;
     }
     __syncthreads();
   }
@@ -606,9 +757,10 @@ void free_dev(MFDevice& d) {
 // single-precision product runs with FP32-accurate BF16x9 emulation on the
 // tensor cores when cuBLAS offers it for the type, else plain FP32.
 template <typename S>
-cudaError_t blas_update(MFDevice& d, S* F, int64_t f, int p0, int nb, cudaStream_t st) {
-  const int64_t lo = p0 + nb, rest = f - lo;
-  if (rest <= 0) return cudaSuccess;
+cudaError_t blas_gemm(MFDevice& d, const S* U, const S* Lb, S* C, int64_t rows, int64_t cols,
+                      int64_t kk, int64_t f, cudaStream_t st) {
+  // row-major C[rows x cols] -= Lb[rows x kk] U[kk x cols], leading dimension f
+  if (rows <= 0 || cols <= 0 || kk <= 0) return cudaSuccess;
   if (!d.blas) {
     if (cublasCreate(&d.blas) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
   }
@@ -618,12 +770,9 @@ cudaError_t blas_update(MFDevice& d, S* F, int64_t f, int p0, int nb, cudaStream
   const float2 am1 = make_float2(-1.f, 0.f), one = make_float2(1.f, 0.f);
   const void* alpha = &am1;
   const void* beta = &one;
-  const S* A = F + p0 * f + lo;  // U block
-  const S* B = F + lo * f + p0;  // L block
-  S* C = F + lo * f + lo;
   for (int attempt = 0; attempt < 2; ++attempt) {
-    cublasStatus_t s = cublasGemmEx(d.blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, (int)rest, nb,
-                                    alpha, A, t, (int)f, B, t, (int)f, beta, C, t, (int)f,
+    cublasStatus_t s = cublasGemmEx(d.blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)cols, (int)rows, (int)kk,
+                                    alpha, U, t, (int)f, Lb, t, (int)f, beta, C, t, (int)f,
                                     d.blas_compute, CUBLAS_GEMM_DEFAULT);
     if (s == CUBLAS_STATUS_SUCCESS) {
       count_launch(1);
@@ -634,6 +783,33 @@ cudaError_t blas_update(MFDevice& d, S* F, int64_t f, int p0, int nb, cudaStream
     d.blas_compute = CUBLAS_COMPUTE_32F;
   }
   return cudaErrorUnknown;
+}
+
+// panel-step update of one front by cuBLAS in super-panels of width
+// kSuperPanel: the panel step at p0 updates only the rows and columns of its
+// super-panel [sp0, bnd), and the last panel of a super-panel applies the
+// trailing block F[bnd:f, bnd:f] -= L[bnd:f, sp0:bnd] U[sp0:bnd, bnd:f] as one
+// GEMM with K = bnd - sp0 (this includes the (k,f) x (k,f) Schur block).
+constexpr int kSuperPanel = 512;
+
+template <typename S>
+cudaError_t blas_update(MFDevice& d, S* F, int64_t f, int64_t k, int p0, int nb,
+                        cudaStream_t st) {
+  const int64_t lo = p0 + nb;
+  if (f - lo <= 0) return cudaSuccess;
+  const int64_t sp0 = (p0 / kSuperPanel) * (int64_t)kSuperPanel;
+  const int64_t bnd = std::min<int64_t>(k, sp0 + kSuperPanel);
+  // rows [lo, f) x cols [lo, bnd)
+  cudaError_t e = blas_gemm<S>(d, F + p0 * f + lo, F + lo * f + p0, F + lo * f + lo, f - lo,
+                               bnd - lo, nb, f, st);
+  if (e != cudaSuccess) return e;
+  // rows [lo, bnd) x cols [bnd, f)
+  e = blas_gemm<S>(d, F + p0 * f + bnd, F + lo * f + p0, F + lo * f + bnd, bnd - lo, f - bnd, nb,
+                   f, st);
+  if (e != cudaSuccess || lo != bnd) return e;
+  // super-panel complete: trailing block with K = bnd - sp0
+  return blas_gemm<S>(d, F + sp0 * f + bnd, F + bnd * f + sp0, F + bnd * f + bnd, f - bnd,
+                      f - bnd, bnd - sp0, f, st);
 }
 
 cudaError_t setup_device(MFHandle& h, int dtype) {
@@ -700,15 +876,19 @@ template <typename S>
 cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st) {
   // panel width 64 (32 for complex double, whose tiles would not fit)
   constexpr int NBT = sizeof(S) <= 8 ? 64 : 32;
-  constexpr int TR = NBT == 64 ? 64 : 128;
-  const size_t trsm_smem = sizeof(S) * (size_t)(NBT + TR) * (NBT + 1);
+  const size_t trsm_smem = sizeof(S) * (size_t)(NBT + 64) * (NBT + 1);
   const size_t gemm_smem = sizeof(S) * (size_t)NBT * (65 + 64);
+  constexpr int kSchurKC = 32;
+  const size_t schur_smem = sizeof(S) * (size_t)kSchurKC * (65 + 64);
   {
-    cudaError_t ea = cudaFuncSetAttribute(panel_trsm_kernel<S, NBT, TR>,
+    cudaError_t ea = cudaFuncSetAttribute(panel_trsm_kernel<S, NBT>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trsm_smem);
     if (ea == cudaSuccess)
       ea = cudaFuncSetAttribute(gemm_update_kernel<S, NBT>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem);
+    if (ea == cudaSuccess)
+      ea = cudaFuncSetAttribute(schur_update_kernel<S, kSchurKC>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)schur_smem);
     if (ea != cudaSuccess) return ea;
   }
   MFDevice& d = h.dev;
@@ -744,6 +924,10 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
       extend_add_kernel<S><<<grid, 128, 0, st>>>(L.d_kids[c], nk, d.d_nodes, d.d_ea, arena);
       count_launch(1);
     }
+    // few large fronts: cuBLAS GEMMs per front with super-panel trailing
+    // updates; otherwise batched kernels and one Schur update per level
+    const int nall = (int)L.nodes_by_k.size();
+    const bool use_blas = kSinglePrecision<S> && nall <= kBlasFronts;
     for (int p0 = 0; p0 < L.max_k; p0 += NBT) {
       // active fronts: prefix of the k-descending list with k > p0
       int cnt = 0;
@@ -753,17 +937,18 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
                                                   tau, d.d_flag);
       count_launch(1);
       const int rest = std::max(0, L.max_rest - p0 - 1);
-      const int tiles = (rest + TR - 1) / TR;
+      const int tiles = (rest + 63) / 64;
       if (tiles > 0) {
         dim3 g1(2 * tiles, cnt);
-        panel_trsm_kernel<S, NBT, TR><<<g1, TR, trsm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0);
+        panel_trsm_kernel<S, NBT><<<g1, 256, trsm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena,
+                                                               p0);
         count_launch(1);
-        if (kSinglePrecision<S> && cnt <= kBlasFronts) {
+        if (use_blas) {
           // few large fronts: one cuBLAS GEMM per front
           for (int q = 0; q < cnt; ++q) {
             const MFNode& nd = s.nodes[L.nodes_by_k[q]];
             const int nbq = (int)std::min<int64_t>(NBT, nd.k - p0);
-            e = blas_update<S>(d, arena + nd.front_off, nd.f, p0, nbq, st);
+            e = blas_update<S>(d, arena + nd.front_off, nd.f, nd.k, p0, nbq, st);
             if (e != cudaSuccess) return e;
           }
         } else {
@@ -774,6 +959,15 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
           count_launch(1);
         }
       }
+    }
+    // Schur blocks F[k:f, k:f] -= L21 U12 with the full K = k, before the
+    // parent level's extend-add reads them
+    if (!use_blas && L.max_u > 0 && nall > 0) {
+      const int tpd = (L.max_u + 63) / 64;
+      dim3 g3(tpd * tpd, nall);
+      schur_update_kernel<S, kSchurKC><<<g3, 256, schur_smem, st>>>(L.d_nodes, nall, d.d_nodes,
+                                                                     arena);
+      count_launch(1);
     }
     if (prof) {
       cudaEventRecord(ev[1], st);
