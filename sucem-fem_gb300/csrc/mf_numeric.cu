@@ -71,22 +71,6 @@ __device__ __forceinline__ float2 s_mul(float2 a, float2 b) {
 __device__ __forceinline__ double2 s_mul(double2 a, double2 b) {
   return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
 }
-__device__ __forceinline__ float s_fma(float c, float a, float b) { return fmaf(a, b, c); }
-__device__ __forceinline__ double s_fma(double c, double a, double b) { return fma(a, b, c); }
-__device__ __forceinline__ float2 s_fma(float2 c, float2 a, float2 b) {
-  c.x = fmaf(a.x, b.x, c.x);
-  c.x = fmaf(-a.y, b.y, c.x);
-  c.y = fmaf(a.x, b.y, c.y);
-  c.y = fmaf(a.y, b.x, c.y);
-  return c;
-}
-__device__ __forceinline__ double2 s_fma(double2 c, double2 a, double2 b) {
-  c.x = fma(a.x, b.x, c.x);
-  c.x = fma(-a.y, b.y, c.x);
-  c.y = fma(a.x, b.y, c.y);
-  c.y = fma(a.y, b.x, c.y);
-  return c;
-}
 __device__ __forceinline__ float s_add(float a, float b) { return a + b; }
 __device__ __forceinline__ double s_add(double a, double b) { return a + b; }
 __device__ __forceinline__ float2 s_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -530,124 +514,206 @@ __device__ __forceinline__ S warp_row_dot(const S* __restrict__ row, const S* __
   return acc;
 }
 
-// forward: y_V = L11^-1 y_V (unit lower), one block per front, 32 rows at a
-// time: the rows' products with the solved part (a warp per row), then the
-// 32 x 32 diagonal tile, staged in shared memory, by one warp
+// The solve walks the pivot block [0, k) of every front in sub-panels
+// [c0, c1) of P = solve_panel<S>() columns (c0 = j * P for sub-step j), so
+// the dense triangular work of a large front is spread over many blocks:
+// a one-block triangular solve of the sub-panel's diagonal tile (held whole
+// in shared memory), then the products of the sub-panel with the rows
+// (forward) or columns (backward) outside it, a warp per row over the GPU.
+template <typename S>
+__host__ __device__ constexpr int solve_panel() {
+  return sizeof(S) == 16 ? 64 : 128;
+}
+constexpr int kTrsvThreads = 1024;      // block size of the sub-panel solves
+constexpr int kBwdChunk = 1024;         // columns per warp in the backward products
+
+// forward, sub-step j: y[c0:c1] = L[c0:c1, c0:c1]^-1 y[c0:c1] (unit lower),
+// one block per front: the strictly lower tile and y[c0:c1] are loaded into
+// shared memory, then 32 rows at a time: their products with the solved
+// rows (a warp per row), then the 32 x 32 diagonal part by one warp.
+// Dynamic shared memory: Dt[P][P+1], ys[P].
 template <typename S>
 __global__ void __launch_bounds__(1024) fwd_trsv_kernel(const int32_t* __restrict__ list, int count,
                                 const DNode* __restrict__ nodes, const S* __restrict__ arena,
-                                S* __restrict__ x) {
-  __shared__ S Dt[32][33];
+                                S* __restrict__ x, int j) {
+  constexpr int P = solve_panel<S>();
+  extern __shared__ __align__(16) unsigned char trsv_smem[];
+  S(*Dt)[P + 1] = reinterpret_cast<S(*)[P + 1]>(trsv_smem);
+  S* ys = reinterpret_cast<S*>(trsv_smem + sizeof(S) * P * (P + 1));
   const int fi = blockIdx.x;
   if (fi >= count) return;
   const DNode nd = nodes[list[fi]];
-  const S* F = arena + nd.off;
-  S* y = x + nd.start;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  for (int b0 = 0; b0 < nd.k; b0 += 32) {
-    const int m = min(32, nd.k - b0);
-    for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) {
-      const int i = t >> 5, j = t & 31;
-      Dt[i][j] = (i < m && j < i) ? F[(int64_t)(b0 + i) * nd.f + b0 + j] : s_zero(S());
-    }
-    // subtract the contributions of the solved rows [0, b0) from rows of this block
+  const int c0 = j * P;
+  if (nd.k <= c0) return;
+  const int m = min(nd.k, c0 + P) - c0;
+  const S* F = arena + nd.off + (int64_t)c0 * nd.f + c0;
+  S* y = x + nd.start + c0;
+#pragma unroll
+  for (int it = 0; it < P * P / kTrsvThreads; ++it) {
+    const int t = it * kTrsvThreads + threadIdx.x;
+    const int i = t / P, jj = t % P;
+    if (i < m && jj < i) Dt[i][jj] = F[(int64_t)i * nd.f + jj];
+  }
+  for (int t = threadIdx.x; t < m; t += kTrsvThreads) ys[t] = y[t];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = kTrsvThreads >> 5;
+  for (int b0 = 0; b0 < m; b0 += 32) {
+    const int mb = min(32, m - b0);
     if (b0 > 0) {
-      for (int r = b0 + warp; r < b0 + m; r += nw) {
-        const S acc = warp_row_dot<S, false>(F + (int64_t)r * nd.f, y, nullptr, 0, b0, lane);
-        if (lane == 0) y[r] = s_add(y[r], acc);
+      for (int r = b0 + warp; r < b0 + mb; r += nw) {
+        S acc = s_zero(S());
+        for (int c = lane; c < b0; c += 32) acc = s_fms(acc, Dt[r][c], ys[c]);
+        for (int o = 16; o > 0; o >>= 1) acc = s_add(acc, s_shfl_down(acc, o));
+        if (lane == 0) ys[r] = s_add(ys[r], acc);
       }
+      __syncthreads();
     }
-    __syncthreads();
     if (warp == 0) {
-      S v = lane < m ? y[b0 + lane] : s_zero(S());
-      for (int j = 0; j < m; ++j) {
-        const S yj = s_shfl(v, j);
-        if (lane > j) v = s_fms(v, Dt[lane][j], yj);
+      const int rl = min(lane, mb - 1);
+      S v = lane < mb ? ys[b0 + lane] : s_zero(S());
+#pragma unroll
+      for (int jj = 0; jj < 31; ++jj) {
+        const S yj = s_shfl(v, jj);
+        if (lane > jj && lane < mb) v = s_fms(v, Dt[b0 + rl][b0 + jj], yj);
       }
-      if (lane < m) y[b0 + lane] = v;
+      if (lane < mb) ys[b0 + lane] = v;
     }
     __syncthreads();
   }
+  for (int t = threadIdx.x; t < m; t += kTrsvThreads) y[t] = ys[t];
 }
 
-// forward update of the ancestors: x[U[r]] -= L21[r,:] . y_V (warp per row)
+// forward, sub-step j: rows r in [c1, f) of the front take
+// -= L[r, c0:c1] . y[c0:c1]; rows inside the pivot block update y (one
+// writer), rows of the update set go to the ancestors' x[U[r - k]]
+// (atomic, sibling fronts share ancestors); a warp per row
 template <typename S>
 __global__ void fwd_gemv_kernel(const int32_t* __restrict__ list, int count,
                                 const DNode* __restrict__ nodes, const int32_t* __restrict__ U,
-                                const S* __restrict__ arena, S* __restrict__ x) {
+                                const S* __restrict__ arena, S* __restrict__ x, int j) {
+  constexpr int P = solve_panel<S>();
   const int fi = blockIdx.y;
   if (fi >= count) return;
   const DNode nd = nodes[list[fi]];
-  const int u = nd.f - nd.k;
+  const int c0 = j * P;
+  if (nd.k <= c0) return;
+  const int c1 = min(nd.k, c0 + P);
+  const int rows = nd.f - c1;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const S* y = x + nd.start;
-  for (int r = warp; r < u; r += nwarps) {
-    const S* row = arena + nd.off + (int64_t)(nd.k + r) * nd.f;
-    const S acc = warp_row_dot<S, false>(row, y, nullptr, 0, nd.k, lane);
-    if (lane == 0) s_atomic_sub(&x[U[nd.u_off + r]], s_fms(s_zero(S()), acc, s_real(S(), 1.0)));
+  S* y = x + nd.start;
+  for (int q = warp; q < rows; q += nwarps) {
+    const int r = c1 + q;
+    const S* row = arena + nd.off + (int64_t)r * nd.f;
+    const S acc = warp_row_dot<S, false>(row, y, nullptr, c0, c1, lane);
+    if (lane == 0) {
+      if (r < nd.k)
+        y[r] = s_add(y[r], acc);
+      else
+        s_atomic_sub(&x[U[nd.u_off + r - nd.k]], s_fms(s_zero(S()), acc, s_real(S(), 1.0)));
+    }
   }
 }
 
-// backward: y_V -= U12 . x_U (warp per row)
+// backward, sub-step j: rows r in [c0, c1) take -= U[r, c1:f] . x over the
+// columns outside the sub-panel (own variables y[c] for c < k, the
+// ancestors' x[U[c - k]] beyond); a warp per (row, kBwdChunk columns),
+// partial sums added atomically
 template <typename S>
 __global__ void bwd_gemv_kernel(const int32_t* __restrict__ list, int count,
                                 const DNode* __restrict__ nodes, const int32_t* __restrict__ U,
-                                const S* __restrict__ arena, S* __restrict__ x) {
+                                const S* __restrict__ arena, S* __restrict__ x, int j) {
+  constexpr int P = solve_panel<S>();
   const int fi = blockIdx.y;
   if (fi >= count) return;
   const DNode nd = nodes[list[fi]];
-  const int u = nd.f - nd.k;
-  if (u <= 0) return;
+  const int c0 = j * P;
+  if (nd.k <= c0) return;
+  const int c1 = min(nd.k, c0 + P);
+  if (c1 >= nd.f) return;
+  const int rows = c1 - c0, ncol = nd.f - c1;
+  const int nch = (ncol + kBwdChunk - 1) / kBwdChunk;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  S* y = x + nd.start;
   const int32_t* Ui = U + nd.u_off;
-  for (int r = warp; r < nd.k; r += nwarps) {
-    const S* row = arena + nd.off + (int64_t)r * nd.f + nd.k;
-    const S acc = warp_row_dot<S, true>(row, x, Ui, 0, u, lane);
-    if (lane == 0) x[nd.start + r] = s_add(x[nd.start + r], acc);
+  for (int w = warp; w < rows * nch; w += nwarps) {
+    const int r = c0 + w % rows, ch = w / rows;
+    const int lo = c1 + ch * kBwdChunk, hi = min(nd.f, lo + kBwdChunk);
+    const S* row = arena + nd.off + (int64_t)r * nd.f;
+    S acc = s_zero(S());
+    if (lo < nd.k) acc = warp_row_dot<S, false>(row, y, nullptr, lo, min(hi, nd.k), lane);
+    if (hi > nd.k)
+      acc = s_add(acc, warp_row_dot<S, true>(row + nd.k, x, Ui, max(lo, nd.k) - nd.k,
+                                             hi - nd.k, lane));
+    if (lane == 0) {
+      if (nch == 1)
+        y[r] = s_add(y[r], acc);
+      else
+        s_atomic_sub(&y[r], s_fms(s_zero(S()), acc, s_real(S(), 1.0)));
+    }
   }
 }
 
-// backward: x_V = U11^-1 y_V (upper, non-unit), one block per front, 32
-// rows at a time from the bottom, the diagonal tile staged in shared memory
+// backward, sub-step j: y[c0:c1] = U[c0:c1, c0:c1]^-1 y[c0:c1] (upper,
+// non-unit), one block per front, the upper tile and y in shared memory,
+// 32 rows at a time from the bottom; the reciprocals of the diagonal are
+// formed in parallel before each 32-row chain.
+// Dynamic shared memory: Dt[P][P+1], ys[P].
 template <typename S>
 __global__ void __launch_bounds__(1024) bwd_trsv_kernel(const int32_t* __restrict__ list, int count,
                                 const DNode* __restrict__ nodes, const S* __restrict__ arena,
-                                S* __restrict__ x) {
-  __shared__ S Dt[32][33];
+                                S* __restrict__ x, int j) {
+  constexpr int P = solve_panel<S>();
+  extern __shared__ __align__(16) unsigned char trsv_smem[];
+  S(*Dt)[P + 1] = reinterpret_cast<S(*)[P + 1]>(trsv_smem);
+  S* ys = reinterpret_cast<S*>(trsv_smem + sizeof(S) * P * (P + 1));
   const int fi = blockIdx.x;
   if (fi >= count) return;
   const DNode nd = nodes[list[fi]];
-  const S* F = arena + nd.off;
-  S* y = x + nd.start;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  const int nblk = (nd.k + 31) / 32;
+  const int c0 = j * P;
+  if (nd.k <= c0) return;
+  const int m = min(nd.k, c0 + P) - c0;
+  const S* F = arena + nd.off + (int64_t)c0 * nd.f + c0;
+  S* y = x + nd.start + c0;
+#pragma unroll
+  for (int it = 0; it < P * P / kTrsvThreads; ++it) {
+    const int t = it * kTrsvThreads + threadIdx.x;
+    const int i = t / P, jj = t % P;
+    if (i < m && jj >= i && jj < m) Dt[i][jj] = F[(int64_t)i * nd.f + jj];
+  }
+  for (int t = threadIdx.x; t < m; t += kTrsvThreads) ys[t] = y[t];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = kTrsvThreads >> 5;
+  const int nblk = (m + 31) / 32;
   for (int bi = nblk - 1; bi >= 0; --bi) {
-    const int b0 = bi * 32, b1 = min(b0 + 32, nd.k), m = b1 - b0;
-    for (int t = threadIdx.x; t < 32 * 32; t += blockDim.x) {
-      const int i = t >> 5, j = t & 31;
-      Dt[i][j] = (i < m && j < m && j >= i) ? F[(int64_t)(b0 + i) * nd.f + b0 + j]
-                                            : s_zero(S());
-    }
-    if (b1 < nd.k) {
+    const int b0 = bi * 32, b1 = min(b0 + 32, m), mb = b1 - b0;
+    if (b1 < m) {
       for (int r = b0 + warp; r < b1; r += nw) {
-        const S acc = warp_row_dot<S, false>(F + (int64_t)r * nd.f, y, nullptr, b1, nd.k, lane);
-        if (lane == 0) y[r] = s_add(y[r], acc);
+        S acc = s_zero(S());
+        for (int c = b1 + lane; c < m; c += 32) acc = s_fms(acc, Dt[r][c], ys[c]);
+        for (int o = 16; o > 0; o >>= 1) acc = s_add(acc, s_shfl_down(acc, o));
+        if (lane == 0) ys[r] = s_add(ys[r], acc);
       }
+      __syncthreads();
     }
-    __syncthreads();
     if (warp == 0) {
-      S v = lane < m ? y[b0 + lane] : s_zero(S());
-      for (int j = m - 1; j >= 0; --j) {
-        if (lane == j) v = s_div(v, Dt[j][j]);
-        const S xj = s_shfl(v, j);
-        if (lane < j) v = s_fms(v, Dt[lane][j], xj);
+      const int rl = min(lane, mb - 1);
+      const S rinv = lane < mb ? s_div(s_one(S()), Dt[b0 + lane][b0 + lane]) : s_zero(S());
+      S v = lane < mb ? ys[b0 + lane] : s_zero(S());
+#pragma unroll
+      for (int jj = 31; jj >= 0; --jj) {
+        if (jj < mb) {
+          if (lane == jj) v = s_mul(v, rinv);
+          const S xj = s_shfl(v, jj);
+          if (lane < jj) v = s_fms(v, Dt[b0 + rl][b0 + jj], xj);
+        }
       }
-      if (lane < m) y[b0 + lane] = v;
+      if (lane < mb) ys[b0 + lane] = v;
     }
     __syncthreads();
   }
+  for (int t = threadIdx.x; t < m; t += kTrsvThreads) y[t] = ys[t];
 }
 
 template <typename S, typename T>
@@ -704,6 +770,9 @@ struct MFDevice {
   int64_t* d_perm = nullptr;
   void* d_x = nullptr;              // solve work vector (new ordering)
   int* d_flag = nullptr;            // perturbed pivot count
+  cudaStream_t cap_stream = nullptr;  // private stream for capturing the solve graph
+  cudaGraphExec_t solve_exec = nullptr;
+  int solve_n = 0;                  // kernel launches in the solve graph
   std::vector<MFLevel> levels;
   bool factored = false;
   int perturbed = 0;
@@ -748,6 +817,8 @@ void free_dev(MFDevice& d) {
       if (L.d_kids[s]) cudaFree(L.d_kids[s]);
   }
   if (d.blas) cublasDestroy(d.blas);
+  if (d.solve_exec) cudaGraphExecDestroy(d.solve_exec);
+  if (d.cap_stream) cudaStreamDestroy(d.cap_stream);
   d = MFDevice();
 }
 
@@ -987,34 +1058,81 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
 }
 
 template <typename S>
-cudaError_t solve_t(MFHandle& h, cudaStream_t st) {
-  MFDevice& d = h.dev;
+cudaError_t solve_prepare() {
+  constexpr int P = solve_panel<S>();
+  const size_t smem = sizeof(S) * (size_t)P * (P + 2);
+  cudaError_t e = cudaFuncSetAttribute(fwd_trsv_kernel<S>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(bwd_trsv_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+  return e;
+}
+
+// the launches of one solve on the work vector d_x; returns their count
+template <typename S>
+int solve_launches(MFDevice& d, cudaStream_t st) {
+  constexpr int P = solve_panel<S>();
+  const size_t smem = sizeof(S) * (size_t)P * (P + 2);
   S* x = (S*)d.d_x;
   const S* arena = (const S*)d.arena;
+  int n = 0;
   for (size_t lv = 0; lv < d.levels.size(); ++lv) {
     const MFLevel& L = d.levels[lv];
     const int cnt = (int)L.nodes_by_k.size();
-    fwd_trsv_kernel<S><<<cnt, 1024, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x);
-    count_launch(1);
-    if (L.max_u > 0) {
-      // one warp per row of L21
-      dim3 g(std::max(1, std::min(256, (L.max_u + 7) / 8)), cnt);
-      fwd_gemv_kernel<S><<<g, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x);
-      count_launch(1);
+    const int nsub = (L.max_k + P - 1) / P;
+    for (int j = 0; j < nsub; ++j) {
+      fwd_trsv_kernel<S><<<cnt, kTrsvThreads, smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x, j);
+      const int rows = L.max_rest - std::min(L.max_k, j * P + 1);
+      dim3 g(std::max(1, std::min(512, (rows + 7) / 8)), cnt);
+      fwd_gemv_kernel<S><<<g, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x, j);
+      n += 2;
     }
   }
   for (int lv = (int)d.levels.size() - 1; lv >= 0; --lv) {
     const MFLevel& L = d.levels[lv];
     const int cnt = (int)L.nodes_by_k.size();
-    if (L.max_u > 0) {
-      dim3 g(std::max(1, std::min(256, (L.max_k + 7) / 8)), cnt);
-      bwd_gemv_kernel<S><<<g, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x);
-      count_launch(1);
+    const int nsub = (L.max_k + P - 1) / P;
+    for (int j = nsub - 1; j >= 0; --j) {
+      const int rows = std::min(P, L.max_k);
+      const int chunks = (L.max_rest - std::min(L.max_k, j * P + 1) + kBwdChunk - 1) / kBwdChunk;
+      dim3 g(std::max(1, std::min(512, (rows * std::max(chunks, 1) + 7) / 8)), cnt);
+      bwd_gemv_kernel<S><<<g, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x, j);
+      bwd_trsv_kernel<S><<<cnt, kTrsvThreads, smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x, j);
+      n += 2;
     }
-    bwd_trsv_kernel<S><<<cnt, 1024, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x);
-    count_launch(1);
   }
-  return cudaGetLastError();
+  return n;
+}
+
+// one solve on d_x: the launch sequence is fixed by the symbolic structure
+// and the device buffers, so it is captured once into a CUDA graph (on a
+// private stream) and replayed into the caller's stream afterwards
+template <typename S>
+cudaError_t solve_t(MFHandle& h, cudaStream_t st) {
+  MFDevice& d = h.dev;
+  cudaError_t e = cudaSuccess;
+  if (!d.solve_exec) {
+    e = solve_prepare<S>();
+    if (e != cudaSuccess) return e;
+    if (!d.cap_stream) e = cudaStreamCreateWithFlags(&d.cap_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+    cudaGraph_t g = nullptr;
+    e = cudaStreamBeginCapture(d.cap_stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    const int n = solve_launches<S>(d, d.cap_stream);
+    e = cudaStreamEndCapture(d.cap_stream, &g);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&d.solve_exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      d.solve_exec = nullptr;
+      return e;
+    }
+    d.solve_n = n;
+  }
+  e = cudaGraphLaunch(d.solve_exec, st);
+  count_launch(d.solve_n);
+  return e;
 }
 
 template <typename S, typename T>
