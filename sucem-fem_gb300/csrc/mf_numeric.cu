@@ -195,8 +195,11 @@ __global__ void max_abs_kernel(int64_t m, const S* __restrict__ v,
 
 // LU (no pivoting, static pivot replacement) of the nb x nb diagonal block;
 // pivots below rel_tol * max|a_ij| are replaced by that value.  16 x 16
-// threads, each owning the rows ty + 16a and columns tx + 16b of the block
-// (padded with the identity beyond nb), two barriers per pivot step.
+// threads, thread (tx, ty) holding rows tx + 16a and columns ty + 16b in
+// registers (the identity beyond nb).  At step i the owner of a_ii checks
+// and inverts the pivot, the owners of column i and row i publish them
+// through shared memory (double-buffered: one barrier per step), and every
+// thread updates its own entries.
 template <typename S, int NBT>
 __global__ void __launch_bounds__(256) diag_lu_kernel(const int32_t* __restrict__ list,
                                                       int count, const DNode* __restrict__ nodes,
@@ -204,7 +207,9 @@ __global__ void __launch_bounds__(256) diag_lu_kernel(const int32_t* __restrict_
                                                       const unsigned long long* __restrict__ amax,
                                                       double rel_tol, int* __restrict__ n_perturbed) {
   constexpr int RB = NBT / 16;
-  __shared__ S D[NBT][NBT + 1];
+  __shared__ S colbuf[2][NBT];
+  __shared__ S rowbuf[2][NBT];
+  __shared__ S pinv[2];
   const int fi = blockIdx.x;
   if (fi >= count) return;
   const DNode nd = nodes[list[fi]];
@@ -214,48 +219,69 @@ __global__ void __launch_bounds__(256) diag_lu_kernel(const int32_t* __restrict_
   const double tau = rel_tol * (am > 0 ? am : 1.0);
   S* base = arena + nd.off + (int64_t)p0 * nd.f + p0;
   const S zero = s_zero(S()), one = s_one(S());
-  for (int t = threadIdx.x; t < NBT * NBT; t += 256) {
-    const int r = t / NBT, c = t % NBT;
-    D[r][c] = (r < nb && c < nb) ? base[(int64_t)r * nd.f + c] : (r == c ? one : zero);
-  }
-  __syncthreads();
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  for (int i = 0; i < nb; ++i) {
-    S piv = D[i][i];
-    const bool pert = s_abs(piv) < tau;
-    if (pert) piv = s_real(piv, tau);
-    S l[RB], u[RB];
+  S R[RB][RB];  // R[a][b] = A[tx + 16a][ty + 16b]
 #pragma unroll
-    for (int a = 0; a < RB; ++a) {
-      const int r = ty + 16 * a;
-      l[a] = r > i ? s_div(D[r][i], piv) : zero;
+  for (int a = 0; a < RB; ++a)
+#pragma unroll
+    for (int b = 0; b < RB; ++b) {
+      const int r = tx + 16 * a, c = ty + 16 * b;
+      R[a][b] = (r < nb && c < nb) ? base[(int64_t)r * nd.f + c] : (r == c ? one : zero);
     }
+  // the 16-column groups are unrolled (register indices stay static), the
+  // steps inside a group are not (a fully unrolled kernel misses the
+  // instruction cache)
 #pragma unroll
-    for (int b = 0; b < RB; ++b) u[b] = D[i][tx + 16 * b];
+  for (int bi = 0; bi < RB; ++bi)
+#pragma unroll 1
+  for (int ii = 0; ii < 16; ++ii) {
+    const int i = bi * 16 + ii;
+    if (i >= nb) break;
+    const int par = i & 1;
+    if (tx == ii && ty == ii) {
+      S piv = R[bi][bi];
+      if (s_abs(piv) < tau) {
+        piv = s_real(piv, tau);
+        R[bi][bi] = piv;
+        atomicAdd(n_perturbed, 1);
+      }
+      pinv[par] = s_div(one, piv);
+    }
+    if (ty == ii) {
+#pragma unroll
+      for (int a = 0; a < RB; ++a) colbuf[par][tx + 16 * a] = R[a][bi];
+    }
+    if (tx == ii) {
+#pragma unroll
+      for (int b = 0; b < RB; ++b) rowbuf[par][ty + 16 * b] = R[bi][b];
+    }
     __syncthreads();
-    if (threadIdx.x == 0 && pert) {
-      D[i][i] = piv;
-      atomicAdd(n_perturbed, 1);
-    }
+    const S rinv = pinv[par];
+    S u[RB];
+#pragma unroll
+    for (int b = 0; b < RB; ++b) u[b] = rowbuf[par][ty + 16 * b];
 #pragma unroll
     for (int a = 0; a < RB; ++a) {
-      const int r = ty + 16 * a;
+      const int r = tx + 16 * a;
       if (r <= i) continue;
+      const S l = s_mul(colbuf[par][r], rinv);
 #pragma unroll
       for (int b = 0; b < RB; ++b) {
-        const int c = tx + 16 * b;
+        const int c = ty + 16 * b;
         if (c > i)
-          D[r][c] = s_fms(D[r][c], l[a], u[b]);
+          R[a][b] = s_fms(R[a][b], l, u[b]);
         else if (c == i)
-          D[r][c] = l[a];
+          R[a][b] = l;
       }
     }
-    __syncthreads();
   }
-  for (int t = threadIdx.x; t < nb * nb; t += 256) {
-    const int r = t / nb, c = t % nb;
-    base[(int64_t)r * nd.f + c] = D[r][c];
-  }
+#pragma unroll
+  for (int a = 0; a < RB; ++a)
+#pragma unroll
+    for (int b = 0; b < RB; ++b) {
+      const int r = tx + 16 * a, c = ty + 16 * b;
+      if (r < nb && c < nb) base[(int64_t)r * nd.f + c] = R[a][b];
+    }
 }
 
 // panel solves by substitution: rows below the diagonal block
@@ -290,19 +316,38 @@ __global__ void __launch_bounds__(256) panel_trsm_kernel(const int32_t* __restri
   const int cnt = min(64, nd.f - first);
   S* F = arena + nd.off;
   const S zero = s_zero(S()), one = s_one(S());
-  for (int t = threadIdx.x; t < NBT * NBT; t += 256) {
-    const int r = t / NBT, c = t % NBT;
-    D[r][c] = (r < nb && c < nb) ? F[(int64_t)(p0 + r) * nd.f + p0 + c] : (r == c ? one : zero);
-  }
-  if (rows) {
-    for (int t = threadIdx.x; t < 64 * NBT; t += 256) {
-      const int r = t / NBT, c = t % NBT;
-      T[r][c] = (r < cnt && c < nb) ? F[(int64_t)(first + r) * nd.f + p0 + c] : zero;
+  {
+    // all loads of the block issued before the first shared-memory store
+    constexpr int ND = NBT * NBT / 256, NT = 64 * NBT / 256;
+    S dv[ND], tv[NT];
+#pragma unroll
+    for (int it = 0; it < ND; ++it) {
+      const int t = it * 256 + threadIdx.x, r = t / NBT, c = t % NBT;
+      dv[it] = (r < nb && c < nb) ? F[(int64_t)(p0 + r) * nd.f + p0 + c] : (r == c ? one : zero);
     }
-  } else {
-    for (int t = threadIdx.x; t < NBT * 64; t += 256) {
-      const int m = t / 64, c = t % 64;
-      T[c][m] = (m < nb && c < cnt) ? F[(int64_t)(p0 + m) * nd.f + first + c] : zero;
+#pragma unroll
+    for (int it = 0; it < NT; ++it) {
+      const int t = it * 256 + threadIdx.x;
+      if (rows) {
+        const int r = t / NBT, c = t % NBT;
+        tv[it] = (r < cnt && c < nb) ? F[(int64_t)(first + r) * nd.f + p0 + c] : zero;
+      } else {
+        const int m = t / 64, c = t % 64;
+        tv[it] = (m < nb && c < cnt) ? F[(int64_t)(p0 + m) * nd.f + first + c] : zero;
+      }
+    }
+#pragma unroll
+    for (int it = 0; it < ND; ++it) {
+      const int t = it * 256 + threadIdx.x;
+      D[t / NBT][t % NBT] = dv[it];
+    }
+#pragma unroll
+    for (int it = 0; it < NT; ++it) {
+      const int t = it * 256 + threadIdx.x;
+      if (rows)
+        T[t / NBT][t % NBT] = tv[it];
+      else
+        T[t % 64][t / 64] = tv[it];
     }
   }
   __syncthreads();
@@ -311,27 +356,35 @@ __global__ void __launch_bounds__(256) panel_trsm_kernel(const int32_t* __restri
   S v[CPT];
 #pragma unroll
   for (int s = 0; s < CPT; ++s) v[s] = T[r][q + 4 * s];
+  // groups of four steps unrolled (register indices stay static), the
+  // steps inside a group not (keeps the kernel within the instruction cache)
   if (rows) {
     // x_j = (a_j - sum_{i<j} x_i U_ij) / U_jj, right-looking over j
 #pragma unroll
-    for (int j = 0; j < NBT; ++j) {
-      if (j >= nb) break;
-      if (q == (j & 3)) v[j >> 2] = s_div(v[j >> 2], D[j][j]);
-      const S xj = s_shfl(v[j >> 2], grp | (j & 3));
+    for (int sj = 0; sj < CPT; ++sj)
+#pragma unroll 1
+      for (int jq = 0; jq < 4; ++jq) {
+        const int j = 4 * sj + jq;
+        if (j >= nb) break;
+        if (q == jq) v[sj] = s_div(v[sj], D[j][j]);
+        const S xj = s_shfl(v[sj], grp | jq);
 #pragma unroll
-      for (int s = (j >> 2); s < CPT; ++s)
-        if (q + 4 * s > j) v[s] = s_fms(v[s], xj, D[j][q + 4 * s]);
-    }
+        for (int s = sj; s < CPT; ++s)
+          if (q + 4 * s > j) v[s] = s_fms(v[s], xj, D[j][q + 4 * s]);
+      }
   } else {
     // x_i = a_i - sum_{m<i} L_im x_m (unit diagonal)
 #pragma unroll
-    for (int m = 0; m < NBT; ++m) {
-      if (m >= nb) break;
-      const S xm = s_shfl(v[m >> 2], grp | (m & 3));
+    for (int sm = 0; sm < CPT; ++sm)
+#pragma unroll 1
+      for (int mq = 0; mq < 4; ++mq) {
+        const int m = 4 * sm + mq;
+        if (m >= nb) break;
+        const S xm = s_shfl(v[sm], grp | mq);
 #pragma unroll
-      for (int s = (m >> 2); s < CPT; ++s)
-        if (q + 4 * s > m) v[s] = s_fms(v[s], D[q + 4 * s][m], xm);
-    }
+        for (int s = sm; s < CPT; ++s)
+          if (q + 4 * s > m) v[s] = s_fms(v[s], D[q + 4 * s][m], xm);
+      }
   }
 #pragma unroll
   for (int s = 0; s < CPT; ++s) T[r][q + 4 * s] = v[s];
@@ -349,14 +402,15 @@ __global__ void __launch_bounds__(256) panel_trsm_kernel(const int32_t* __restri
   }
 }
 
-// trailing update C -= Lpanel * Upanel over the (f-p0-nb)^2 block,
-// 64x64 tile per block, 4x4 outputs per thread, K = nb <= NBT.
+// trailing update C -= Lpanel * Upanel over the (f-p0-nb)^2 block outside
+// [bnd, f)^2, 64x64 tile per block, 4x4 outputs per thread, K = nb <= NBT.
 // Dynamic shared memory: As[NBT][65] (As[t][i] = L[i][t]) then Bs[NBT][64].
 template <typename S, int NBT>
 __global__ void __launch_bounds__(256) gemm_update_kernel(const int32_t* __restrict__ list,
                                                           int count,
                                                           const DNode* __restrict__ nodes,
-                                                          S* __restrict__ arena, int p0) {
+                                                          S* __restrict__ arena, int p0,
+                                                          int sp) {
   extern __shared__ __align__(16) unsigned char gemm_smem[];
   S(*As)[65] = reinterpret_cast<S(*)[65]>(gemm_smem);
   S(*Bs)[64] = reinterpret_cast<S(*)[64]>(gemm_smem + sizeof(S) * NBT * 65);
@@ -374,13 +428,29 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(const int32_t* __restr
   const int i0 = lo + ti * 64, j0 = lo + tj * 64;
   // the (k,f) x (k,f) Schur block is updated once, after all panels, by
   // schur_update_kernel with the full K = k (see factor_t)
-  if (i0 >= nd.k && j0 >= nd.k) return;
+  // the block [bnd, f) x [bnd, f) is left for a later update with a longer
+  // K: the Schur block (bnd = k) or, with super-panels of width sp, the
+  // trailing block of the current super-panel
+  const int bnd = sp > 0 ? min(nd.k, (p0 / sp) * sp + sp) : nd.k;
+  if (i0 >= bnd && j0 >= bnd) return;
   S* F = arena + nd.off;
-  for (int t = threadIdx.x; t < 64 * NBT; t += 256) {
-    const int i = t / NBT, c = t % NBT;
-    As[c][i] = (i0 + i < nd.f && c < nb) ? F[(int64_t)(i0 + i) * nd.f + p0 + c] : s_zero(S());
-    const int r = t / 64, j = t % 64;
-    Bs[r][j] = (j0 + j < nd.f && r < nb) ? F[(int64_t)(p0 + r) * nd.f + j0 + j] : s_zero(S());
+  {
+    constexpr int NL = 64 * NBT / 256;
+    S av[NL], bv[NL];
+#pragma unroll
+    for (int it = 0; it < NL; ++it) {
+      const int t = it * 256 + threadIdx.x;
+      const int i = t / NBT, c = t % NBT;
+      av[it] = (i0 + i < nd.f && c < nb) ? F[(int64_t)(i0 + i) * nd.f + p0 + c] : s_zero(S());
+      const int r = t / 64, j = t % 64;
+      bv[it] = (j0 + j < nd.f && r < nb) ? F[(int64_t)(p0 + r) * nd.f + j0 + j] : s_zero(S());
+    }
+#pragma unroll
+    for (int it = 0; it < NL; ++it) {
+      const int t = it * 256 + threadIdx.x;
+      As[t % NBT][t / NBT] = av[it];
+      Bs[t / 64][t % 64] = bv[it];
+    }
   }
   __syncthreads();
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
@@ -397,7 +467,7 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(const int32_t* __restr
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
       const int j = j0 + tx + 16 * b;
-      cv[a][b] = (i < nd.f && j < nd.f && (i < nd.k || j < nd.k)) ? F[(int64_t)i * nd.f + j]
+      cv[a][b] = (i < nd.f && j < nd.f && (i < bnd || j < bnd)) ? F[(int64_t)i * nd.f + j]
                                                                  : s_zero(S());
     }
   }
@@ -419,7 +489,7 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(const int32_t* __restr
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
       const int j = j0 + tx + 16 * b;
-      if (j >= nd.f || (i >= nd.k && j >= nd.k)) continue;
+      if (j >= nd.f || (i >= bnd && j >= bnd)) continue;
       F[(int64_t)i * nd.f + j] = s_add(cv[a][b], acc[a][b]);
     }
   }
@@ -451,26 +521,44 @@ __global__ void __launch_bounds__(256) schur_update_kernel(const int32_t* __rest
   for (int a = 0; a < 4; ++a)
 #pragma unroll
     for (int b = 0; b < 4; ++b) acc[a][b] = s_zero(S());
-  for (int kc = 0; kc < nd.k; kc += KC) {
-    const int kn = min(KC, nd.k - kc);
-    __syncthreads();
-    for (int t = threadIdx.x; t < 64 * KC; t += 256) {
+  // chunk kc of L21 (rows i0.., columns kc..) and U12 (rows kc.., columns
+  // j0..) through registers, the next chunk loaded while this one is used
+  constexpr int NL = 64 * KC / 256;
+  S av[NL], bv[NL];
+  auto load = [&](int kc) {
+#pragma unroll
+    for (int it = 0; it < NL; ++it) {
+      const int t = it * 256 + threadIdx.x;
       const int i = t / KC, c = t % KC;
-      As[c][i] = (i0 + i < nd.f && c < kn) ? F[(int64_t)(i0 + i) * nd.f + kc + c] : s_zero(S());
+      av[it] = (i0 + i < nd.f && kc + c < nd.k) ? F[(int64_t)(i0 + i) * nd.f + kc + c]
+                                                : s_zero(S());
       const int r = t / 64, j = t % 64;
-      Bs[r][j] = (j0 + j < nd.f && r < kn) ? F[(int64_t)(kc + r) * nd.f + j0 + j] : s_zero(S());
+      bv[it] = (j0 + j < nd.f && kc + r < nd.k) ? F[(int64_t)(kc + r) * nd.f + j0 + j]
+                                                : s_zero(S());
+    }
+  };
+  load(0);
+  for (int kc = 0; kc < nd.k; kc += KC) {
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < NL; ++it) {
+      const int t = it * 256 + threadIdx.x;
+      As[t % KC][t / KC] = av[it];
+      Bs[t / 64][t % 64] = bv[it];
     }
     __syncthreads();
+    if (kc + KC < nd.k) load(kc + KC);
+    const int kn = min(KC, nd.k - kc);
     for (int t = 0; t < kn; ++t) {
-      S av[4], bv[4];
+      S a4[4], b4[4];
 #pragma unroll
-      for (int a = 0; a < 4; ++a) av[a] = As[t][ty + 16 * a];
+      for (int a = 0; a < 4; ++a) a4[a] = As[t][ty + 16 * a];
 #pragma unroll
-      for (int b = 0; b < 4; ++b) bv[b] = Bs[t][tx + 16 * b];
+      for (int b = 0; b < 4; ++b) b4[b] = Bs[t][tx + 16 * b];
 #pragma unroll
       for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = s_fms(acc[a][b], av[a], bv[b]);
+        for (int b = 0; b < 4; ++b) acc[a][b] = s_fms(acc[a][b], a4[a], b4[b]);
     }
   }
 #pragma unroll
@@ -856,33 +944,12 @@ cudaError_t blas_gemm(MFDevice& d, const S* U, const S* Lb, S* C, int64_t rows, 
   return cudaErrorUnknown;
 }
 
-// panel-step update of one front by cuBLAS in super-panels of width
-// kSuperPanel: the panel step at p0 updates only the rows and columns of its
-// super-panel [sp0, bnd), and the last panel of a super-panel applies the
-// trailing block F[bnd:f, bnd:f] -= L[bnd:f, sp0:bnd] U[sp0:bnd, bnd:f] as one
-// GEMM with K = bnd - sp0 (this includes the (k,f) x (k,f) Schur block).
+// cuBLAS levels work in super-panels of kSuperPanel columns: the panel
+// steps update only the rows and columns of their super-panel (batched
+// kernel), and the last panel of a super-panel [sp0, bnd) applies the
+// trailing block F[bnd:f, bnd:f] -= L[bnd:f, sp0:bnd] U[sp0:bnd, bnd:f] as
+// one GEMM with K = bnd - sp0 (the last of these is the Schur update).
 constexpr int kSuperPanel = 512;
-
-template <typename S>
-cudaError_t blas_update(MFDevice& d, S* F, int64_t f, int64_t k, int p0, int nb,
-                        cudaStream_t st) {
-  const int64_t lo = p0 + nb;
-  if (f - lo <= 0) return cudaSuccess;
-  const int64_t sp0 = (p0 / kSuperPanel) * (int64_t)kSuperPanel;
-  const int64_t bnd = std::min<int64_t>(k, sp0 + kSuperPanel);
-  // rows [lo, f) x cols [lo, bnd)
-  cudaError_t e = blas_gemm<S>(d, F + p0 * f + lo, F + lo * f + p0, F + lo * f + lo, f - lo,
-                               bnd - lo, nb, f, st);
-  if (e != cudaSuccess) return e;
-  // rows [lo, bnd) x cols [bnd, f)
-  e = blas_gemm<S>(d, F + p0 * f + bnd, F + lo * f + p0, F + lo * f + bnd, bnd - lo, f - bnd, nb,
-                   f, st);
-  if (e != cudaSuccess || lo != bnd) return e;
-  // super-panel complete: trailing block with K = bnd - sp0
-  return blas_gemm<S>(d, F + sp0 * f + bnd, F + bnd * f + sp0, F + bnd * f + bnd, f - bnd,
-                      f - bnd, bnd - sp0, f, st);
-}
-
 cudaError_t setup_device(MFHandle& h, int dtype) {
   MFDevice& d = h.dev;
   int dev = 0;
@@ -991,8 +1058,8 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
     for (int c = 0; c < 2; ++c) {
       const int nk = (int)L.kids[c].size();
       if (nk == 0) continue;
-      dim3 grid(64, nk);
-      extend_add_kernel<S><<<grid, 128, 0, st>>>(L.d_kids[c], nk, d.d_nodes, d.d_ea, arena);
+      dim3 grid(std::max(16, std::min(1024, 8192 / nk)), nk);
+      extend_add_kernel<S><<<grid, 256, 0, st>>>(L.d_kids[c], nk, d.d_nodes, d.d_ea, arena);
       count_launch(1);
     }
     // few large fronts: cuBLAS GEMMs per front with super-panel trailing
@@ -1014,26 +1081,33 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
         panel_trsm_kernel<S, NBT><<<g1, 256, trsm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena,
                                                                p0);
         count_launch(1);
+        const int tpd = (rest + 63) / 64;
+        dim3 g2(tpd * tpd, cnt);
+        gemm_update_kernel<S, NBT><<<g2, 256, gemm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena,
+                                                                p0, use_blas ? kSuperPanel : 0);
+        count_launch(1);
         if (use_blas) {
-          // few large fronts: one cuBLAS GEMM per front
+          // fronts whose super-panel ends with this panel: trailing GEMM
           for (int q = 0; q < cnt; ++q) {
             const MFNode& nd = s.nodes[L.nodes_by_k[q]];
-            const int nbq = (int)std::min<int64_t>(NBT, nd.k - p0);
-            e = blas_update<S>(d, arena + nd.front_off, nd.f, nd.k, p0, nbq, st);
+            const int64_t lo = p0 + std::min<int64_t>(NBT, nd.k - p0);
+            const int64_t sp0 = (p0 / kSuperPanel) * (int64_t)kSuperPanel;
+            const int64_t bnd = std::min<int64_t>(nd.k, sp0 + kSuperPanel);
+            if (lo != bnd || bnd >= nd.f) continue;
+            S* F = arena + nd.front_off;
+            const int64_t f = nd.f;
+            e = blas_gemm<S>(d, F + sp0 * f + bnd, F + bnd * f + sp0, F + bnd * f + bnd, f - bnd,
+                             f - bnd, bnd - sp0, f, st);
             if (e != cudaSuccess) return e;
           }
-        } else {
-          const int tpd = (rest + 63) / 64;
-          dim3 g2(tpd * tpd, cnt);
-          gemm_update_kernel<S, NBT><<<g2, 256, gemm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena,
-                                                                  p0);
-          count_launch(1);
         }
       }
     }
     // Schur blocks F[k:f, k:f] -= L21 U12 with the full K = k, before the
     // parent level's extend-add reads them
     if (!use_blas && L.max_u > 0 && nall > 0) {
+      // one batched launch for all fronts of the level (per-front cuBLAS
+      // calls leave the GPU underfilled at these front sizes)
       const int tpd = (L.max_u + 63) / 64;
       dim3 g3(tpd * tpd, nall);
       schur_update_kernel<S, kSchurKC><<<g3, 256, schur_smem, st>>>(L.d_nodes, nall, d.d_nodes,
