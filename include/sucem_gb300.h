@@ -233,6 +233,11 @@ void sucem_lu_destroy(sucem_lu* lu);
  *           multiply-adds, largest front} */
 int sucem_lu_info(const sucem_lu* lu, double* out);
 int sucem_lu_copy_perm(const sucem_lu* lu, int64_t* perm);
+/* The assembly tree, for inspection: out[3*i .. 3*i+2] = {level (leaves 0),
+ * pivots k, front size f} of tree node i (i < tree nodes of sucem_lu_info).
+ * No reference counterpart (the reference's direct solve is a library
+ * call). */
+int sucem_lu_fronts(const sucem_lu* lu, int64_t* out);
 int sucem_lu_factor(sucem_lu* lu, int dtype, const void* vals, double pivot_tol, void* stream);
 int sucem_lu_solve(sucem_lu* lu, int io_dtype, const void* b, void* x, void* stream);
 int sucem_lu_perturbed(sucem_lu* lu);

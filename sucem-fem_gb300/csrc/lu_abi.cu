@@ -96,6 +96,17 @@ int sucem_lu_info(const sucem_lu* lu, double* out) {
   return SUCEM_OK;
 }
 
+int sucem_lu_fronts(const sucem_lu* lu, int64_t* out) {
+  if (!lu || !out) return fail("null argument", SUCEM_ERR_ARG);
+  const sucem::MFSymbolic& s = sucem::mf_sym(lu->h);
+  for (size_t i = 0; i < s.nodes.size(); ++i) {
+    out[3 * i] = s.nodes[i].level;
+    out[3 * i + 1] = s.nodes[i].k;
+    out[3 * i + 2] = s.nodes[i].f;
+  }
+  return SUCEM_OK;
+}
+
 int sucem_lu_copy_perm(const sucem_lu* lu, int64_t* perm) {
   if (!lu || !perm) return fail("null argument", SUCEM_ERR_ARG);
   const sucem::MFSymbolic& s = sucem::mf_sym(lu->h);

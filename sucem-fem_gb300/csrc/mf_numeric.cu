@@ -36,6 +36,9 @@ namespace {
 constexpr int kBlasFronts = 16;
 template <typename S>
 constexpr bool kSinglePrecision = std::is_same<S, float>::value || std::is_same<S, float2>::value;
+// complex single precision: Schur-block updates on the tensor cores (mf_tc.cuh)
+template <typename S>
+constexpr bool kTensorCore = std::is_same<S, float2>::value;
 
 // ---- scalar helpers ----
 __device__ __forceinline__ float s_zero(float) { return 0.f; }
@@ -144,6 +147,8 @@ struct DNode {
   int32_t parent;
   int32_t child_slot;  // 0 or 1: position among the parent's children
 };
+
+#include "mf_tc.cuh"
 
 // ---- factor kernels ----
 template <typename S>
@@ -1024,6 +1029,9 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
     if (ea == cudaSuccess)
       ea = cudaFuncSetAttribute(gemm_update_kernel<S, NBT>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem);
+    if (ea == cudaSuccess && kTensorCore<S>)
+      ea = cudaFuncSetAttribute(tc_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                tc::SMEM_BYTES);
     if (ea == cudaSuccess)
       ea = cudaFuncSetAttribute(schur_update_kernel<S, kSchurKC>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)schur_smem);
@@ -1033,7 +1041,8 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
   const MFSymbolic& s = h.sym;
   S* arena = (S*)d.arena;
   cudaError_t e = cudaMemsetAsync(arena, 0, (size_t)s.arena * sizeof(S), st);
-  // d_flag[0]: perturbed-pivot count; d_flag[2..3]: max |a_ij| (as bits)
+  // d_flag[0]: perturbed-pivot count; d_flag[1]: tensor-core update timed
+  // out; d_flag[2..3]: max |a_ij| (as bits)
   if (e == cudaSuccess) e = cudaMemsetAsync(d.d_flag, 0, 16, st);
   if (e != cudaSuccess) return e;
   unsigned long long* amax = reinterpret_cast<unsigned long long*>(d.d_flag + 2);
@@ -1086,7 +1095,26 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
         gemm_update_kernel<S, NBT><<<g2, 256, gemm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena,
                                                                 p0, use_blas ? kSuperPanel : 0);
         count_launch(1);
-        if (use_blas) {
+        if (use_blas && kTensorCore<S>) {
+          // fronts whose super-panel ends with this panel: trailing block on
+          // the tensor cores, one launch for all of them
+          int max_mn = 0;
+          for (int q = 0; q < cnt; ++q) {
+            const MFNode& nd = s.nodes[L.nodes_by_k[q]];
+            const int64_t lo = p0 + std::min<int64_t>(NBT, nd.k - p0);
+            const int64_t sp0 = (p0 / kSuperPanel) * (int64_t)kSuperPanel;
+            const int64_t bnd = std::min<int64_t>(nd.k, sp0 + kSuperPanel);
+            if (lo == bnd && bnd < nd.f) max_mn = std::max<int>(max_mn, (int)(nd.f - bnd));
+          }
+          if (max_mn > 0) {
+            const int tpd = (max_mn + tc::BM - 1) / tc::BM;
+            dim3 g4(tpd * tpd, cnt);
+            tc_update_kernel<<<g4, tc::THREADS, tc::SMEM_BYTES, st>>>(
+                L.d_nodes, cnt, d.d_nodes, reinterpret_cast<float2*>(arena), p0, kSuperPanel, NBT,
+                d.d_flag + 1);
+            count_launch(1);
+          }
+        } else if (use_blas) {
           // fronts whose super-panel ends with this panel: trailing GEMM
           for (int q = 0; q < cnt; ++q) {
             const MFNode& nd = s.nodes[L.nodes_by_k[q]];
@@ -1105,7 +1133,13 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
     }
     // Schur blocks F[k:f, k:f] -= L21 U12 with the full K = k, before the
     // parent level's extend-add reads them
-    if (!use_blas && L.max_u > 0 && nall > 0) {
+    if (kTensorCore<S> && !use_blas && L.max_u > 0 && nall > 0) {
+      const int tpd = (L.max_u + tc::BM - 1) / tc::BM;
+      dim3 g3(tpd * tpd, nall);
+      tc_update_kernel<<<g3, tc::THREADS, tc::SMEM_BYTES, st>>>(
+          L.d_nodes, nall, d.d_nodes, reinterpret_cast<float2*>(arena), 0, 0, NBT, d.d_flag + 1);
+      count_launch(1);
+    } else if (!use_blas && L.max_u > 0 && nall > 0) {
       // one batched launch for all fronts of the level (per-front cuBLAS
       // calls leave the GPU underfilled at these front sizes)
       const int tpd = (L.max_u + 63) / 64;
@@ -1251,9 +1285,10 @@ cudaError_t mf_solve(MFHandle& h, int io_dtype, const void* b, void* x, cudaStre
 }
 
 int mf_perturbed(MFHandle& h) {
-  int v = 0;
-  if (h.dev.d_flag) cudaMemcpy(&v, h.dev.d_flag, sizeof(int), cudaMemcpyDeviceToHost);
-  return v;
+  int v[2] = {0, 0};
+  if (h.dev.d_flag) cudaMemcpy(v, h.dev.d_flag, sizeof(v), cudaMemcpyDeviceToHost);
+  // d_flag[1]: a bounded wait of the tensor-core update gave up
+  return v[1] ? -1 : v[0];
 }
 
 void mf_free(MFHandle& h) { free_dev(h.dev); }

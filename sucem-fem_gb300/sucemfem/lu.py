@@ -15,6 +15,7 @@ _native.declare("sucem_lu_analyse", ctypes.c_int,
 _native.declare("sucem_lu_destroy", None, [c_vp])
 _native.declare("sucem_lu_info", ctypes.c_int, [c_vp, c_vp])
 _native.declare("sucem_lu_copy_perm", ctypes.c_int, [c_vp, c_vp])
+_native.declare("sucem_lu_fronts", ctypes.c_int, [c_vp, c_vp])
 _native.declare("sucem_lu_factor", ctypes.c_int, [c_vp, ctypes.c_int, c_vp, ctypes.c_double, c_vp])
 _native.declare("sucem_lu_solve", ctypes.c_int, [c_vp, ctypes.c_int, c_vp, c_vp, c_vp])
 _native.declare("sucem_lu_perturbed", ctypes.c_int, [c_vp])
@@ -60,6 +61,13 @@ class SparseLU:
         if h is not None and h.value and _native._lib is not None:
             _native._lib.sucem_lu_destroy(h)
             self._h = None
+
+    def fronts(self):
+        """Assembly tree as an int64 array of (level, pivots k, front size f)
+        rows, one per tree node."""
+        out = np.empty((self.info["nodes"], 3), dtype=np.int64)
+        call("sucem_lu_fronts", self._h, ptr(out))
+        return out
 
     def perm(self):
         p = np.empty(self.n, dtype=np.int64)
