@@ -1090,6 +1090,8 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
         panel_trsm_kernel<S, NBT><<<g1, 256, trsm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena,
                                                                p0);
         count_launch(1);
+        // K = nb panel update outside the deferred block: CUDA cores (the
+        // panel steps are latency-bound; tensor-core tiles do not pay off)
         const int tpd = (rest + 63) / 64;
         dim3 g2(tpd * tpd, cnt);
         gemm_update_kernel<S, NBT><<<g2, 256, gemm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena,
@@ -1110,8 +1112,8 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
             const int tpd = (max_mn + tc::BM - 1) / tc::BM;
             dim3 g4(tpd * tpd, cnt);
             tc_update_kernel<<<g4, tc::THREADS, tc::SMEM_BYTES, st>>>(
-                L.d_nodes, cnt, d.d_nodes, reinterpret_cast<float2*>(arena), p0, kSuperPanel, NBT,
-                d.d_flag + 1);
+                L.d_nodes, cnt, d.d_nodes, reinterpret_cast<float2*>(arena), tc::kTrailing, p0,
+                kSuperPanel, NBT, d.d_flag + 1);
             count_launch(1);
           }
         } else if (use_blas) {
@@ -1137,7 +1139,8 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
       const int tpd = (L.max_u + tc::BM - 1) / tc::BM;
       dim3 g3(tpd * tpd, nall);
       tc_update_kernel<<<g3, tc::THREADS, tc::SMEM_BYTES, st>>>(
-          L.d_nodes, nall, d.d_nodes, reinterpret_cast<float2*>(arena), 0, 0, NBT, d.d_flag + 1);
+          L.d_nodes, nall, d.d_nodes, reinterpret_cast<float2*>(arena), tc::kSchur, 0, 0, NBT,
+          d.d_flag + 1);
       count_launch(1);
     } else if (!use_blas && L.max_u > 0 && nall > 0) {
       // one batched launch for all fronts of the level (per-front cuBLAS

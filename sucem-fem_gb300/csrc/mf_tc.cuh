@@ -2,11 +2,10 @@
 // fronts, included by mf_numeric.cu inside its anonymous namespace (uses
 // DNode and the row-major front arena).
 //
-// For every front of a level it computes, over one 128 x 128 tile per CTA,
-//   F[r0:f, r0:f] -= F[r0:f, kk0:kk0+K] * F[kk0:kk0+K, r0:f]
-// with (r0, kk0, K) = (k, 0, k) for the Schur block after all pivot panels,
-// or, on levels factorised in super-panels of width sp, the trailing block
-// of the super-panel that ends with panel p0.
+// For every front of a level it applies, over one 128 x 128 tile per CTA,
+//   F[rows, cols] -= F[rows, kk0:kk0+K] * F[kk0:kk0+K, cols]
+// for one of two updates (tile_of): the Schur block after all pivot panels,
+// or the trailing block of a finished super-panel.
 //
 // Arithmetic: complex FP32 operands are split into TF32 pairs x = hi + lo
 // (hi = x rounded to TF32, lo = x - hi), and every real product is formed as
@@ -16,7 +15,8 @@
 // instruction's A-negation bit.
 //
 // Pipeline: K is consumed in chunks of 16; all 256 threads load a chunk
-// (A: 128 rows x 16, B: 16 x 128 columns), split it and store eight K-major
+// (A: 128 rows x 16, B: 16 x 128 columns; two chunks ahead, through two
+// register buffers), split it and store eight K-major
 // operand planes (Re/Im x hi/lo for A and B) in the canonical no-swizzle
 // core-matrix layout (8 rows x 16 bytes per core matrix, 128 bytes apart
 // along K, 512 bytes apart along M/N) into one of three stages; one thread
@@ -107,14 +107,53 @@ __device__ __forceinline__ void store_split(uint8_t* planes, int off, const floa
   *reinterpret_cast<float4*>(planes + 3 * PLANE + off) = il;
 }
 
+// one output tile: rows [row0, row0 + nrow) x columns [col0, col0 + ncol) of
+// the front take -= F[rows, kk0:kk0+K] * F[kk0:kk0+K, columns]
+struct Tile {
+  int row0, nrow, col0, ncol, kk0, K;
+};
+
+enum Mode { kSchur = 0, kTrailing = 1 };
+
+// tile `bx` of the front's update in the given mode (false: no such tile)
+//   kSchur:    [k, f)^2 with K = k (after all pivot panels)
+//   kTrailing: [bnd, f)^2 with K = bnd - sp0, for the super-panel
+//              [sp0, bnd) of width sp that ends with the panel at p0
+__device__ __forceinline__ bool tile_of(const DNode& nd, int mode, int p0, int sp, int nbt,
+                                        int bx, Tile& t) {
+  int r0;
+  if (mode == kSchur) {
+    r0 = nd.k;
+    t.kk0 = 0;
+    t.K = nd.k;
+  } else {
+    if (p0 >= nd.k) return false;
+    const int sp0 = (p0 / sp) * sp;
+    const int bnd = min(nd.k, sp0 + sp);
+    if (p0 + min(nbt, nd.k - p0) != bnd) return false;
+    r0 = bnd;
+    t.kk0 = sp0;
+    t.K = bnd - sp0;
+  }
+  const int mn = nd.f - r0;
+  if (mn <= 0 || t.K <= 0) return false;
+  const int tpd = (mn + BM - 1) / BM;
+  if (bx >= tpd * tpd) return false;
+  t.row0 = r0 + (bx / tpd) * BM;
+  t.col0 = r0 + (bx % tpd) * BN;
+  t.nrow = min(BM, nd.f - t.row0);
+  t.ncol = min(BN, nd.f - t.col0);
+  return true;
+}
+
 }  // namespace tc
 
-// sp == 0: Schur block (r0 = k, kk0 = 0, K = k) of every listed front;
-// sp > 0: trailing block of the super-panel [sp0, bnd) of width sp that ends
-// with the panel at p0 (width nbt), for the fronts where it does.
+// the update of the given mode (tc::Mode) for every listed front, one
+// 128 x 128 output tile per block (blockIdx.x: tile, blockIdx.y: front)
 __global__ void __launch_bounds__(tc::THREADS, 1)
     tc_update_kernel(const int32_t* __restrict__ list, int count, const DNode* __restrict__ nodes,
-                     float2* __restrict__ arena, int p0, int sp, int nbt, int* __restrict__ err) {
+                     float2* __restrict__ arena, int mode, int p0, int sp, int nbt,
+                     int* __restrict__ err) {
   using namespace tc;
   extern __shared__ __align__(128) uint8_t tc_smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
@@ -125,25 +164,9 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
   const int fi = blockIdx.y;
   if (fi >= count) return;
   const DNode nd = nodes[list[fi]];
-  int r0, kk0, K;
-  if (sp == 0) {
-    r0 = nd.k;
-    kk0 = 0;
-    K = nd.k;
-  } else {
-    if (p0 >= nd.k) return;
-    const int sp0 = (p0 / sp) * sp;
-    const int bnd = min(nd.k, sp0 + sp);
-    if (p0 + min(nbt, nd.k - p0) != bnd) return;
-    r0 = bnd;
-    kk0 = sp0;
-    K = bnd - sp0;
-  }
-  const int mn = nd.f - r0;
-  if (mn <= 0 || K <= 0) return;
-  const int tpd = (mn + BM - 1) / BM;
-  if ((int)blockIdx.x >= tpd * tpd) return;
-  const int i0 = ((int)blockIdx.x / tpd) * BM, j0 = ((int)blockIdx.x % tpd) * BN;
+  Tile tl;
+  if (!tile_of(nd, mode, p0, sp, nbt, (int)blockIdx.x, tl)) return;
+  const int kk0 = tl.kk0, K = tl.K;
   float2* F = arena + nd.off;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -151,9 +174,9 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
   // consecutive k from bkh*8)
   const int ar = tid % BM, akh = tid / BM;
   const int bn = tid % BN, bkh = tid / BN;
-  const bool arow_ok = i0 + ar < mn, bcol_ok = j0 + bn < mn;
-  const float2* Arow = F + (int64_t)(r0 + i0 + (arow_ok ? ar : 0)) * nd.f + kk0;
-  const float2* Bcol = F + (int64_t)kk0 * nd.f + r0 + j0 + (bcol_ok ? bn : 0);
+  const bool arow_ok = ar < tl.nrow, bcol_ok = bn < tl.ncol;
+  const float2* Arow = F + (int64_t)(tl.row0 + (arow_ok ? ar : 0)) * nd.f + kk0;
+  const float2* Bcol = F + (int64_t)kk0 * nd.f + tl.col0 + (bcol_ok ? bn : 0);
 
   if (tid == 0) {
 #pragma unroll
@@ -174,8 +197,9 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
 
   const int nchunks = (K + KC - 1) / KC;
   const float2 zero = make_float2(0.f, 0.f);
-  float2 av[8], bv[8];
-  auto gload = [&](int c) {
+  // two register buffers: chunk c + 2 is loaded while chunk c is stored
+  float2 av0[8], bv0[8], av1[8], bv1[8];
+  auto gload = [&](float2* av, float2* bv, int c) {
     const int ka = c * KC + akh * 8, kb = c * KC + bkh * 8;
 #pragma unroll
     for (int j = 0; j < 8; ++j) av[j] = (arow_ok && ka + j < K) ? Arow[ka + j] : zero;
@@ -184,8 +208,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
       bv[j] = (bcol_ok && kb + j < K) ? Bcol[(int64_t)(kb + j) * nd.f] : zero;
   };
   bool ok = true;
-  gload(0);
-  for (int c = 0; c < nchunks; ++c) {
+  auto step = [&](float2* av, float2* bv, int c) {
     const int s = c % STAGES;
     if (c >= STAGES) ok = wait_parity(smem_u32(&mbar[s]), ((c / STAGES) - 1) & 1) && ok;
     uint8_t* st = smem + s * STAGE_BYTES;
@@ -194,7 +217,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
       store_split(st, core_off(ar, akh * 2 + h), av + 4 * h);
       store_split(st + 4 * PLANE, core_off(bn, bkh * 2 + h), bv + 4 * h);
     }
-    if (c + 1 < nchunks) gload(c + 1);
+    if (c + 2 < nchunks) gload(av, bv, c + 2);
     asm volatile("fence.proxy.async.shared::cta;");
     __syncthreads();
     if (tid == 0) {
@@ -230,6 +253,12 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
               smem_u32(&mbar[s])));
     }
+  };
+  gload(av0, bv0, 0);
+  if (nchunks > 1) gload(av1, bv1, 1);
+  for (int c = 0; c < nchunks; c += 2) {
+    step(av0, bv0, c);
+    if (c + 1 < nchunks) step(av1, bv1, c + 1);
   }
   // the last commit covers every MMA of the tile
   const int cl = nchunks - 1;
@@ -241,8 +270,8 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
     // warp w reads TMEM lanes 32 (w % 4) .. +31 (tile rows) and columns
     // 64 (w / 4) .. +63 of both accumulators, 16 at a time
     const int q = warp & 3, half = warp >> 2;
-    const int row = i0 + q * 32 + lane;
-    float2* Crow = F + (int64_t)(r0 + (row < mn ? row : 0)) * nd.f + r0;
+    const int row = q * 32 + lane;
+    float2* Crow = F + (int64_t)(tl.row0 + (row < tl.nrow ? row : 0)) * nd.f + tl.col0;
 #pragma unroll 1
     for (int cc = 0; cc < 4; ++cc) {
       const int col0 = half * 64 + cc * 16;
@@ -261,11 +290,11 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
             "=r"(im[12]), "=r"(im[13]), "=r"(im[14]), "=r"(im[15])
           : "r"(tre + BN));
       asm volatile("tcgen05.wait::ld.sync.aligned;");
-      if (row < mn) {
+      if (row < tl.nrow) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          const int col = j0 + col0 + j;
-          if (col < mn) {
+          const int col = col0 + j;
+          if (col < tl.ncol) {
             float2 v = Crow[col];
             v.x -= __uint_as_float(re[j]);
             v.y -= __uint_as_float(im[j]);
