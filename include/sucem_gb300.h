@@ -241,6 +241,11 @@ int sucem_lu_fronts(const sucem_lu* lu, int64_t* out);
 int sucem_lu_factor(sucem_lu* lu, int dtype, const void* vals, double pivot_tol, void* stream);
 int sucem_lu_solve(sucem_lu* lu, int io_dtype, const void* b, void* x, void* stream);
 int sucem_lu_perturbed(sucem_lu* lu);
+/* Tensor-core Schur-update launches of the last complex64 factorisation
+ * (waits for them): out[3] = {launches, summed event-timed duration in ms,
+ * algorithmic flops (8 per complex multiply-add)}.  No reference
+ * counterpart (measurement hook). */
+int sucem_lu_kernel_stats(sucem_lu* lu, double* out);
 
 #ifdef __cplusplus
 }

@@ -137,4 +137,10 @@ int sucem_lu_solve(sucem_lu* lu, int io_dtype, const void* b, void* x, void* str
 
 int sucem_lu_perturbed(sucem_lu* lu) { return lu ? sucem::mf_perturbed(*lu->h) : 0; }
 
+int sucem_lu_kernel_stats(sucem_lu* lu, double* out) {
+  if (!lu || !out) return fail("null argument", SUCEM_ERR_ARG);
+  sucem::mf_tc_stats(*lu->h, out);
+  return SUCEM_OK;
+}
+
 }  // extern "C"

@@ -68,5 +68,8 @@ struct MFHandle;
 cudaError_t mf_factor(MFHandle& h, int dtype, const void* vals, double tau, cudaStream_t st);
 cudaError_t mf_solve(MFHandle& h, int io_dtype, const void* b, void* x, cudaStream_t st);
 int mf_perturbed(MFHandle& h);
+// tensor-core update launches of the last factorisation: out[0] launches,
+// out[1] their summed event-timed duration (ms), out[2] algorithmic flops
+void mf_tc_stats(MFHandle& h, double* out);
 void mf_free(MFHandle& h);
 }  // namespace sucem

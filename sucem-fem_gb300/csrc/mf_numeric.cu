@@ -841,8 +841,17 @@ __global__ void permute_out_kernel(int64_t n, const int64_t* __restrict__ perm,
 }  // namespace
 
 // ---- host object ----
+// one tensor-core trailing update: the fronts of a level whose super-panel
+// ends with the panel at p0
+struct TcLaunch {
+  int p0 = 0, count = 0, tpd = 0;   // tpd: tiles per side of the largest block
+  double flops = 0;                 // algorithmic flops (8 per complex MAC)
+  int32_t* d_list = nullptr;        // node ids
+};
+
 struct MFLevel {
   std::vector<int32_t> nodes_by_k;  // node ids sorted by k descending
+  std::vector<TcLaunch> tcl;        // complex64 only, ordered by p0
   std::vector<int32_t> kids[2];     // children by slot
   int max_k = 0, max_rest = 0, max_u = 0;
   int32_t* d_nodes = nullptr;
@@ -864,8 +873,12 @@ struct MFDevice {
   void* d_x = nullptr;              // solve work vector (new ordering)
   int* d_flag = nullptr;            // perturbed pivot count
   cudaStream_t cap_stream = nullptr;  // private stream for capturing the solve graph
+  std::vector<cudaEvent_t> tc_ev;   // start/stop events around tensor-core launches
+  int tc_n = 0;                     // tensor-core launches in the last factorisation
+  double tc_flops = 0;              // their algorithmic flops (8 per complex MAC)
   cudaGraphExec_t solve_exec = nullptr;
   int solve_n = 0;                  // kernel launches in the solve graph
+  int tc_sp = 0;                    // super-panel width of the tensor-core path (complex64)
   std::vector<MFLevel> levels;
   bool factored = false;
   int perturbed = 0;
@@ -906,11 +919,14 @@ void free_dev(MFDevice& d) {
     if (p) cudaFree(p);
   for (auto& L : d.levels) {
     if (L.d_nodes) cudaFree(L.d_nodes);
+    for (auto& t : L.tcl)
+      if (t.d_list) cudaFree(t.d_list);
     for (int s = 0; s < 2; ++s)
       if (L.d_kids[s]) cudaFree(L.d_kids[s]);
   }
   if (d.blas) cublasDestroy(d.blas);
   if (d.solve_exec) cudaGraphExecDestroy(d.solve_exec);
+  for (cudaEvent_t ev : d.tc_ev) cudaEventDestroy(ev);
   if (d.cap_stream) cudaStreamDestroy(d.cap_stream);
   d = MFDevice();
 }
@@ -955,6 +971,62 @@ cudaError_t blas_gemm(MFDevice& d, const S* U, const S* Lb, S* C, int64_t rows, 
 // trailing block F[bnd:f, bnd:f] -= L[bnd:f, sp0:bnd] U[sp0:bnd, bnd:f] as
 // one GEMM with K = bnd - sp0 (the last of these is the Schur update).
 constexpr int kSuperPanel = 512;
+// complex64 factorisations work in super-panels of d.tc_sp columns on every
+// level; for each level, the panels p0 at which some fronts' super-panel
+// ends get one tensor-core launch over exactly those fronts (list on the
+// device).  Narrower super-panels move panel work onto the tensor cores
+// but re-read and re-write the trailing block once per super-panel; 512
+// measured best (20^3 order-2 box: 128 -> 107 ms, 256 -> 87 ms, 512 -> 82 ms
+// per factorisation).  SUCEM_LU_SUPERPANEL overrides it (a multiple of 64).
+constexpr int kTcSuperPanel = 512;
+constexpr int kTcPanel = 64;  // panel width of the complex64 factorisation
+
+cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s) {
+  d.tc_sp = kTcSuperPanel;
+  if (const char* v = getenv("SUCEM_LU_SUPERPANEL")) {
+    const int w = atoi(v);
+    if (w >= kTcPanel && w % kTcPanel == 0) d.tc_sp = w;
+  }
+  const int sp = d.tc_sp;
+  for (auto& L : d.levels) {
+    std::vector<std::pair<int, int32_t>> ends;  // (p0, node)
+    for (int32_t i : L.nodes_by_k) {
+      const MFNode& nd = s.nodes[i];
+      for (int64_t p0 = 0; p0 < nd.k; p0 += kTcPanel) {
+        const int64_t lo = p0 + std::min<int64_t>(kTcPanel, nd.k - p0);
+        const int64_t bnd = std::min<int64_t>(nd.k, (p0 / sp) * (int64_t)sp + sp);
+        if (lo == bnd && bnd < nd.f) ends.push_back({(int)p0, i});
+      }
+    }
+    std::stable_sort(ends.begin(), ends.end(),
+                     [](const std::pair<int, int32_t>& a, const std::pair<int, int32_t>& b) {
+                       return a.first < b.first;
+                     });
+    for (size_t a = 0; a < ends.size();) {
+      size_t b = a;
+      TcLaunch t;
+      t.p0 = ends[a].first;
+      std::vector<int32_t> ids;
+      int max_mn = 0;
+      for (; b < ends.size() && ends[b].first == t.p0; ++b) {
+        const MFNode& nd = s.nodes[ends[b].second];
+        const int64_t sp0 = (t.p0 / sp) * (int64_t)sp;
+        const int64_t bnd = std::min<int64_t>(nd.k, sp0 + sp);
+        ids.push_back(ends[b].second);
+        max_mn = std::max<int>(max_mn, (int)(nd.f - bnd));
+        t.flops += 8.0 * (double)(nd.f - bnd) * (double)(nd.f - bnd) * (double)(bnd - sp0);
+      }
+      t.count = (int)ids.size();
+      t.tpd = (max_mn + tc::BM - 1) / tc::BM;
+      cudaError_t e = upv(&t.d_list, ids);
+      if (e != cudaSuccess) return e;
+      L.tcl.push_back(t);
+      a = b;
+    }
+  }
+  return cudaSuccess;
+}
+
 cudaError_t setup_device(MFHandle& h, int dtype) {
   MFDevice& d = h.dev;
   int dev = 0;
@@ -1011,14 +1083,27 @@ cudaError_t setup_device(MFHandle& h, int dtype) {
   if (e == cudaSuccess) e = cudaMalloc(&d.arena, (size_t)std::max<int64_t>(s.arena, 1) * d.elem);
   if (e == cudaSuccess) e = cudaMalloc(&d.d_x, (size_t)std::max<int64_t>(s.n, 1) * d.elem);
   if (e == cudaSuccess) e = cudaMalloc((void**)&d.d_flag, 16);
+  if (e == cudaSuccess && dtype == SUCEM_C64) e = plan_tc(d, s);
   if (e != cudaSuccess) free_dev(d);
   return e;
+}
+
+// events around the i-th tensor-core launch of a factorisation
+cudaError_t tc_event(MFDevice& d, int i, int which, cudaStream_t st) {
+  while ((int)d.tc_ev.size() < 2 * (i + 1)) {
+    cudaEvent_t ev;
+    cudaError_t e = cudaEventCreate(&ev);
+    if (e != cudaSuccess) return e;
+    d.tc_ev.push_back(ev);
+  }
+  return cudaEventRecord(d.tc_ev[2 * i + which], st);
 }
 
 template <typename S>
 cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st) {
   // panel width 64 (32 for complex double, whose tiles would not fit)
   constexpr int NBT = sizeof(S) <= 8 ? 64 : 32;
+  static_assert(!kTensorCore<S> || NBT == kTcPanel, "tensor-core plan assumes this panel width");
   const size_t trsm_smem = sizeof(S) * (size_t)(NBT + 64) * (NBT + 1);
   const size_t gemm_smem = sizeof(S) * (size_t)NBT * (65 + 64);
   constexpr int kSchurKC = 32;
@@ -1040,6 +1125,8 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
   MFDevice& d = h.dev;
   const MFSymbolic& s = h.sym;
   S* arena = (S*)d.arena;
+  d.tc_n = 0;
+  d.tc_flops = 0;
   cudaError_t e = cudaMemsetAsync(arena, 0, (size_t)s.arena * sizeof(S), st);
   // d_flag[0]: perturbed-pivot count; d_flag[1]: tensor-core update timed
   // out; d_flag[2..3]: max |a_ij| (as bits)
@@ -1071,10 +1158,15 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
       extend_add_kernel<S><<<grid, 256, 0, st>>>(L.d_kids[c], nk, d.d_nodes, d.d_ea, arena);
       count_launch(1);
     }
-    // few large fronts: cuBLAS GEMMs per front with super-panel trailing
-    // updates; otherwise batched kernels and one Schur update per level
+    // complex64: every level in super-panels of d.tc_sp columns, the
+    // trailing blocks on the tensor cores (precomputed launch lists);
+    // otherwise few large fronts take cuBLAS GEMMs per front with
+    // super-panels of kSuperPanel, the rest one Schur update per level
     const int nall = (int)L.nodes_by_k.size();
-    const bool use_blas = kSinglePrecision<S> && nall <= kBlasFronts;
+    const bool tc_level = kTensorCore<S> && d.tc_sp > 0;
+    const bool use_blas = !tc_level && kSinglePrecision<S> && nall <= kBlasFronts;
+    const int spw = tc_level ? d.tc_sp : (use_blas ? kSuperPanel : 0);
+    size_t next_tc = 0;
     for (int p0 = 0; p0 < L.max_k; p0 += NBT) {
       // active fronts: prefix of the k-descending list with k > p0
       int cnt = 0;
@@ -1095,54 +1187,45 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
         const int tpd = (rest + 63) / 64;
         dim3 g2(tpd * tpd, cnt);
         gemm_update_kernel<S, NBT><<<g2, 256, gemm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena,
-                                                                p0, use_blas ? kSuperPanel : 0);
+                                                                p0, spw);
         count_launch(1);
-        if (use_blas && kTensorCore<S>) {
-          // fronts whose super-panel ends with this panel: trailing block on
-          // the tensor cores, one launch for all of them
-          int max_mn = 0;
-          for (int q = 0; q < cnt; ++q) {
-            const MFNode& nd = s.nodes[L.nodes_by_k[q]];
-            const int64_t lo = p0 + std::min<int64_t>(NBT, nd.k - p0);
-            const int64_t sp0 = (p0 / kSuperPanel) * (int64_t)kSuperPanel;
-            const int64_t bnd = std::min<int64_t>(nd.k, sp0 + kSuperPanel);
-            if (lo == bnd && bnd < nd.f) max_mn = std::max<int>(max_mn, (int)(nd.f - bnd));
-          }
-          if (max_mn > 0) {
-            const int tpd = (max_mn + tc::BM - 1) / tc::BM;
-            dim3 g4(tpd * tpd, cnt);
-            tc_update_kernel<<<g4, tc::THREADS, tc::SMEM_BYTES, st>>>(
-                L.d_nodes, cnt, d.d_nodes, reinterpret_cast<float2*>(arena), tc::kTrailing, p0,
-                kSuperPanel, NBT, d.d_flag + 1);
-            count_launch(1);
-          }
-        } else if (use_blas) {
-          // fronts whose super-panel ends with this panel: trailing GEMM
-          for (int q = 0; q < cnt; ++q) {
-            const MFNode& nd = s.nodes[L.nodes_by_k[q]];
-            const int64_t lo = p0 + std::min<int64_t>(NBT, nd.k - p0);
-            const int64_t sp0 = (p0 / kSuperPanel) * (int64_t)kSuperPanel;
-            const int64_t bnd = std::min<int64_t>(nd.k, sp0 + kSuperPanel);
-            if (lo != bnd || bnd >= nd.f) continue;
-            S* F = arena + nd.front_off;
-            const int64_t f = nd.f;
-            e = blas_gemm<S>(d, F + sp0 * f + bnd, F + bnd * f + sp0, F + bnd * f + bnd, f - bnd,
-                             f - bnd, bnd - sp0, f, st);
-            if (e != cudaSuccess) return e;
-          }
+      }
+      if (tc_level) {
+        // fronts whose super-panel ends with this panel: trailing block on
+        // the tensor cores, one launch over exactly those fronts
+        while (next_tc < L.tcl.size() && L.tcl[next_tc].p0 == p0) {
+          const TcLaunch& t = L.tcl[next_tc++];
+          dim3 g4(t.tpd * t.tpd, t.count);
+          e = tc_event(d, d.tc_n, 0, st);
+          if (e != cudaSuccess) return e;
+          tc_update_kernel<<<g4, tc::THREADS, tc::SMEM_BYTES, st>>>(
+              t.d_list, t.count, d.d_nodes, reinterpret_cast<float2*>(arena), p0, spw, NBT,
+              d.d_flag + 1);
+          e = tc_event(d, d.tc_n, 1, st);
+          if (e != cudaSuccess) return e;
+          d.tc_n++;
+          d.tc_flops += t.flops;
+          count_launch(1);
+        }
+      } else if (use_blas && tiles > 0) {
+        // fronts whose super-panel ends with this panel: trailing GEMM
+        for (int q = 0; q < cnt; ++q) {
+          const MFNode& nd = s.nodes[L.nodes_by_k[q]];
+          const int64_t lo = p0 + std::min<int64_t>(NBT, nd.k - p0);
+          const int64_t sp0 = (p0 / kSuperPanel) * (int64_t)kSuperPanel;
+          const int64_t bnd = std::min<int64_t>(nd.k, sp0 + kSuperPanel);
+          if (lo != bnd || bnd >= nd.f) continue;
+          S* F = arena + nd.front_off;
+          const int64_t f = nd.f;
+          e = blas_gemm<S>(d, F + sp0 * f + bnd, F + bnd * f + sp0, F + bnd * f + bnd, f - bnd,
+                           f - bnd, bnd - sp0, f, st);
+          if (e != cudaSuccess) return e;
         }
       }
     }
     // Schur blocks F[k:f, k:f] -= L21 U12 with the full K = k, before the
     // parent level's extend-add reads them
-    if (kTensorCore<S> && !use_blas && L.max_u > 0 && nall > 0) {
-      const int tpd = (L.max_u + tc::BM - 1) / tc::BM;
-      dim3 g3(tpd * tpd, nall);
-      tc_update_kernel<<<g3, tc::THREADS, tc::SMEM_BYTES, st>>>(
-          L.d_nodes, nall, d.d_nodes, reinterpret_cast<float2*>(arena), tc::kSchur, 0, 0, NBT,
-          d.d_flag + 1);
-      count_launch(1);
-    } else if (!use_blas && L.max_u > 0 && nall > 0) {
+    if (!tc_level && !use_blas && L.max_u > 0 && nall > 0) {
       // one batched launch for all fronts of the level (per-front cuBLAS
       // calls leave the GPU underfilled at these front sizes)
       const int tpd = (L.max_u + 63) / 64;
@@ -1292,6 +1375,20 @@ int mf_perturbed(MFHandle& h) {
   if (h.dev.d_flag) cudaMemcpy(v, h.dev.d_flag, sizeof(v), cudaMemcpyDeviceToHost);
   // d_flag[1]: a bounded wait of the tensor-core update gave up
   return v[1] ? -1 : v[0];
+}
+
+void mf_tc_stats(MFHandle& h, double* out) {
+  MFDevice& d = h.dev;
+  double ms = 0;
+  for (int i = 0; i < d.tc_n; ++i) {
+    float t = 0;
+    if (cudaEventSynchronize(d.tc_ev[2 * i + 1]) == cudaSuccess &&
+        cudaEventElapsedTime(&t, d.tc_ev[2 * i], d.tc_ev[2 * i + 1]) == cudaSuccess)
+      ms += t;
+  }
+  out[0] = d.tc_n;
+  out[1] = ms;
+  out[2] = d.tc_flops;
 }
 
 void mf_free(MFHandle& h) { free_dev(h.dev); }

@@ -2,10 +2,11 @@
 // fronts, included by mf_numeric.cu inside its anonymous namespace (uses
 // DNode and the row-major front arena).
 //
-// For every front of a level it applies, over one 128 x 128 tile per CTA,
-//   F[rows, cols] -= F[rows, kk0:kk0+K] * F[kk0:kk0+K, cols]
-// for one of two updates (tile_of): the Schur block after all pivot panels,
-// or the trailing block of a finished super-panel.
+// Complex64 fronts are factorised in super-panels; when the super-panel
+// [sp0, bnd) of a front is finished (its last 64-column panel factorised),
+// the trailing block takes, over one 128 x 128 tile per CTA,
+//   F[bnd:f, bnd:f] -= F[bnd:f, sp0:bnd] * F[sp0:bnd, bnd:f]
+// (the last super-panel's trailing block is the Schur complement).
 //
 // Arithmetic: complex FP32 operands are split into TF32 pairs x = hi + lo
 // (hi = x rounded to TF32, lo = x - hi), and every real product is formed as
@@ -113,34 +114,23 @@ struct Tile {
   int row0, nrow, col0, ncol, kk0, K;
 };
 
-enum Mode { kSchur = 0, kTrailing = 1 };
-
-// tile `bx` of the front's update in the given mode (false: no such tile)
-//   kSchur:    [k, f)^2 with K = k (after all pivot panels)
-//   kTrailing: [bnd, f)^2 with K = bnd - sp0, for the super-panel
-//              [sp0, bnd) of width sp that ends with the panel at p0
-__device__ __forceinline__ bool tile_of(const DNode& nd, int mode, int p0, int sp, int nbt,
-                                        int bx, Tile& t) {
-  int r0;
-  if (mode == kSchur) {
-    r0 = nd.k;
-    t.kk0 = 0;
-    t.K = nd.k;
-  } else {
-    if (p0 >= nd.k) return false;
-    const int sp0 = (p0 / sp) * sp;
-    const int bnd = min(nd.k, sp0 + sp);
-    if (p0 + min(nbt, nd.k - p0) != bnd) return false;
-    r0 = bnd;
-    t.kk0 = sp0;
-    t.K = bnd - sp0;
-  }
-  const int mn = nd.f - r0;
+// tile `bx` of the trailing block [bnd, f)^2 with K = bnd - sp0 of the
+// super-panel [sp0, bnd) of width sp that ends with the panel at p0 (false:
+// the front's super-panel does not end there, or no such tile)
+__device__ __forceinline__ bool tile_of(const DNode& nd, int p0, int sp, int nbt, int bx,
+                                        Tile& t) {
+  if (p0 >= nd.k) return false;
+  const int sp0 = (p0 / sp) * sp;
+  const int bnd = min(nd.k, sp0 + sp);
+  if (p0 + min(nbt, nd.k - p0) != bnd) return false;
+  t.kk0 = sp0;
+  t.K = bnd - sp0;
+  const int mn = nd.f - bnd;
   if (mn <= 0 || t.K <= 0) return false;
   const int tpd = (mn + BM - 1) / BM;
   if (bx >= tpd * tpd) return false;
-  t.row0 = r0 + (bx / tpd) * BM;
-  t.col0 = r0 + (bx % tpd) * BN;
+  t.row0 = bnd + (bx / tpd) * BM;
+  t.col0 = bnd + (bx % tpd) * BN;
   t.nrow = min(BM, nd.f - t.row0);
   t.ncol = min(BN, nd.f - t.col0);
   return true;
@@ -148,12 +138,11 @@ __device__ __forceinline__ bool tile_of(const DNode& nd, int mode, int p0, int s
 
 }  // namespace tc
 
-// the update of the given mode (tc::Mode) for every listed front, one
-// 128 x 128 output tile per block (blockIdx.x: tile, blockIdx.y: front)
+// the trailing update of every listed front, one 128 x 128 output tile per
+// block (blockIdx.x: tile, blockIdx.y: front)
 __global__ void __launch_bounds__(tc::THREADS, 1)
     tc_update_kernel(const int32_t* __restrict__ list, int count, const DNode* __restrict__ nodes,
-                     float2* __restrict__ arena, int mode, int p0, int sp, int nbt,
-                     int* __restrict__ err) {
+                     float2* __restrict__ arena, int p0, int sp, int nbt, int* __restrict__ err) {
   using namespace tc;
   extern __shared__ __align__(128) uint8_t tc_smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
@@ -165,7 +154,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
   if (fi >= count) return;
   const DNode nd = nodes[list[fi]];
   Tile tl;
-  if (!tile_of(nd, mode, p0, sp, nbt, (int)blockIdx.x, tl)) return;
+  if (!tile_of(nd, p0, sp, nbt, (int)blockIdx.x, tl)) return;
   const int kk0 = tl.kk0, K = tl.K;
   float2* F = arena + nd.off;
 

@@ -19,6 +19,7 @@ _native.declare("sucem_lu_fronts", ctypes.c_int, [c_vp, c_vp])
 _native.declare("sucem_lu_factor", ctypes.c_int, [c_vp, ctypes.c_int, c_vp, ctypes.c_double, c_vp])
 _native.declare("sucem_lu_solve", ctypes.c_int, [c_vp, ctypes.c_int, c_vp, c_vp, c_vp])
 _native.declare("sucem_lu_perturbed", ctypes.c_int, [c_vp])
+_native.declare("sucem_lu_kernel_stats", ctypes.c_int, [c_vp, c_vp])
 
 DTYPES = {"f32": _native.F32, "f64": _native.F64, "c64": _native.C64, "c128": _native.C128}
 
@@ -85,7 +86,20 @@ class SparseLU:
         return self
 
     def perturbed(self):
-        return _native.lib().sucem_lu_perturbed(self._h)
+        """Number of replaced (perturbed) pivots of the last factorisation."""
+        v = _native.lib().sucem_lu_perturbed(self._h)
+        if v < 0:
+            raise RuntimeError("LU factorisation: a tensor-core update gave up waiting "
+                               "(bounded wait expired); the factor is invalid")
+        return v
+
+    def kernel_stats(self):
+        """Tensor-core Schur updates of the last complex64 factorisation:
+        launches, summed device time (ms, CUDA events on the factor's stream)
+        and algorithmic flops."""
+        out = np.zeros(3, dtype=np.float64)
+        call("sucem_lu_kernel_stats", self._h, ptr(out))
+        return {"launches": int(out[0]), "ms": float(out[1]), "flops": float(out[2])}
 
     def solve(self, b, x=None, stream=None):
         """b: device tensor (factor dtype, or complex128/float64 for a
