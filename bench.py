@@ -269,7 +269,8 @@ def run_gpu(args):
     fac_tflops = lu_flops / (fac_ms * 1e-3) / 1e12
     tc_tflops = tc["flops"] / (tc["ms"] * 1e-3) / 1e12 if tc["ms"] > 0 else 0.0
     tc_flops_launch = tc["flops"] / max(1, tc["launches"])
-    tc_bytes = profiled_traffic("tc_update_kernel")  # DRAM bytes per factor, all launches
+    # DRAM bytes of all tensor-core launches of one factorisation (ncu)
+    tc_bytes = profiled_traffic("tc_update_kernel_per_factorisation")
     tc_traffic = tc_bytes / max(1, tc["launches"]) if tc_bytes else None
     asm_ms = statistics.mean(asm)
     asm_gbs = assembly_bytes(V) / (asm_ms * 1e-3) / 1e9
@@ -397,7 +398,10 @@ def run_reference(args):
 def run_kernel_case(args):
     """Small single-kernel cases for profiling (no JSON contract): 'factor'
     runs warmup+steps complex64 LU factorisations of the driven matrix,
-    'assemble' the fused FP32 assembly, at --cubes^3 and --order."""
+    'lu-solve' one factorisation then warmup+steps LU solves (the
+    preconditioner application of every FGMRES iteration; device-timed
+    mean reported), 'assemble' the fused FP32 assembly, at --cubes^3 and
+    --order."""
     import torch
     from sucemfem import _device
     from sucemfem._native import call, ptr
@@ -410,14 +414,33 @@ def run_kernel_case(args):
     d_eps = torch.as_tensor(eps, dtype=torch.float32, device=dev)
     A = torch.empty(V.nnz, dtype=torch.complex64, device=dev)
     sp = _device.stream_ptr()
-    lu = lu_for_space(V) if args.only == "factor" else None
-    for _ in range(args.warmup + args.steps):
+    lu = lu_for_space(V) if args.only in ("factor", "lu-solve") else None
+    out = {"case": args.only, "cubes": args.cubes, "order": args.order, "n": V.n, "nnz": V.nnz,
+           "runs": args.warmup + args.steps}
+    if args.only == "lu-solve":
         call("sucem_assemble_helmholtz", h, 4, ptr(d_eps), None, float(k0), ptr(A), sp)
-        if lu is not None:
-            lu.factor(A, "c64")
-    torch.cuda.synchronize()
-    print(json.dumps({"case": args.only, "cubes": args.cubes, "order": args.order, "n": V.n,
-                      "nnz": V.nnz, "runs": args.warmup + args.steps}))
+        lu.factor(A, "c64")
+        g = torch.Generator(device="cpu").manual_seed(0)
+        b = torch.complex(torch.randn(V.n, generator=g, dtype=torch.float64),
+                          torch.randn(V.n, generator=g, dtype=torch.float64)).to(dev)
+        x = torch.empty_like(b)
+        for _ in range(args.warmup):
+            lu.solve(b, x)
+        stream = torch.cuda.current_stream(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            lu.solve(b, x)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out["ms_per_solve"] = e0.elapsed_time(e1) / max(1, args.steps)
+    else:
+        for _ in range(args.warmup + args.steps):
+            call("sucem_assemble_helmholtz", h, 4, ptr(d_eps), None, float(k0), ptr(A), sp)
+            if lu is not None:
+                lu.factor(A, "c64")
+        torch.cuda.synchronize()
+    print(json.dumps(out))
 
 
 def jittered_box(n, frac=0.2, seed=0):
@@ -604,7 +627,8 @@ def run_serve(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", default="solve",
-                    choices=["solve", "factor", "assemble", "serve", "precision", "eigen-batch"],
+                    choices=["solve", "factor", "lu-solve", "assemble", "serve", "precision",
+                             "eigen-batch"],
                     help="profiling cases: factor / assemble at --cubes, --order; serve; precision")
     ap.add_argument("--precision-solve-cubes", type=int, default=30)
     ap.add_argument("--cavities", type=int, default=256)

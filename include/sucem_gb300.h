@@ -168,6 +168,27 @@ int sucem_compact_count_noalloc(const sucem_space* sp, int dtype, const void* va
 int sucem_point_sources(const sucem_space* sp, const double* pts, const double* values, int npts,
                         int32_t* cells_out, double* contrib, void* stream);
 
+/* The field E(p) = sum_i x_i N_i(p) at points.  Replaces
+ * Reconstruct.reconstruct_points (sucemfem/PostProcessing/
+ * PostProcessing.py:27-60).  Points are located as for the point sources
+ * (lowest-index cell whose closure contains the point).  Device arrays: x
+ * the DOF vector (dtype SUCEM_C64 or SUCEM_C128, interleaved complex); pts
+ * double[npts*3]; cells_out int32[npts] (0x7f7f7f7f for a point outside the
+ * mesh); E complex128[npts*3] (NaN for a point outside the mesh). */
+int sucem_reconstruct_points(const sucem_space* sp, int dtype, const void* x, const double* pts,
+                             int npts, int32_t* cells_out, double* E, void* stream);
+
+/* Real power flux through the whole mesh boundary, replacing
+ * SurfaceFlux.calc_flux (sucemfem/PostProcessing/power_flux.py:11-60):
+ *   (1/(k0 Z0)) * int n . (E_r x (-curl E_i / mu_r) + E_i x (curl E_r / mu_r)) ds
+ * over every exterior facet with the outward normal n (a 9-point facet rule,
+ * exact for orders 1 and 2).  Device arrays: x (SUCEM_C64 or SUCEM_C128);
+ * mu_r double per cell or NULL (1); part double[nt] scratch (per-cell
+ * contributions); out double[1].  The sum is taken in a fixed order, so
+ * repeated calls give identical results. */
+int sucem_surface_flux(const sucem_space* sp, int dtype, const void* x, double k0,
+                       const double* mu_r, double* part, double* out, void* stream);
+
 /* ---- vectors and general CSR (device arrays) ----
  * The Krylov / refinement building blocks behind solve_sparse_system and the
  * solver classes of sucemfem/Utilities/LinalgSolvers.py:239-322.

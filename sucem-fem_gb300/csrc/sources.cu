@@ -1,7 +1,11 @@
-// Current point sources: point location and N1curl basis evaluation on the
-// GPU, the replacement of calc_pointsource_contrib
-// (sucemfem/Sources/point_source.py:49-94: CGAL point location, then FIAT
-// evaluate_basis_all, contribution N_i(p) . J).
+// Field evaluation on the GPU: point location and N1curl basis evaluation
+// for the current point sources (replacing calc_pointsource_contrib,
+// sucemfem/Sources/point_source.py:49-94: CGAL point location, then FIAT
+// evaluate_basis_all, contribution N_i(p) . J), the field at arbitrary
+// points (Reconstruct.reconstruct_points,
+// sucemfem/PostProcessing/PostProcessing.py:27-60) and the real power flux
+// through the boundary (SurfaceFlux.calc_flux,
+// sucemfem/PostProcessing/power_flux.py:11-60).
 //
 // Cell rule: among the cells whose closure contains the point (barycentric
 // coordinates >= -1e-12) the lowest cell index is taken.  Points on a
@@ -112,6 +116,215 @@ __global__ void evaluate_kernel(int64_t nt, const int4* __restrict__ cells,
 
 bool g_tables_loaded[64] = {false};
 
+// ---- surface power flux ----
+// 3 x 3 collapsed Gauss rule on the reference triangle (s, t); exact to
+// degree 4, the flux integrand has degree 2 * order - 1
+constexpr int kFaceQ = 9;
+// UFC local faces: face f is opposite vertex f
+__constant__ int c_face_vert[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+__constant__ double c_fw[kFaceQ];
+// reference basis value (0..2) and curl (3..5) at the quadrature points of
+// every local face, per order
+__constant__ double c_fq1[4][kFaceQ][6][6];
+__constant__ double c_fq2[4][kFaceQ][20][6];
+bool g_face_loaded[64] = {false};
+
+template <int ND>
+void face_tables(const double (*nb)[3][10], double (*out)[kFaceQ][ND][6], double* w) {
+  const double g[3] = {-0.7745966692414834, 0.0, 0.7745966692414834};
+  const double gw[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+  const double rv[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  const int fv[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+  for (int f = 0; f < 4; ++f)
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        const int q = 3 * i + j;
+        const double u = 0.5 * (g[i] + 1.0), v = 0.5 * (g[j] + 1.0);
+        const double s = u, t = v * (1.0 - u);
+        w[q] = 0.25 * gw[i] * gw[j] * (1.0 - u);
+        double X[3];
+        for (int r = 0; r < 3; ++r)
+          X[r] = rv[fv[f][0]][r] + s * (rv[fv[f][1]][r] - rv[fv[f][0]][r]) +
+                 t * (rv[fv[f][2]][r] - rv[fv[f][0]][r]);
+        const double mono[10] = {1.0,         X[0],        X[1],        X[2],        X[0] * X[0],
+                                 X[1] * X[1], X[2] * X[2], X[0] * X[1], X[0] * X[2], X[1] * X[2]};
+        for (int a = 0; a < ND; ++a) {
+          double d[3][3];  // d[p][r] = dN_p / dX_r
+          for (int p = 0; p < 3; ++p) {
+            const double* c = nb[a][p];
+            double val = 0;
+            for (int m = 0; m < 10; ++m) val += c[m] * mono[m];
+            out[f][q][a][p] = val;
+            d[p][0] = c[1] + 2 * c[4] * X[0] + c[7] * X[1] + c[8] * X[2];
+            d[p][1] = c[2] + 2 * c[5] * X[1] + c[7] * X[0] + c[9] * X[2];
+            d[p][2] = c[3] + 2 * c[6] * X[2] + c[8] * X[0] + c[9] * X[1];
+          }
+          out[f][q][a][3] = d[2][1] - d[1][2];
+          out[f][q][a][4] = d[0][2] - d[2][0];
+          out[f][q][a][5] = d[1][0] - d[0][1];
+        }
+      }
+}
+
+__device__ __forceinline__ double2 ld_c(const double2* x, int64_t i) { return x[i]; }
+__device__ __forceinline__ double2 ld_c(const float2* x, int64_t i) {
+  const float2 v = x[i];
+  return make_double2(v.x, v.y);
+}
+
+// one thread per cell: the flux through its exterior facets (in local face
+// order), written to part[c] (0 for interior cells)
+template <int ND, typename T>
+__global__ void surface_flux_kernel(int64_t nt, const int4* __restrict__ cells,
+                                    const double* __restrict__ xyz,
+                                    const uint8_t* __restrict__ ext_mask,
+                                    const int32_t* __restrict__ cell_dofs,
+                                    const T* __restrict__ x, const double* __restrict__ mu_r,
+                                    double scale, double* __restrict__ part) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nt) return;
+  const int mask = ext_mask[c];
+  double acc = 0.0;
+  if (mask) {
+    const int4 v = cells[c];
+    double J[3][3], Ji[3][3], x0[3];
+    jac(xyz, v, J, x0);
+    inv3(J, Ji);
+    const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                       J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                       J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    const int vid[4] = {v.x, v.y, v.z, v.w};
+    double2 xe[ND];
+    for (int a = 0; a < ND; ++a) xe[a] = ld_c(x, cell_dofs[c * ND + a]);
+    const double inv_mu = mu_r ? 1.0 / mu_r[c] : 1.0;
+    for (int f = 0; f < 4; ++f) {
+      if (!(mask >> f & 1)) continue;
+      double P[3][3];
+      for (int k = 0; k < 3; ++k)
+        for (int r = 0; r < 3; ++r) P[k][r] = xyz[3 * (int64_t)vid[c_face_vert[f][k]] + r];
+      double cr[3] = {(P[1][1] - P[0][1]) * (P[2][2] - P[0][2]) - (P[1][2] - P[0][2]) * (P[2][1] - P[0][1]),
+                      (P[1][2] - P[0][2]) * (P[2][0] - P[0][0]) - (P[1][0] - P[0][0]) * (P[2][2] - P[0][2]),
+                      (P[1][0] - P[0][0]) * (P[2][1] - P[0][1]) - (P[1][1] - P[0][1]) * (P[2][0] - P[0][0])};
+      // outward: away from the vertex opposite the face
+      double o = 0;
+      for (int r = 0; r < 3; ++r) o += cr[r] * (P[0][r] - xyz[3 * (int64_t)vid[f] + r]);
+      const double sg = o < 0 ? -1.0 : 1.0;
+      const double area2 = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+      double n[3];
+      for (int r = 0; r < 3; ++r) n[r] = sg * cr[r] / area2;
+      double s = 0;
+      for (int q = 0; q < kFaceQ; ++q) {
+        double eh[2][3] = {{0, 0, 0}, {0, 0, 0}}, ch[2][3] = {{0, 0, 0}, {0, 0, 0}};
+        for (int a = 0; a < ND; ++a) {
+          const double* t = ND == 6 ? c_fq1[f][q][a % 6] : c_fq2[f][q][a];
+          for (int r = 0; r < 3; ++r) {
+            eh[0][r] += xe[a].x * t[r];
+            eh[1][r] += xe[a].y * t[r];
+            ch[0][r] += xe[a].x * t[3 + r];
+            ch[1][r] += xe[a].y * t[3 + r];
+          }
+        }
+        // E = J^-T E_hat, curl E = J curl E_hat / det J  (Re, Im)
+        double E[2][3], C[2][3];
+        for (int k = 0; k < 2; ++k)
+          for (int i = 0; i < 3; ++i) {
+            E[k][i] = Ji[0][i] * eh[k][0] + Ji[1][i] * eh[k][1] + Ji[2][i] * eh[k][2];
+            C[k][i] = (J[i][0] * ch[k][0] + J[i][1] * ch[k][1] + J[i][2] * ch[k][2]) / det * inv_mu;
+          }
+        // n . (E_r x (-curl E_i) + E_i x curl E_r)
+        double g3[3];
+        for (int i = 0; i < 3; ++i) {
+          const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+          g3[i] = -(E[0][i1] * C[1][i2] - E[0][i2] * C[1][i1]) + (E[1][i1] * C[0][i2] - E[1][i2] * C[0][i1]);
+        }
+        s += c_fw[q] * (n[0] * g3[0] + n[1] * g3[1] + n[2] * g3[2]);
+      }
+      acc += s * area2;
+    }
+  }
+  part[c] = acc * scale;
+}
+
+// one block: out[0] = sum of part[0:n) in a fixed order
+__global__ void __launch_bounds__(1024) sum_kernel(int64_t n, const double* __restrict__ part,
+                                                   double* __restrict__ out) {
+  __shared__ double red[1024];
+  double s = 0;
+  for (int64_t i = threadIdx.x; i < n; i += 1024) s += part[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = 512; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = red[0];
+}
+
+// ---- field at points: one warp per point, lane = local basis function ----
+template <int ND, typename T>
+__global__ void reconstruct_kernel(int64_t nt, const int4* __restrict__ cells,
+                                   const double* __restrict__ xyz,
+                                   const int32_t* __restrict__ cell_dofs, const T* __restrict__ x,
+                                   const double* __restrict__ pts, int npts,
+                                   const int* __restrict__ cell_in, double* __restrict__ E) {
+  const int p = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (p >= npts) return;
+  const int c = cell_in[p];
+  double* out = E + 6 * (int64_t)p;
+  if (c < 0 || c >= nt) {
+    if (lane < 6) out[lane] = __longlong_as_double(0x7ff8000000000000LL);  // NaN: outside
+    return;
+  }
+  double J[3][3], Ji[3][3], x0[3];
+  jac(xyz, cells[c], J, x0);
+  inv3(J, Ji);
+  const double d[3] = {pts[3 * p] - x0[0], pts[3 * p + 1] - x0[1], pts[3 * p + 2] - x0[2]};
+  double X[3];
+  for (int r = 0; r < 3; ++r) X[r] = Ji[r][0] * d[0] + Ji[r][1] * d[1] + Ji[r][2] * d[2];
+  double e[6] = {0, 0, 0, 0, 0, 0};
+  if (lane < ND) {
+    const double mono[10] = {1.0,         X[0],        X[1],        X[2],        X[0] * X[0],
+                             X[1] * X[1], X[2] * X[2], X[0] * X[1], X[0] * X[2], X[1] * X[2]};
+    double nh[3];
+    for (int q = 0; q < 3; ++q) {
+      double s = 0;
+      for (int m = 0; m < 10; ++m) s += (ND == 6 ? c_nb1[lane % 6][q][m] : c_nb2[lane][q][m]) * mono[m];
+      nh[q] = s;
+    }
+    const double2 xv = ld_c(x, cell_dofs[(int64_t)c * ND + lane]);
+    for (int i = 0; i < 3; ++i) {
+      const double ni = Ji[0][i] * nh[0] + Ji[1][i] * nh[1] + Ji[2][i] * nh[2];
+      e[2 * i] = xv.x * ni;
+      e[2 * i + 1] = xv.y * ni;
+    }
+  }
+  for (int k = 0; k < 6; ++k)
+    for (int o = 16; o > 0; o >>= 1) e[k] += __shfl_down_sync(~0u, e[k], o);
+  if (lane == 0)
+    for (int k = 0; k < 6; ++k) out[k] = e[k];
+}
+
+cudaError_t load_point_tables(int dev) {
+  if (dev < 64 && g_tables_loaded[dev]) return cudaSuccess;
+  cudaError_t e = cudaMemcpyToSymbol(c_nb1, NB1, sizeof(NB1));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_nb2, NB2, sizeof(NB2));
+  if (e == cudaSuccess && dev < 64) g_tables_loaded[dev] = true;
+  return e;
+}
+
+cudaError_t load_face_tables(int dev) {
+  if (dev < 64 && g_face_loaded[dev]) return cudaSuccess;
+  static double t1[4][kFaceQ][6][6], t2[4][kFaceQ][20][6], w[kFaceQ];
+  face_tables<6>(NB1, t1, w);
+  face_tables<20>(NB2, t2, w);
+  cudaError_t e = cudaMemcpyToSymbol(c_fq1, t1, sizeof(t1));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_fq2, t2, sizeof(t2));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_fw, w, sizeof(w));
+  if (e == cudaSuccess && dev < 64) g_face_loaded[dev] = true;
+  return e;
+}
+
 }  // namespace
 }  // namespace sucem
 
@@ -127,13 +340,9 @@ extern "C" int sucem_point_sources(const sucem_space* sp, const double* pts,
   cudaStream_t s = (cudaStream_t)stream;
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 64 && !g_tables_loaded[dev]) {
-    cudaError_t e = cudaMemcpyToSymbol(c_nb1, NB1, sizeof(NB1));
-    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_nb2, NB2, sizeof(NB2));
-    if (e != cudaSuccess) return cuda_fail(e, "sucem_point_sources tables");
-    g_tables_loaded[dev] = true;
-  }
-  cudaError_t e = cudaMemsetAsync(cells_out, 0x7f, sizeof(int32_t) * npts, s);
+  cudaError_t e = load_point_tables(dev);
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_point_sources tables");
+  e = cudaMemsetAsync(cells_out, 0x7f, sizeof(int32_t) * npts, s);
   if (e != cudaSuccess) return cuda_fail(e, "sucem_point_sources memset");
   // 0x7f7f7f7f (>= nt for any supported mesh) marks a point outside the mesh
   const int threads = 256;
@@ -149,4 +358,78 @@ extern "C" int sucem_point_sources(const sucem_space* sp, const double* pts,
   e = cudaGetLastError();
   count_launch(2);
   return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_point_sources");
+}
+
+extern "C" int sucem_reconstruct_points(const sucem_space* sp, int dtype, const void* x,
+                                        const double* pts, int npts, int32_t* cells_out,
+                                        double* E, void* stream) {
+  using namespace sucem;
+  const DeviceSpace* d = sp ? sp->s.dev : nullptr;
+  if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  if (dtype != SUCEM_C64 && dtype != SUCEM_C128) return fail("dtype must be complex", SUCEM_ERR_ARG);
+  if (npts < 0) return fail("negative point count", SUCEM_ERR_ARG);
+  if (npts == 0) return SUCEM_OK;
+  if (!x || !pts || !cells_out || !E) return fail("null argument", SUCEM_ERR_ARG);
+  cudaStream_t s = (cudaStream_t)stream;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaError_t e = load_point_tables(dev);
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_reconstruct_points tables");
+  e = cudaMemsetAsync(cells_out, 0x7f, sizeof(int32_t) * npts, s);
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_reconstruct_points memset");
+  const int threads = 256;
+  locate_kernel<<<(unsigned)((d->nt + threads - 1) / threads), threads, 0, s>>>(
+      d->nt, d->cells, d->xyz, pts, npts, cells_out);
+  const unsigned eb = (unsigned)(((int64_t)npts * 32 + threads - 1) / threads);
+  if (d->nd == 6 && dtype == SUCEM_C128)
+    reconstruct_kernel<6, double2><<<eb, threads, 0, s>>>(d->nt, d->cells, d->xyz, d->cell_dofs,
+                                                          (const double2*)x, pts, npts, cells_out, E);
+  else if (d->nd == 6)
+    reconstruct_kernel<6, float2><<<eb, threads, 0, s>>>(d->nt, d->cells, d->xyz, d->cell_dofs,
+                                                         (const float2*)x, pts, npts, cells_out, E);
+  else if (dtype == SUCEM_C128)
+    reconstruct_kernel<20, double2><<<eb, threads, 0, s>>>(d->nt, d->cells, d->xyz, d->cell_dofs,
+                                                           (const double2*)x, pts, npts, cells_out, E);
+  else
+    reconstruct_kernel<20, float2><<<eb, threads, 0, s>>>(d->nt, d->cells, d->xyz, d->cell_dofs,
+                                                          (const float2*)x, pts, npts, cells_out, E);
+  e = cudaGetLastError();
+  count_launch(2);
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_reconstruct_points");
+}
+
+extern "C" int sucem_surface_flux(const sucem_space* sp, int dtype, const void* x, double k0,
+                                  const double* mu_r, double* part, double* out, void* stream) {
+  using namespace sucem;
+  const DeviceSpace* d = sp ? sp->s.dev : nullptr;
+  if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  if (dtype != SUCEM_C64 && dtype != SUCEM_C128) return fail("dtype must be complex", SUCEM_ERR_ARG);
+  if (!(k0 > 0)) return fail("k0 must be positive", SUCEM_ERR_ARG);
+  if (!x || !part || !out) return fail("null argument", SUCEM_ERR_ARG);
+  cudaStream_t s = (cudaStream_t)stream;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaError_t e = load_face_tables(dev);
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_surface_flux tables");
+  // Consts.py: Z0 = mu0 * c0
+  const double z0 = 3.141592653589793 * 4e-7 * 299792458.0;
+  const double scale = 1.0 / (k0 * z0);
+  const int threads = 128;
+  const unsigned blocks = (unsigned)((d->nt + threads - 1) / threads);
+  if (d->nd == 6 && dtype == SUCEM_C128)
+    surface_flux_kernel<6, double2><<<blocks, threads, 0, s>>>(
+        d->nt, d->cells, d->xyz, d->ext_mask, d->cell_dofs, (const double2*)x, mu_r, scale, part);
+  else if (d->nd == 6)
+    surface_flux_kernel<6, float2><<<blocks, threads, 0, s>>>(
+        d->nt, d->cells, d->xyz, d->ext_mask, d->cell_dofs, (const float2*)x, mu_r, scale, part);
+  else if (dtype == SUCEM_C128)
+    surface_flux_kernel<20, double2><<<blocks, threads, 0, s>>>(
+        d->nt, d->cells, d->xyz, d->ext_mask, d->cell_dofs, (const double2*)x, mu_r, scale, part);
+  else
+    surface_flux_kernel<20, float2><<<blocks, threads, 0, s>>>(
+        d->nt, d->cells, d->xyz, d->ext_mask, d->cell_dofs, (const float2*)x, mu_r, scale, part);
+  sum_kernel<<<1, 1024, 0, s>>>(d->nt, part, out);
+  e = cudaGetLastError();
+  count_launch(2);
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_surface_flux");
 }

@@ -1,11 +1,83 @@
 """Tetrahedral mesh objects standing in for the dolfin ones the reference's
 drivers receive (dolfin.Mesh, dolfin.MeshFunction, dolfin.UnitCube,
-dolfin.DomainBoundary).  Plain numpy arrays underneath."""
+dolfin.DomainBoundary).  Plain numpy arrays underneath.  ``Mesh(filename)``
+and ``MeshFunction(type, mesh, filename)`` read DOLFIN XML files (the
+format of the reference's meshes and facet/physical-region functions)."""
+import xml.etree.ElementTree as ET
+
 import numpy as np
 
 
+def _tag(e):
+    return e.tag.rsplit("}", 1)[-1]
+
+
+def _child(e, name):
+    for c in e:
+        if _tag(c) == name:
+            return c
+    return None
+
+
+def read_dolfin_xml_mesh(filename):
+    """(coordinates (nv, 3), cells (nt, 4)) of a DOLFIN XML tetrahedral mesh
+    (``<dolfin><mesh celltype="tetrahedron" dim="3"><vertices>...
+    <cells><tetrahedron index v0 v1 v2 v3/>``)."""
+    root = ET.parse(filename).getroot()
+    mesh = root if _tag(root) == "mesh" else _child(root, "mesh")
+    if mesh is None:
+        raise ValueError("%s: no <mesh> element" % filename)
+    if mesh.get("celltype", "tetrahedron") != "tetrahedron" or int(mesh.get("dim", 3)) != 3:
+        raise ValueError("%s: only 3-D tetrahedral meshes are supported" % filename)
+    verts, cells = _child(mesh, "vertices"), _child(mesh, "cells")
+    if verts is None or cells is None:
+        raise ValueError("%s: <vertices> and <cells> are required" % filename)
+    nv = int(verts.get("size", len(verts)))
+    x = np.full((nv, 3), np.nan)
+    for v in verts:
+        i = int(v.get("index"))
+        x[i] = [float(v.get("x")), float(v.get("y", 0.0)), float(v.get("z", 0.0))]
+    nt = int(cells.get("size", len(cells)))
+    c = np.full((nt, 4), -1, dtype=np.int64)
+    for t in cells:
+        if _tag(t) != "tetrahedron":
+            raise ValueError("%s: cell type %s is not a tetrahedron" % (filename, _tag(t)))
+        c[int(t.get("index"))] = [int(t.get("v%d" % k)) for k in range(4)]
+    if np.isnan(x).any() or (c < 0).any() or c.max() >= nv:
+        raise ValueError("%s: incomplete vertex or cell list" % filename)
+    return x, c
+
+
+def read_dolfin_xml_meshfunction(filename):
+    """(dim, values) of a DOLFIN XML mesh function (``<meshfunction
+    type="uint" dim=".." size=".."><entity index value/>``)."""
+    root = ET.parse(filename).getroot()
+    if _tag(root) in ("meshfunction", "mesh_function"):
+        mf = root
+    else:
+        mf = _child(root, "meshfunction")
+        if mf is None:
+            mf = _child(root, "mesh_function")
+    if mf is None:
+        raise ValueError("%s: no <meshfunction> element" % filename)
+    size = int(mf.get("size"))
+    vals = np.zeros(size, dtype=np.int64)
+    seen = np.zeros(size, dtype=bool)
+    for e in mf:
+        i = int(e.get("index"))
+        vals[i] = int(e.get("value"))
+        seen[i] = True
+    if not seen.all():
+        raise ValueError("%s: %d entities without a value" % (filename, int((~seen).sum())))
+    return int(mf.get("dim")), vals
+
+
 class Mesh:
-    def __init__(self, coordinates, cells):
+    def __init__(self, coordinates, cells=None):
+        if cells is None:
+            if not isinstance(coordinates, str):
+                raise ValueError("Mesh(filename) or Mesh(coordinates, cells)")
+            coordinates, cells = read_dolfin_xml_mesh(coordinates)
         self._x = np.ascontiguousarray(coordinates, dtype=np.float64)
         c = np.asarray(cells, dtype=np.int64)
         if c.ndim != 2 or c.shape[1] != 4 or self._x.ndim != 2 or self._x.shape[1] != 3:
@@ -42,6 +114,19 @@ class MeshFunction:
 
     def __init__(self, value_type, mesh, dim, value=0):
         self.mesh = mesh
+        if isinstance(dim, str):
+            # MeshFunction(type, mesh, filename): DOLFIN XML; facet (dim 2)
+            # indices follow DOLFIN's facet numbering, which the space's
+            # face numbering reproduces
+            fdim, vals = read_dolfin_xml_meshfunction(dim)
+            self.dim = fdim
+            if fdim == 3 and len(vals) != mesh.num_cells():
+                raise ValueError("cell function size %d != %d cells" % (len(vals), mesh.num_cells()))
+            if fdim not in (2, 3):
+                raise ValueError("only cell (3) and facet (2) mesh functions are supported")
+            self._a = vals
+            self._fill = value
+            return
         self.dim = int(dim)
         if self.dim == 3:
             size = mesh.num_cells()

@@ -10,7 +10,14 @@ written here.  Sources:
 * sucemfem/Sources/tests/fillament_source_test_data.pickle
   (test_fillament_source.py:34-69): order-2 filament RHS contributions.
 * sucemfem/PostProcessing/tests/data/power_flux_reference_dofs_*.pickle
-  (generator power_flux_generate_dofs.py:33-102): order-2 driven solution.
+  (generator power_flux_generate_dofs.py:33-102): order-2 driven solution,
+  its DOLFIN XML mesh (coordinates rounded to 6 digits: the mesh the
+  reference's power-flux test integrates on; kept as XML text) and the
+  test's expected flux (test_power_flux.py:54, SurfaceFlux, and :77,
+  VariationalSurfaceFlux).
+* functional_tests/data/meshes/rectangular_prism{,_facet_region}.xml: a
+  DOLFIN XML mesh and facet mesh function, kept as XML text for the reader
+  tests.
 * sucemfem/PostProcessing/tests/data/reference_dofs-2-0.149896229-*.pickle
   (generator ntff_generate_dofs.py:40-95): order-2 driven solution of a
   point dipole on a shifted 5^3 cube.
@@ -42,11 +49,22 @@ def main():
                         **{k: np.asarray(v) for k, v in d.items()})
     dd = os.path.join(REF, "sucemfem/PostProcessing/tests/data")
     d = load_pickle(os.path.join(dd, "power_flux_reference_dofs_f-1000000000.000000_o-2_s-0.074948_l-0.100000_h-0.166667.pickle"))
+    with open(os.path.join(dd, d["meshfile"])) as f:
+        mesh_xml = f.read()
     np.savez_compressed(os.path.join(OUT, "power_flux_solution_o2.npz"),
                         x=d["x"], freq=d["freq"], order=d["order"], I=d["I"],
                         source_endpoints=d["source_endpoints"],
                         domain_size=0.25 * 299792458 / 1e9, max_edge_len=299792458 / 1e9 / 6,
-                        no_integration_points=100)
+                        no_integration_points=100, mesh_xml=np.array(mesh_xml),
+                        flux_surface=26.3586862457,
+                        flux_variational=26.9015957282 - 7.85747240242e-08j)
+    md = os.path.join(REF, "functional_tests/data/meshes")
+    texts = {}
+    for key, name in (("mesh_xml", "rectangular_prism.xml"),
+                      ("facet_xml", "rectangular_prism_facet_region.xml")):
+        with open(os.path.join(md, name)) as f:
+            texts[key] = np.array(f.read())
+    np.savez_compressed(os.path.join(OUT, "rectangular_prism_xml.npz"), **texts)
     d = load_pickle(os.path.join(dd, "reference_dofs-2-0.149896229-0.0499654096667.pickle"))
     np.savez_compressed(os.path.join(OUT, "ntff_solution_o2.npz"),
                         x=d["x"], freq=d["freq"], order=d["order"],

@@ -1,0 +1,98 @@
+"""GPU post-processing parity (through the C-ABI): the surface power flux
+against the reference's golden (test_power_flux.py:54, 7 places, on the
+test's own XML mesh) and the FP64 oracle, and the field at points against
+the oracle."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import fem, postproc
+
+pytestmark = pytest.mark.gpu
+
+
+def _xml_space(tmp_path, text, order):
+    from sucemfem.mesh import Mesh
+    from sucemfem.space import FunctionSpace
+    p = os.path.join(str(tmp_path), "m.xml")
+    with open(p, "w") as f:
+        f.write(str(text))
+    m = Mesh(p)
+    return m, FunctionSpace(m, order=order)
+
+
+def test_surface_flux_reference_golden(tmp_path):
+    from sucemfem.PostProcessing.power_flux import SurfaceFlux
+    g = golden("power_flux_solution_o2.npz")
+    m, V = _xml_space(tmp_path, g["mesh_xml"], 2)
+    k0 = 2 * np.pi * float(g["freq"]) / fem.C0
+    sf = SurfaceFlux(V)
+    sf.set_k0(k0)
+    sf.set_dofs(g["x"])
+    v = sf.calc_flux()
+    assert abs(v - float(g["flux_surface"])) < 5e-8, v
+    A = fem.assemble(m.coordinates(), m.cells(), 2)
+    ref = postproc.surface_flux(m.coordinates(), m.cells(), 2, A.topo, A.dofmap, g["x"], k0)
+    assert abs(v - ref) < 1e-12 * abs(ref)
+    assert sf.calc_flux() == v  # fixed-order reduction: bit-identical repeat
+
+
+def test_surface_flux_complex64_dofs_and_mu(tmp_path):
+    import torch
+    from sucemfem import _device
+    from sucemfem.PostProcessing.power_flux import SurfaceFlux
+    g = golden("power_flux_solution_o2.npz")
+    m, V = _xml_space(tmp_path, g["mesh_xml"], 2)
+    k0 = 2 * np.pi * float(g["freq"]) / fem.C0
+    mu = np.random.default_rng(3).uniform(1.0, 3.0, m.num_cells())
+    A = fem.assemble(m.coordinates(), m.cells(), 2)
+    ref = postproc.surface_flux(m.coordinates(), m.cells(), 2, A.topo, A.dofmap, g["x"], k0, mu)
+    sf = SurfaceFlux(V)
+    sf.set_k0(k0)
+    sf.set_mur_function(mu)
+    sf.set_dofs(g["x"])
+    assert abs(sf.calc_flux() - ref) < 1e-12 * abs(ref)
+    sf.set_dofs(torch.as_tensor(g["x"]).to(torch.complex64).to(_device.device()))
+    assert abs(sf.calc_flux() - ref) < 1e-5 * abs(ref)
+
+
+def test_surface_flux_order1_box():
+    from sucemfem.mesh import Mesh
+    from sucemfem.space import FunctionSpace
+    from sucemfem.PostProcessing.power_flux import SurfaceFlux
+    coords, cells = fem.box_mesh(1.0, 0.5, 0.75, 3, 2, 3)
+    coords = fem.jitter_interior(coords, cells, 0.25, 0.2, seed=1)
+    V = FunctionSpace(Mesh(coords, cells), order=1)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(V.n) + 1j * rng.standard_normal(V.n)
+    A = fem.assemble(coords, cells, 1)
+    ref = postproc.surface_flux(coords, cells, 1, A.topo, A.dofmap, x, 7.0)
+    sf = SurfaceFlux(V)
+    sf.set_k0(7.0)
+    sf.set_dofs(x)
+    assert abs(sf.calc_flux() - ref) < 1e-12 * max(1.0, abs(ref))
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_reconstruct_points(order):
+    from sucemfem.mesh import Mesh
+    from sucemfem.space import FunctionSpace
+    from sucemfem.PostProcessing import Reconstruct
+    coords, cells = fem.box_mesh(1.0, 1.0, 1.0, 3, 3, 3)
+    coords = fem.jitter_interior(coords, cells, 1 / 3, 0.2, seed=2)
+    V = FunctionSpace(Mesh(coords, cells), order=order)
+    A = fem.assemble(coords, cells, order)
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal(V.n) + 1j * rng.standard_normal(V.n)
+    pts = np.vstack([rng.uniform(0.02, 0.98, (40, 3)), [[0.5, 0.5, 0.5], [2.0, 0.5, 0.5]]])
+    r = Reconstruct(V)
+    r.set_dof_values(x)
+    got = r.reconstruct_points(pts)
+    ref = postproc.reconstruct_points(coords, cells, order, A.dofmap, x, pts)
+    inside = ~np.isnan(ref[:, 0].real)
+    assert inside.sum() == len(pts) - 1 and not inside[-1]
+    assert np.all(np.isnan(got[~inside].real))
+    err = np.abs(got[inside] - ref[inside]).max() / np.abs(ref[inside]).max()
+    assert err < 1e-12, err
