@@ -189,6 +189,21 @@ int sucem_reconstruct_points(const sucem_space* sp, int dtype, const void* x, co
 int sucem_surface_flux(const sucem_space* sp, int dtype, const void* x, double k0,
                        const double* mu_r, double* part, double* out, void* stream);
 
+/* Surface near-to-far-field transform, replacing NTFF.calc_pt
+ * (sucemfem/PostProcessing/surface_ntff.py:29-155): equivalent currents
+ * J = n x H (H = j curl E / (k0 Z0)) and M = -n x E on every exterior facet,
+ * radiated to the directions (theta[d], phi[d]) (radians, device arrays):
+ *   N = int J e^{j k0 r'.r_hat} ds,  L = int M e^{j k0 r'.r_hat} ds,
+ *   E_theta = -r_fac (L_phi + Z0 N_theta),  E_phi = r_fac (L_theta - Z0 N_phi),
+ *   r_fac = j k0 e^{-j k0} / (4 pi)  (far field normalised to radius 1),
+ * with the 9-point collapsed Gauss-Jacobi facet rule.  out: device double
+ * [ndir*12] = per direction E_theta, E_phi, L_theta, L_phi, N_theta, N_phi
+ * (complex, interleaved); each direction is summed in a fixed order.  The
+ * per-point scratch lives in the space handle (allocated on the first
+ * call): calls on one space must not overlap on the GPU. */
+int sucem_ntff(const sucem_space* sp, int dtype, const void* x, double k0, int ndir,
+               const double* theta, const double* phi, double* out, void* stream);
+
 /* ---- vectors and general CSR (device arrays) ----
  * The Krylov / refinement building blocks behind solve_sparse_system and the
  * solver classes of sucemfem/Utilities/LinalgSolvers.py:239-322.

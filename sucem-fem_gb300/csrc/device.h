@@ -27,6 +27,11 @@ struct DeviceSpace {
   int32_t* boundary_dofs = nullptr;
   int64_t n_boundary = 0;
   int32_t* bidx = nullptr;        // nt: index among cells with exterior facets, -1 otherwise
+  // exterior facets (cell, local face) and the far-field scratch of the
+  // NTFF (allocated on first use)
+  int32_t* ext_facets = nullptr;  // n_ext*2
+  int64_t n_ext = 0;
+  double* ntff_pts = nullptr;     // n_ext*9 points x 16 doubles
   int64_t nb = 0;                 // number of cells with exterior facets
   // per-cell coefficient scratch of the assembly (allocated on first use)
   float* g_f = nullptr;           // nt*12

@@ -15,6 +15,7 @@
 
 #include <climits>
 #include <cstdint>
+#include <vector>
 
 #include "../../include/sucem_gb300.h"
 #include "device.h"
@@ -117,8 +118,10 @@ __global__ void evaluate_kernel(int64_t nt, const int4* __restrict__ cells,
 bool g_tables_loaded[64] = {false};
 
 // ---- surface power flux ----
-// 3 x 3 collapsed Gauss rule on the reference triangle (s, t); exact to
-// degree 4, the flux integrand has degree 2 * order - 1
+// 3 x 3 collapsed Gauss-Jacobi rule on the reference triangle (Gauss-Jacobi
+// (alpha = 1) in the collapsed direction, Gauss-Legendre in the other): exact
+// to degree 5 (the flux integrand has degree 2 * order - 1), and the rule the
+// reference's form compiler integrates its far-field forms with
 constexpr int kFaceQ = 9;
 // UFC local faces: face f is opposite vertex f
 __constant__ int c_face_vert[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
@@ -127,25 +130,32 @@ __constant__ double c_fw[kFaceQ];
 // every local face, per order
 __constant__ double c_fq1[4][kFaceQ][6][6];
 __constant__ double c_fq2[4][kFaceQ][20][6];
+// reference coordinates of the quadrature points of every local face
+__constant__ double c_fX[4][kFaceQ][3];
 bool g_face_loaded[64] = {false};
 
 template <int ND>
-void face_tables(const double (*nb)[3][10], double (*out)[kFaceQ][ND][6], double* w) {
-  const double g[3] = {-0.7745966692414834, 0.0, 0.7745966692414834};
-  const double gw[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+void face_tables(const double (*nb)[3][10], double (*out)[kFaceQ][ND][6], double* w,
+                 double (*Xo)[kFaceQ][3]) {
+  // Gauss-Jacobi (1, 0) and Gauss-Legendre nodes and weights on [-1, 1]
+  const double ga[3] = {-0.8228240809745921, -0.1810662711185305, 0.5753189235216941};
+  const double gwa[3] = {0.8037276549558384, 0.9169644254383448, 0.2793079196058167};
+  const double gb[3] = {-0.7745966692414834, 0.0, 0.7745966692414834};
+  const double gwb[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
   const double rv[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
   const int fv[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
   for (int f = 0; f < 4; ++f)
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) {
         const int q = 3 * i + j;
-        const double u = 0.5 * (g[i] + 1.0), v = 0.5 * (g[j] + 1.0);
+        const double u = 0.5 * (ga[i] + 1.0), v = 0.5 * (gb[j] + 1.0);
         const double s = u, t = v * (1.0 - u);
-        w[q] = 0.25 * gw[i] * gw[j] * (1.0 - u);
+        w[q] = 0.125 * gwa[i] * gwb[j];  // the Jacobi weight carries (1 - u)
         double X[3];
         for (int r = 0; r < 3; ++r)
           X[r] = rv[fv[f][0]][r] + s * (rv[fv[f][1]][r] - rv[fv[f][0]][r]) +
                  t * (rv[fv[f][2]][r] - rv[fv[f][0]][r]);
+        for (int r = 0; r < 3; ++r) Xo[f][q][r] = X[r];
         const double mono[10] = {1.0,         X[0],        X[1],        X[2],        X[0] * X[0],
                                  X[1] * X[1], X[2] * X[2], X[0] * X[1], X[0] * X[2], X[1] * X[2]};
         for (int a = 0; a < ND; ++a) {
@@ -305,6 +315,142 @@ __global__ void reconstruct_kernel(int64_t nt, const int4* __restrict__ cells,
     for (int k = 0; k < 6; ++k) out[k] = e[k];
 }
 
+// ---- near-to-far-field transform (surface equivalence) ----
+// per exterior facet (one thread), per quadrature point: the physical point,
+// the weight (rule weight x twice the facet area), the equivalent electric
+// current J = n x H with H = j curl E / (k0 Z0) and the magnetic current
+// M = -n x E: 16 doubles per point (x3, w, J re/im x3, M re/im x3)
+template <int ND, typename T>
+__global__ void ntff_points_kernel(int64_t nfac, const int32_t* __restrict__ facets,
+                                   const int4* __restrict__ cells, const double* __restrict__ xyz,
+                                   const int32_t* __restrict__ cell_dofs, const T* __restrict__ x,
+                                   double inv_k0z0, double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nfac) return;
+  const int c = facets[2 * i], f = facets[2 * i + 1];
+  const int4 v = cells[c];
+  double J[3][3], Ji[3][3], x0[3];
+  jac(xyz, v, J, x0);
+  inv3(J, Ji);
+  const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                     J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                     J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  const int vid[4] = {v.x, v.y, v.z, v.w};
+  double P[3][3];
+  for (int k = 0; k < 3; ++k)
+    for (int r = 0; r < 3; ++r) P[k][r] = xyz[3 * (int64_t)vid[c_face_vert[f][k]] + r];
+  double cr[3] = {(P[1][1] - P[0][1]) * (P[2][2] - P[0][2]) - (P[1][2] - P[0][2]) * (P[2][1] - P[0][1]),
+                  (P[1][2] - P[0][2]) * (P[2][0] - P[0][0]) - (P[1][0] - P[0][0]) * (P[2][2] - P[0][2]),
+                  (P[1][0] - P[0][0]) * (P[2][1] - P[0][1]) - (P[1][1] - P[0][1]) * (P[2][0] - P[0][0])};
+  double o = 0;
+  for (int r = 0; r < 3; ++r) o += cr[r] * (P[0][r] - xyz[3 * (int64_t)vid[f] + r]);
+  const double sg = o < 0 ? -1.0 : 1.0;
+  const double area2 = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+  double n[3];
+  for (int r = 0; r < 3; ++r) n[r] = sg * cr[r] / area2;
+  double2 xe[ND];
+  for (int a = 0; a < ND; ++a) xe[a] = ld_c(x, cell_dofs[(int64_t)c * ND + a]);
+  for (int q = 0; q < kFaceQ; ++q) {
+    double eh[2][3] = {{0, 0, 0}, {0, 0, 0}}, ch[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    for (int a = 0; a < ND; ++a) {
+      const double* t = ND == 6 ? c_fq1[f][q][a % 6] : c_fq2[f][q][a];
+      for (int r = 0; r < 3; ++r) {
+        eh[0][r] += xe[a].x * t[r];
+        eh[1][r] += xe[a].y * t[r];
+        ch[0][r] += xe[a].x * t[3 + r];
+        ch[1][r] += xe[a].y * t[3 + r];
+      }
+    }
+    double E[2][3], H[2][3];
+    for (int i3 = 0; i3 < 3; ++i3) {
+      for (int k = 0; k < 2; ++k)
+        E[k][i3] = Ji[0][i3] * eh[k][0] + Ji[1][i3] * eh[k][1] + Ji[2][i3] * eh[k][2];
+      const double cre = (J[i3][0] * ch[0][0] + J[i3][1] * ch[0][1] + J[i3][2] * ch[0][2]) / det;
+      const double cim = (J[i3][0] * ch[1][0] + J[i3][1] * ch[1][1] + J[i3][2] * ch[1][2]) / det;
+      H[0][i3] = -cim * inv_k0z0;  // H = j curl E / (k0 Z0)
+      H[1][i3] = cre * inv_k0z0;
+    }
+    double* o16 = out + 16 * (i * kFaceQ + q);
+    for (int r = 0; r < 3; ++r)
+      o16[r] = x0[r] + J[r][0] * c_fX[f][q][0] + J[r][1] * c_fX[f][q][1] + J[r][2] * c_fX[f][q][2];
+    o16[3] = c_fw[q] * area2;
+    for (int r = 0; r < 3; ++r) {
+      const int r1 = (r + 1) % 3, r2 = (r + 2) % 3;
+      for (int k = 0; k < 2; ++k) {
+        o16[4 + 2 * r + k] = n[r1] * H[k][r2] - n[r2] * H[k][r1];       // n x H
+        o16[10 + 2 * r + k] = -(n[r1] * E[k][r2] - n[r2] * E[k][r1]);   // -n x E
+      }
+    }
+  }
+}
+
+// one block per direction (theta, phi in radians): N = sum w J e^{j k0 r.rhat},
+// L = sum w M e^{j k0 r.rhat} in a fixed order, then
+// out[12 d ..] = E_theta, E_phi, L_theta, L_phi, N_theta, N_phi (complex)
+__global__ void __launch_bounds__(256) ntff_dir_kernel(int64_t npts, const double* __restrict__ pts,
+                                                       const double* __restrict__ theta,
+                                                       const double* __restrict__ phi, double k0,
+                                                       double z0, double* __restrict__ out) {
+  __shared__ double red[12][256];
+  const int d = blockIdx.x;
+  double st, ct, sp, cp;
+  sincos(theta[d], &st, &ct);
+  sincos(phi[d], &sp, &cp);
+  const double rh[3] = {st * cp, st * sp, ct};
+  double acc[12];
+  for (int k = 0; k < 12; ++k) acc[k] = 0;
+  for (int64_t i = threadIdx.x; i < npts; i += 256) {
+    const double* p = pts + 16 * i;
+    double s, c;
+    sincos(k0 * (rh[0] * p[0] + rh[1] * p[1] + rh[2] * p[2]), &s, &c);
+    const double w = p[3];
+    for (int r = 0; r < 3; ++r) {
+      const double jr = p[4 + 2 * r], ji = p[5 + 2 * r], mr = p[10 + 2 * r], mi = p[11 + 2 * r];
+      acc[2 * r] += w * (jr * c - ji * s);
+      acc[2 * r + 1] += w * (jr * s + ji * c);
+      acc[6 + 2 * r] += w * (mr * c - mi * s);
+      acc[7 + 2 * r] += w * (mr * s + mi * c);
+    }
+  }
+  for (int k = 0; k < 12; ++k) red[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h)
+      for (int k = 0; k < 12; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double th[3] = {ct * cp, ct * sp, -st}, ph[3] = {-sp, cp, 0.0};
+    double Nt[2] = {0, 0}, Np[2] = {0, 0}, Lt[2] = {0, 0}, Lp[2] = {0, 0};
+    for (int r = 0; r < 3; ++r)
+      for (int k = 0; k < 2; ++k) {
+        Nt[k] += th[r] * red[2 * r + k][0];
+        Np[k] += ph[r] * red[2 * r + k][0];
+        Lt[k] += th[r] * red[6 + 2 * r + k][0];
+        Lp[k] += ph[r] * red[6 + 2 * r + k][0];
+      }
+    // r_fac = j k0 e^{-j k0} / (4 pi)
+    double sk, ck;
+    sincos(k0, &sk, &ck);
+    const double fr = k0 * sk / (4 * 3.141592653589793), fi = k0 * ck / (4 * 3.141592653589793);
+    const double ar = Lp[0] + z0 * Nt[0], ai = Lp[1] + z0 * Nt[1];   // E_theta = -r_fac a
+    const double br = Lt[0] - z0 * Np[0], bi = Lt[1] - z0 * Np[1];   // E_phi = r_fac b
+    double* o = out + 12 * (int64_t)d;
+    o[0] = -(fr * ar - fi * ai);
+    o[1] = -(fr * ai + fi * ar);
+    o[2] = fr * br - fi * bi;
+    o[3] = fr * bi + fi * br;
+    o[4] = Lt[0];
+    o[5] = Lt[1];
+    o[6] = Lp[0];
+    o[7] = Lp[1];
+    o[8] = Nt[0];
+    o[9] = Nt[1];
+    o[10] = Np[0];
+    o[11] = Np[1];
+  }
+}
+
 cudaError_t load_point_tables(int dev) {
   if (dev < 64 && g_tables_loaded[dev]) return cudaSuccess;
   cudaError_t e = cudaMemcpyToSymbol(c_nb1, NB1, sizeof(NB1));
@@ -315,12 +461,13 @@ cudaError_t load_point_tables(int dev) {
 
 cudaError_t load_face_tables(int dev) {
   if (dev < 64 && g_face_loaded[dev]) return cudaSuccess;
-  static double t1[4][kFaceQ][6][6], t2[4][kFaceQ][20][6], w[kFaceQ];
-  face_tables<6>(NB1, t1, w);
-  face_tables<20>(NB2, t2, w);
+  static double t1[4][kFaceQ][6][6], t2[4][kFaceQ][20][6], w[kFaceQ], X[4][kFaceQ][3];
+  face_tables<6>(NB1, t1, w, X);
+  face_tables<20>(NB2, t2, w, X);
   cudaError_t e = cudaMemcpyToSymbol(c_fq1, t1, sizeof(t1));
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_fq2, t2, sizeof(t2));
   if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_fw, w, sizeof(w));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_fX, X, sizeof(X));
   if (e == cudaSuccess && dev < 64) g_face_loaded[dev] = true;
   return e;
 }
@@ -432,4 +579,64 @@ extern "C" int sucem_surface_flux(const sucem_space* sp, int dtype, const void* 
   e = cudaGetLastError();
   count_launch(2);
   return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_surface_flux");
+}
+
+extern "C" int sucem_ntff(const sucem_space* sp, int dtype, const void* x, double k0, int ndir,
+                          const double* theta, const double* phi, double* out, void* stream) {
+  using namespace sucem;
+  DeviceSpace* d = sp ? sp->s.dev : nullptr;
+  if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  if (dtype != SUCEM_C64 && dtype != SUCEM_C128) return fail("dtype must be complex", SUCEM_ERR_ARG);
+  if (!(k0 > 0)) return fail("k0 must be positive", SUCEM_ERR_ARG);
+  if (ndir < 0) return fail("negative direction count", SUCEM_ERR_ARG);
+  if (ndir == 0) return SUCEM_OK;
+  if (!x || !theta || !phi || !out) return fail("null argument", SUCEM_ERR_ARG);
+  cudaStream_t s = (cudaStream_t)stream;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaError_t e = load_face_tables(dev);
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_ntff tables");
+  if (!d->ext_facets) {
+    // exterior facets in (cell, local face) order, and the point scratch
+    const Space& hs = sp->s;
+    std::vector<int32_t> fl;
+    for (int64_t c = 0; c < (int64_t)hs.ext_mask.size(); ++c)
+      for (int f = 0; f < 4; ++f)
+        if (hs.ext_mask[c] >> f & 1) {
+          fl.push_back((int32_t)c);
+          fl.push_back(f);
+        }
+    d->n_ext = (int64_t)fl.size() / 2;
+    if (d->n_ext == 0) return fail("the mesh has no exterior facets", SUCEM_ERR_ARG);
+    e = cudaMalloc((void**)&d->ext_facets, fl.size() * sizeof(int32_t));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(d->ext_facets, fl.data(), fl.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMalloc((void**)&d->ntff_pts, (size_t)d->n_ext * kFaceQ * 16 * sizeof(double));
+    if (e != cudaSuccess) {
+      if (d->ext_facets) cudaFree(d->ext_facets);
+      d->ext_facets = nullptr;
+      return cuda_fail(e, "sucem_ntff allocation");
+    }
+  }
+  const double z0 = 3.141592653589793 * 4e-7 * 299792458.0;
+  const double inv = 1.0 / (k0 * z0);
+  const int threads = 128;
+  const unsigned blocks = (unsigned)((d->n_ext + threads - 1) / threads);
+  if (d->nd == 6 && dtype == SUCEM_C128)
+    ntff_points_kernel<6, double2><<<blocks, threads, 0, s>>>(
+        d->n_ext, d->ext_facets, d->cells, d->xyz, d->cell_dofs, (const double2*)x, inv, d->ntff_pts);
+  else if (d->nd == 6)
+    ntff_points_kernel<6, float2><<<blocks, threads, 0, s>>>(
+        d->n_ext, d->ext_facets, d->cells, d->xyz, d->cell_dofs, (const float2*)x, inv, d->ntff_pts);
+  else if (dtype == SUCEM_C128)
+    ntff_points_kernel<20, double2><<<blocks, threads, 0, s>>>(
+        d->n_ext, d->ext_facets, d->cells, d->xyz, d->cell_dofs, (const double2*)x, inv, d->ntff_pts);
+  else
+    ntff_points_kernel<20, float2><<<blocks, threads, 0, s>>>(
+        d->n_ext, d->ext_facets, d->cells, d->xyz, d->cell_dofs, (const float2*)x, inv, d->ntff_pts);
+  ntff_dir_kernel<<<ndir, 256, 0, s>>>(d->n_ext * kFaceQ, d->ntff_pts, theta, phi, k0, z0, out);
+  e = cudaGetLastError();
+  count_launch(2);
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_ntff");
 }

@@ -15,6 +15,10 @@ written here.  Sources:
   reference's power-flux test integrates on; kept as XML text) and the
   test's expected flux (test_power_flux.py:54, SurfaceFlux, and :77,
   VariationalSurfaceFlux).
+* sucemfem/PostProcessing/tests/data/reference_surface_ntff-2-*.pickle
+  (test_ntff.py:62-92): far fields of the ntff_solution_o2 DOFs evaluated on
+  the unshifted centred cube (the test builds get_centred_cube without the
+  source translation the generator used).
 * functional_tests/data/meshes/rectangular_prism{,_facet_region}.xml: a
   DOLFIN XML mesh and facet mesh function, kept as XML text for the reader
   tests.
@@ -58,6 +62,14 @@ def main():
                         no_integration_points=100, mesh_xml=np.array(mesh_xml),
                         flux_surface=26.3586862457,
                         flux_variational=26.9015957282 - 7.85747240242e-08j)
+    d = load_pickle(os.path.join(dd, "reference_surface_ntff-2-0.149896229-0.0499654096667.pickle"))
+    ff = d["ff_result_data"]
+    np.savez_compressed(os.path.join(OUT, "surface_ntff_o2.npz"),
+                        theta_deg=np.asarray(ff["theta_deg"], dtype=np.float64),
+                        phi_deg=np.asarray(ff["phi_deg"], dtype=np.float64),
+                        E_ff=np.asarray(ff["E_ff"]),
+                        E_theta_analytical=np.asarray(ff["E_theta_analytical"]),
+                        rtol=1e-12, atol=1e-7)
     md = os.path.join(REF, "functional_tests/data/meshes")
     texts = {}
     for key, name in (("mesh_xml", "rectangular_prism.xml"),

@@ -91,3 +91,34 @@ def test_xml_reader_rejects_bad_input(tmp_path):
                '<cells size="0"/></mesh></dolfin>')
     with pytest.raises(ValueError):
         Mesh(p)
+
+
+def _ntff_case():
+    g = golden("ntff_solution_o2.npz")
+    coords, cells = fem.centred_cube(g["domain_size"], float(g["max_edge_len"]))
+    return g, coords, cells
+
+
+def test_surface_ntff_oracle_matches_reference_golden():
+    """test_ntff.py:80-92: allclose(rtol 1e-12, atol 1e-7), unshifted cube."""
+    g, coords, cells = _ntff_case()
+    f = golden("surface_ntff_o2.npz")
+    A = fem.assemble(coords, cells, 2)
+    Et, Ep = postproc.ntff(coords, cells, 2, A.topo, A.dofmap, g["x"], float(g["freq"]),
+                           f["theta_deg"], f["phi_deg"])
+    E = np.stack([Et, Ep], axis=1)
+    assert np.allclose(E, f["E_ff"], rtol=float(f["rtol"]), atol=float(f["atol"]))
+    assert np.abs(E - f["E_ff"]).max() < 1e-8
+
+
+def test_get_centred_cube_matches_oracle():
+    from sucemfem.Utilities.MeshGenerators import get_centred_cube
+    g, coords, cells = _ntff_case()
+    m = get_centred_cube(g["domain_size"], float(g["max_edge_len"]))
+    assert np.array_equal(m.cells(), cells)
+    assert np.allclose(m.coordinates(), coords, rtol=0, atol=1e-15)
+    # with the source translation (ntff_generate_dofs.py:51): the origin is
+    # the centroid of the nearest containing cell
+    m2 = get_centred_cube(g["domain_size"], float(g["max_edge_len"]), [0.0, 0.0, 0.0])
+    c = int(fem.locate_cells(coords, cells, np.zeros(3))[0][0])
+    assert np.allclose(m2.coordinates(), coords - coords[cells[c]].mean(0), atol=1e-15)

@@ -96,3 +96,46 @@ def test_reconstruct_points(order):
     assert np.all(np.isnan(got[~inside].real))
     err = np.abs(got[inside] - ref[inside]).max() / np.abs(ref[inside]).max()
     assert err < 1e-12, err
+
+
+def test_surface_ntff_reference_golden():
+    from sucemfem.PostProcessing.surface_ntff import NTFF
+    from sucemfem.space import FunctionSpace
+    from sucemfem.Utilities.MeshGenerators import get_centred_cube
+    g = golden("ntff_solution_o2.npz")
+    f = golden("surface_ntff_o2.npz")
+    m = get_centred_cube(g["domain_size"], float(g["max_edge_len"]))
+    V = FunctionSpace(m, order=2)
+    dut = NTFF(V)
+    dut.set_frequency(float(g["freq"]))
+    dut.set_dofs(g["x"])
+    E = np.array([dut.calc_pt(th, ph) for th, ph in zip(f["theta_deg"], f["phi_deg"])])
+    assert np.allclose(E, f["E_ff"], rtol=float(f["rtol"]), atol=float(f["atol"]))
+    A = fem.assemble(m.coordinates(), m.cells(), 2)
+    Et, Ep = postproc.ntff(m.coordinates(), m.cells(), 2, A.topo, A.dofmap, g["x"],
+                           float(g["freq"]), f["theta_deg"], f["phi_deg"])
+    ref = np.stack([Et, Ep], axis=1)
+    assert np.abs(E - ref).max() < 1e-12 * np.abs(ref).max()
+    Et2, Ep2 = dut.calc_pts(f["theta_deg"], f["phi_deg"])
+    assert np.array_equal(np.stack([Et2, Ep2], axis=1), E)  # fixed-order sums
+    assert len(dut._L) == len(f["theta_deg"]) and len(dut._N) == len(f["theta_deg"])
+
+
+def test_surface_ntff_order1_many_directions():
+    from sucemfem.mesh import Mesh
+    from sucemfem.PostProcessing.surface_ntff import NTFF
+    from sucemfem.space import FunctionSpace
+    coords, cells = fem.box_mesh(0.3, 0.2, 0.25, 3, 2, 3, origin=(-0.15, -0.1, -0.125))
+    V = FunctionSpace(Mesh(coords, cells), order=1)
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal(V.n) + 1j * rng.standard_normal(V.n)
+    th = rng.uniform(0, 180, 50)
+    ph = rng.uniform(0, 360, 50)
+    dut = NTFF(V)
+    dut.set_frequency(1e9)
+    dut.set_dofs(x)
+    Et, Ep = dut.calc_pts(th, ph)
+    A = fem.assemble(coords, cells, 1)
+    rt, rp = postproc.ntff(coords, cells, 1, A.topo, A.dofmap, x, 1e9, th, ph)
+    scale = max(np.abs(rt).max(), np.abs(rp).max())
+    assert np.abs(Et - rt).max() < 1e-12 * scale and np.abs(Ep - rp).max() < 1e-12 * scale
