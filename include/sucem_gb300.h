@@ -72,6 +72,8 @@ int sucem_space_sizes(const sucem_space* sp, int64_t* out);
 #define SUCEM_COPY_CELL_EDGES 8     /* int32[nt*6] cell -> edge ids (UFC local order) */
 #define SUCEM_COPY_CELL_FACES 9     /* int32[nt*4] cell -> face ids (= facet numbering) */
 #define SUCEM_COPY_DOF_XYZ 10       /* double[n*3] DOF locations (edge midpoint / face centroid) */
+#define SUCEM_COPY_BOUNDARY_DUAL 11 /* double[n_boundary_dofs*6] dual functional of each boundary
+                                       DOF: point, tangent (DOF(u) = u(point).tangent) */
 int sucem_space_copy(const sucem_space* sp, int what, void* host_dst);
 
 /* Copies the space to CUDA device `device` (idempotent). */
@@ -203,6 +205,33 @@ int sucem_surface_flux(const sucem_space* sp, int dtype, const void* x, double k
  * call): calls on one space must not overlap on the GPU. */
 int sucem_ntff(const sucem_space* sp, int dtype, const void* x, double k0, int ndir,
                const double* theta, const double* phi, double* out, void* stream);
+
+/* The EM functional of CalcEMFunctional.calc_functional
+ * (sucemfem/PostProcessing/PostProcessing.py:62-173):
+ *   I = sum over the marked cells of
+ *       int curl E . curl g / mu_r - k0^2 eps_r E . g dx   (bilinear)
+ * evaluated element by element (exact: the reference element tensors).
+ * Device arrays: E, g complex128[n]; eps_r, mu_r_inv double per cell or
+ * NULL (1); cell_mask uint8 per cell or NULL (all cells); part
+ * double[2*nt] scratch; out double[2] (fixed-order sum). */
+int sucem_em_functional(const sucem_space* sp, const double* E, const double* g, double k0,
+                        const double* eps_r, const double* mu_r_inv, const uint8_t* cell_mask,
+                        double* part, double* out, void* stream);
+
+/* Cells with an edge on the boundary (sucemfem/Geometry.py:76-90
+ * BoundaryEdgeCells), host array uint8[nt]. */
+int sucem_boundary_edge_cells(const sucem_space* sp, uint8_t* mask);
+
+/* Plane-wave testing functions interpolated onto the boundary DOFs, the
+ * SurfaceInterpolant of TransformTestingExpression
+ * (sucemfem/PostProcessing/variational_ntff.py:31-66,
+ * sucemfem/Interpolation/Interpolation.py:71-82): for wave w and boundary
+ * DOF d (dual functional point p, tangent t)
+ *   g[w*n + d] = j (t . cf_w) e^{j k0 rhat_w . p}
+ * Device arrays: rhat, cf double[npw*3]; g complex128[npw*n]; only the
+ * boundary DOFs are written (the caller zeroes the rest). */
+int sucem_plane_wave_dofs(const sucem_space* sp, int npw, const double* rhat, const double* cf,
+                          double k0, double* g, void* stream);
 
 /* ---- vectors and general CSR (device arrays) ----
  * The Krylov / refinement building blocks behind solve_sparse_system and the

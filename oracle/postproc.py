@@ -101,9 +101,10 @@ def gauss_jacobi_tri(n=3):
     return u.ravel(), (v * (1 - u)).ravel(), w.ravel()
 
 
-def ntff(coords, cells, order, topo, dm, x, frequency, theta_deg, phi_deg, rule=None):
+def ntff(coords, cells, order, topo, dm, x, frequency, theta_deg, phi_deg, rule=None,
+         full=False):
     """surface_ntff.py:120-155 NTFF.calc_pt for each direction:
-    (E_theta, E_phi) arrays."""
+    (E_theta, E_phi) arrays (full=True: also L_theta, L_phi, N_theta, N_phi)."""
     s, t, w = gauss_jacobi_tri(3) if rule is None else rule
     k0 = 2 * np.pi * frequency / fem.C0
     fc_, lf_ = topo.exterior_facets()
@@ -136,7 +137,7 @@ def ntff(coords, cells, order, topo, dm, x, frequency, theta_deg, phi_deg, rule=
         M.append(-np.cross(n[:, None], E, axis=0))
     P, W = np.concatenate(P, axis=1), np.concatenate(W)
     Jc, M = np.concatenate(Jc, axis=1), np.concatenate(M, axis=1)
-    Et, Ep = [], []
+    Et, Ep, LN = [], [], []
     for th_d, ph_d in zip(np.atleast_1d(theta_deg), np.atleast_1d(phi_deg)):
         th, ph = np.deg2rad(th_d), np.deg2rad(ph_d)
         rhat = np.array([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)])
@@ -147,4 +148,114 @@ def ntff(coords, cells, order, topo, dm, x, frequency, theta_deg, phi_deg, rule=
         rf = 1j * k0 * np.exp(-1j * k0) / (4 * np.pi)
         Et.append(-rf * (phh @ Lv + fem.Z0 * (thh @ Nv)))
         Ep.append(rf * (thh @ Lv - fem.Z0 * (phh @ Nv)))
+        LN.append([thh @ Lv, phh @ Lv, thh @ Nv, phh @ Nv])
+    if full:
+        LN = np.array(LN)
+        return np.array(Et), np.array(Ep), LN[:, 0], LN[:, 1], LN[:, 2], LN[:, 3]
+    return np.array(Et), np.array(Ep)
+
+
+# --------------------------------------------------------------------------
+# variational post-processing (CalcEMFunctional and its users)
+# --------------------------------------------------------------------------
+def boundary_edge_cells(topo):
+    """Geometry.BoundaryEdgeCells (sucemfem/Geometry.py:76-90): cells that
+    have an edge lying on the boundary (an edge of an exterior facet)."""
+    fc, lf = topo.exterior_facets()
+    bedges = set()
+    for c, f in zip(fc, lf):
+        verts = set(topo.cells[c][list(fem.FACES[f])])
+        for le in range(6):
+            if set(topo.cells[c][list(fem.EDGES[le])]) <= verts:
+                bedges.add(int(topo.cell_edges[c, le]))
+    be = np.zeros(topo.ne, dtype=bool)
+    be[list(bedges)] = True
+    return np.any(be[topo.cell_edges], axis=1)
+
+
+def calc_em_functional(coords, cells, order, dm, E, g, k0, cell_mask=None, eps_r=None,
+                       mu_r=None):
+    """CalcEMFunctional.calc_functional (PostProcessing.py:62-173):
+    int curl E . curl g / mu_r - k0^2 eps_r E . g over the marked cells
+    (bilinear, no conjugation)."""
+    nt = len(cells)
+    eps = np.ones(nt) if eps_r is None else np.asarray(eps_r, dtype=float)
+    mu = np.ones(nt) if mu_r is None else np.asarray(mu_r, dtype=float)
+    S, T = fem.element_matrices(coords, cells, order, eps, mu)
+    sel = np.arange(nt) if cell_mask is None else np.nonzero(cell_mask)[0]
+    Ec, gc = np.asarray(E)[dm[sel]], np.asarray(g)[dm[sel]]
+    A = S[sel] - k0 ** 2 * T[sel]
+    return np.einsum("ca,cab,cb->", gc, A, Ec)
+
+
+def variational_surface_flux(coords, cells, order, topo, dm, x, k0):
+    """VariationalSurfaceFlux.calc_flux (power_flux.py:62-133): the functional
+    over the boundary-edge cells with g = j conj(x_D) / (k0 Z0), x_D the DOF
+    vector restricted to the boundary DOFs (DirichletBC of E on the domain
+    boundary applied to a zero vector); the flux is its conjugate."""
+    xd = np.zeros(len(x), dtype=complex)
+    b = fem.pec_dofs(topo, order)
+    xd[b] = np.asarray(x)[b]
+    g = 1j * np.conj(xd) / k0 / fem.Z0
+    return np.conj(calc_em_functional(coords, cells, order, dm, x, g, k0,
+                                      boundary_edge_cells(topo)))
+
+
+def dof_points_tangents(coords, cells, order, dm, dofs):
+    """Physical point and tangent of each DOF's dual functional (the DOF of
+    u is u(p) . t): the reference (point, tangent) of FIAT's N1curl dual
+    basis mapped by the first cell holding the DOF (x = x0 + J X, t = J t)."""
+    ref = n1curl_exact.dof_functionals(order)
+    nd = dm.shape[1]
+    owner = np.full(int(dm.max()) + 1, -1, dtype=np.int64)
+    flat = dm.ravel()
+    first = np.unique(flat, return_index=True)
+    owner[first[0]] = first[1]
+    idx = owner[np.asarray(dofs)]
+    cell, loc = idx // nd, idx % nd
+    J, det, Jinv = fem.geometry(coords, cells[cell])
+    P = np.array([[float(v) for v in ref[l][0]] for l in loc])
+    T = np.array([[float(v) for v in ref[l][1]] for l in loc])
+    pts = coords[cells[cell, 0]] + np.einsum("cij,cj->ci", J, P)
+    tans = np.einsum("cij,cj->ci", J, T)
+    return pts, tans
+
+
+def surface_interpolant(coords, cells, order, topo, dm, n, f):
+    """SurfaceInterpolant.calculate_interpolation
+    (sucemfem/Interpolation/Interpolation.py:26-82): the expression's DOFs
+    (dual functionals) on the boundary DOFs, zero elsewhere.  f maps points
+    (m, 3) to complex vectors (m, 3)."""
+    b = fem.pec_dofs(topo, order)
+    pts, tans = dof_points_tangents(coords, cells, order, dm, b)
+    g = np.zeros(n, dtype=complex)
+    g[b] = np.sum(tans * f(pts), axis=1)
+    return g
+
+
+def variational_ntff(coords, cells, order, topo, dm, x, frequency, theta_deg, phi_deg):
+    """variational_ntff.py:68-131 NTFF.calc_pt: the H-field part by the
+    functional over the boundary-edge cells with the plane-wave testing
+    function g = interp(j/k0 rhat x (ahat x rhat) e^{j k0 rhat.r}), the
+    E-field part L from the surface forms."""
+    k0 = 2 * np.pi * frequency / fem.C0
+    mask = boundary_edge_cells(topo)
+    n = len(x)
+    _, _, Lt, Lp, _, _ = ntff(coords, cells, order, topo, dm, x, frequency, theta_deg, phi_deg,
+                              full=True)
+    Et, Ep = [], []
+    for i, (th_d, ph_d) in enumerate(zip(np.atleast_1d(theta_deg), np.atleast_1d(phi_deg))):
+        th, ph = np.deg2rad(th_d), np.deg2rad(ph_d)
+        rhat = np.array([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)])
+        thh = np.array([np.cos(th) * np.cos(ph), np.cos(th) * np.sin(ph), -np.sin(th)])
+        phh = np.array([-np.sin(ph), np.cos(ph), 0.0])
+        EH = []
+        for ahat in (thh, phh):
+            cf = np.cross(rhat, np.cross(ahat, rhat)) / k0
+            g = surface_interpolant(coords, cells, order, topo, dm, n,
+                                    lambda p: 1j * cf[None] * np.exp(1j * k0 * (p @ rhat))[:, None])
+            EH.append(calc_em_functional(coords, cells, order, dm, x, g, k0, mask))
+        rf = 1j * k0 * np.exp(-1j * k0) / (4 * np.pi)
+        Et.append(rf * (-Lp[i] + EH[0]))
+        Ep.append(rf * (Lt[i] + EH[1]))
     return np.array(Et), np.array(Ep)

@@ -16,6 +16,7 @@
 #include "handle.h"
 
 namespace sucem {
+void boundary_dual(const Space& hs, std::vector<double>& pt);
 thread_local std::string g_last_error;
 static std::atomic<long long> g_launches{0};
 void count_launch(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
@@ -59,7 +60,7 @@ void free_device_space(DeviceSpace* d) {
                   d->ent_ptr, d->inc_cell, d->inc_rec,  d->indptr,        d->indices,
                   d->cell_dofs, d->boundary_dofs, d->kc_f, d->km_f, d->kt_f,
                   d->kc_d,    d->km_d,    d->kt_d, d->bidx, d->g_f, d->g_d, d->h_f, d->h_d,
-                  d->kab_f, d->kab_d, d->ext_facets, d->ntff_pts};
+                  d->kab_f, d->kab_d, d->ext_facets, d->ntff_pts, d->bdof_pt};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   cudaSetDevice(prev);
@@ -231,6 +232,11 @@ int sucem_space_copy(const sucem_space* sp, int what, void* dst) {
     case SUCEM_COPY_CELL_EDGES: return cp(s.cell_edges.data(), s.cell_edges.size() * 4);
     case SUCEM_COPY_CELL_FACES: return cp(s.cell_faces.data(), s.cell_faces.size() * 4);
     case SUCEM_COPY_DOF_XYZ: return cp(s.dof_xyz.data(), s.dof_xyz.size() * 8);
+    case SUCEM_COPY_BOUNDARY_DUAL: {
+      std::vector<double> pt;
+      sucem::boundary_dual(s, pt);
+      return cp(pt.data(), pt.size() * 8);
+    }
     default: return fail("unknown copy selector", SUCEM_ERR_ARG);
   }
 }

@@ -32,6 +32,9 @@ struct DeviceSpace {
   int32_t* ext_facets = nullptr;  // n_ext*2
   int64_t n_ext = 0;
   double* ntff_pts = nullptr;     // n_ext*9 points x 16 doubles
+  // dual functional (physical point, tangent) of every boundary DOF, for
+  // interpolating expressions onto the boundary (allocated on first use)
+  double* bdof_pt = nullptr;      // n_boundary*6
   int64_t nb = 0;                 // number of cells with exterior facets
   // per-cell coefficient scratch of the assembly (allocated on first use)
   float* g_f = nullptr;           // nt*12

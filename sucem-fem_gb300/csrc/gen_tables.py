@@ -28,6 +28,9 @@ off-diagonal weights symmetrised (K_pq + K_qp):
                          components are exact, so off-face DOFs give exact 0).
 * ``NB<o>[n][3][10]``    monomial coefficients of N_a,p in
                          1,x,y,z,x^2,y^2,z^2,xy,xz,yz (point sources)
+* ``DUAL<o>[n][6]``      the dual functional of local DOF a: reference
+                         point (0..2) and tangent (3..5), DOF(u) = u(p).t
+                         (interpolation of expressions onto the space)
 """
 from fractions import Fraction as F
 from math import factorial
@@ -273,6 +276,8 @@ def main(path):
         lines.append("static const double KM%d[6][%d][%d] = %s;" % (order, n, n, _fmt(KM, 0)))
         lines.append("static const double KT%d[4][3][%d][%d] = %s;" % (order, n, n, _fmt(KT, 0)))
         lines.append("static const double NB%d[%d][3][10] = %s;" % (order, n, _fmt(NB, 0)))
+        DU = [[F(x) for x in p] + [F(x) for x in t] for p, t in dofs(order)]
+        lines.append("static const double DUAL%d[%d][6] = %s;" % (order, n, _fmt(DU, 0)))
         lines.append("")
     with open(path, "w") as f:
         f.write("\n".join(lines))

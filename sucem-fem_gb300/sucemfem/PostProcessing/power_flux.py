@@ -57,3 +57,46 @@ class SurfaceFlux:
              ptr(self.mur) if self.mur is not None else None, ptr(part), ptr(out),
              _device.stream_ptr())
         return float(out.item())
+
+
+class VariationalSurfaceFlux:
+    """Power flux by the variational functional (power_flux.py:62-133): the
+    EM functional over the cells with an edge on the boundary, with the
+    testing function g = j conj(x_D) / (k0 Z0), x_D the DOF vector kept on
+    the boundary DOFs only; the flux is its conjugate."""
+
+    def __init__(self, function_space):
+        from .PostProcessing import CalcEMFunctional, boundary_edge_cells
+        self.function_space = V = function_space
+        self.functional = CalcEMFunctional(V)
+        self.functional.set_cell_mask(boundary_edge_cells(V))
+        self.k0_dirty = True
+
+    def set_dofs(self, dofs):
+        import torch
+        V = self.function_space
+        x = device_dofs(dofs).to(torch.complex128)
+        b = torch.as_tensor(V.boundary_dofs.astype(np.int64), device=x.device)
+        xd = torch.zeros_like(x)
+        xd[b] = x[b]
+        self.dirich_dofs = xd
+        self.functional.set_E_dofs(x)
+        self.k0_dirty = True
+
+    def set_k0(self, k0):
+        self.k0 = float(k0)
+        self.functional.set_k0(k0)
+        self.k0_dirty = True
+
+    def set_epsr_function(self, epsr_function):
+        self.functional.set_epsr_function(epsr_function)
+
+    def set_mur_function(self, mur_function):
+        self.functional.set_mur_function(mur_function)
+
+    def calc_flux(self):
+        from ..Consts import Z0
+        if self.k0_dirty:
+            self.functional.set_g_dofs(1j * self.dirich_dofs.conj() / self.k0 / Z0)
+            self.k0_dirty = False
+        return self.functional.calc_functional().conjugate()

@@ -13,7 +13,7 @@ SUCEM_OK = 0
 ERR_ARG, ERR_MEMORY, ERR_CUDA, ERR_STATE, ERR_NOCONV, ERR_BREAKDOWN = -1, -2, -3, -4, -5, -6
 
 COPY = dict(indptr=0, indices=1, cell_dofs=2, boundary_dofs=3, edges=4, faces=5, cells=6, ext_mask=7,
-            cell_edges=8, cell_faces=9, dof_xyz=10)
+            cell_edges=8, cell_faces=9, dof_xyz=10, boundary_dual=11)
 DEV = dict(indptr=0, indices=1, cell_dofs=2, boundary_dofs=3)
 
 _lib = None

@@ -19,6 +19,8 @@ written here.  Sources:
   (test_ntff.py:62-92): far fields of the ntff_solution_o2 DOFs evaluated on
   the unshifted centred cube (the test builds get_centred_cube without the
   source translation the generator used).
+* reference_variational_ntff-2-*.pickle (test_ntff.py:95-100): the same
+  directions by the variational transform.
 * functional_tests/data/meshes/rectangular_prism{,_facet_region}.xml: a
   DOLFIN XML mesh and facet mesh function, kept as XML text for the reader
   tests.
@@ -70,6 +72,12 @@ def main():
                         E_ff=np.asarray(ff["E_ff"]),
                         E_theta_analytical=np.asarray(ff["E_theta_analytical"]),
                         rtol=1e-12, atol=1e-7)
+    d = load_pickle(os.path.join(dd, "reference_variational_ntff-2-0.149896229-0.0499654096667.pickle"))
+    ff = d["ff_result_data"]
+    np.savez_compressed(os.path.join(OUT, "variational_ntff_o2.npz"),
+                        theta_deg=np.asarray(ff["theta_deg"], dtype=np.float64),
+                        phi_deg=np.asarray(ff["phi_deg"], dtype=np.float64),
+                        E_ff=np.asarray(ff["E_ff"]), rtol=1e-12, atol=1e-7)
     md = os.path.join(REF, "functional_tests/data/meshes")
     texts = {}
     for key, name in (("mesh_xml", "rectangular_prism.xml"),

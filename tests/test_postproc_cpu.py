@@ -6,6 +6,7 @@ import os
 import xml.etree.ElementTree as ET
 
 import numpy as np
+import pytest
 
 from conftest import golden
 from oracle import fem, postproc
@@ -122,3 +123,65 @@ def test_get_centred_cube_matches_oracle():
     m2 = get_centred_cube(g["domain_size"], float(g["max_edge_len"]), [0.0, 0.0, 0.0])
     c = int(fem.locate_cells(coords, cells, np.zeros(3))[0][0])
     assert np.allclose(m2.coordinates(), coords - coords[cells[c]].mean(0), atol=1e-15)
+
+
+def test_variational_surface_flux_oracle_matches_reference_golden():
+    """test_power_flux.py:77: assertAlmostEqual(calc_flux(), 26.9015957282-7.857e-08j)."""
+    g = golden("power_flux_solution_o2.npz")
+    coords, cells = _parse(str(g["mesh_xml"]))
+    A = fem.assemble(coords, cells, 2)
+    k0 = 2 * np.pi * float(g["freq"]) / fem.C0
+    v = postproc.variational_surface_flux(coords, cells, 2, A.topo, A.dofmap, g["x"], k0)
+    assert abs(v - complex(g["flux_variational"])) < 5e-8, v
+
+
+def test_variational_ntff_oracle_matches_reference_golden():
+    g, coords, cells = _ntff_case()
+    f = golden("variational_ntff_o2.npz")
+    A = fem.assemble(coords, cells, 2)
+    Et, Ep = postproc.variational_ntff(coords, cells, 2, A.topo, A.dofmap, g["x"],
+                                       float(g["freq"]), f["theta_deg"], f["phi_deg"])
+    E = np.stack([Et, Ep], axis=1)
+    assert np.allclose(E, f["E_ff"], rtol=float(f["rtol"]), atol=float(f["atol"]))
+    assert np.abs(E - f["E_ff"]).max() < 1e-8
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_boundary_dual_and_edge_cells_match_oracle(order):
+    """Host-side tables of the product (no GPU): boundary DOF dual
+    functionals and the boundary-edge cells against the oracle."""
+    from sucemfem.mesh import Mesh
+    from sucemfem.space import FunctionSpace
+    from sucemfem.Interpolation.Interpolation import boundary_dual
+    from sucemfem.PostProcessing.PostProcessing import boundary_edge_cells
+    coords, cells = fem.box_mesh(1.0, 0.5, 0.75, 3, 2, 3)
+    coords = fem.jitter_interior(coords, cells, 0.25, 0.2, seed=5)
+    V = FunctionSpace(Mesh(coords, cells), order=order)
+    A = fem.assemble(coords, cells, order)
+    b, p, t = boundary_dual(V)
+    assert np.array_equal(b, fem.pec_dofs(A.topo, order))
+    rp, rt = postproc.dof_points_tangents(coords, cells, order, A.dofmap, b)
+    assert np.allclose(p, rp, atol=1e-14) and np.allclose(t, rt, atol=1e-14)
+    assert np.array_equal(boundary_edge_cells(V).astype(bool), postproc.boundary_edge_cells(A.topo))
+
+
+def test_surface_interpolant_host_matches_oracle():
+    from sucemfem.mesh import Mesh
+    from sucemfem.space import FunctionSpace
+    from sucemfem.Interpolation import SurfaceInterpolant
+    from sucemfem.PostProcessing.variational_ntff import TransformTestingExpression
+    coords, cells = fem.box_mesh(0.3, 0.2, 0.25, 3, 2, 3, origin=(-0.15, -0.1, -0.125))
+    V = FunctionSpace(Mesh(coords, cells), order=2)
+    A = fem.assemble(coords, cells, 2)
+    rhat = np.array([0.3, -0.5, 0.8]) / np.linalg.norm([0.3, -0.5, 0.8])
+    ahat = np.array([0.0, 0.8, 0.5])
+    k0 = 21.0
+    t = TransformTestingExpression()
+    t.set_parms(rhat, ahat, k0)
+    si = SurfaceInterpolant(V)
+    si.set_interpolant_expression(*t.get_expression())
+    got = si.calculate_interpolation()
+    cf = np.cross(rhat, np.cross(ahat, rhat)) / k0
+    ref = postproc.surface_interpolant(coords, cells, 2, A.topo, A.dofmap, V.n,
+                                       lambda p: 1j * cf[None] * np.exp(1j * k0 * (p @ rhat))[:, None])
+    assert np.abs(got - ref).max() < 1e-13 * np.abs(ref).max()

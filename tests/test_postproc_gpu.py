@@ -139,3 +139,86 @@ def test_surface_ntff_order1_many_directions():
     rt, rp = postproc.ntff(coords, cells, 1, A.topo, A.dofmap, x, 1e9, th, ph)
     scale = max(np.abs(rt).max(), np.abs(rp).max())
     assert np.abs(Et - rt).max() < 1e-12 * scale and np.abs(Ep - rp).max() < 1e-12 * scale
+
+
+def test_variational_surface_flux_reference_golden(tmp_path):
+    from sucemfem.PostProcessing.power_flux import VariationalSurfaceFlux
+    g = golden("power_flux_solution_o2.npz")
+    m, V = _xml_space(tmp_path, g["mesh_xml"], 2)
+    k0 = 2 * np.pi * float(g["freq"]) / fem.C0
+    dut = VariationalSurfaceFlux(V)
+    dut.set_k0(k0)
+    dut.set_dofs(g["x"])
+    v = dut.calc_flux()
+    assert abs(v - complex(g["flux_variational"])) < 5e-8, v
+    A = fem.assemble(m.coordinates(), m.cells(), 2)
+    ref = postproc.variational_surface_flux(m.coordinates(), m.cells(), 2, A.topo, A.dofmap,
+                                            g["x"], k0)
+    assert abs(v - ref) < 1e-12 * abs(ref)
+
+
+def test_variational_ntff_reference_golden():
+    from sucemfem.PostProcessing.variational_ntff import NTFF
+    from sucemfem.space import FunctionSpace
+    from sucemfem.Utilities.MeshGenerators import get_centred_cube
+    g = golden("ntff_solution_o2.npz")
+    f = golden("variational_ntff_o2.npz")
+    m = get_centred_cube(g["domain_size"], float(g["max_edge_len"]))
+    V = FunctionSpace(m, order=2)
+    dut = NTFF(V)
+    dut.set_frequency(float(g["freq"]))
+    dut.set_dofs(g["x"])
+    E = np.array([dut.calc_pt(th, ph) for th, ph in zip(f["theta_deg"], f["phi_deg"])])
+    assert np.allclose(E, f["E_ff"], rtol=float(f["rtol"]), atol=float(f["atol"]))
+    A = fem.assemble(m.coordinates(), m.cells(), 2)
+    Et, Ep = postproc.variational_ntff(m.coordinates(), m.cells(), 2, A.topo, A.dofmap, g["x"],
+                                       float(g["freq"]), f["theta_deg"], f["phi_deg"])
+    ref = np.stack([Et, Ep], axis=1)
+    assert np.abs(E - ref).max() < 1e-11 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_em_functional_materials_and_domains(order):
+    from sucemfem.mesh import Mesh
+    from sucemfem.space import FunctionSpace
+    from sucemfem.PostProcessing import CalcEMFunctional
+    coords, cells = fem.box_mesh(1.0, 0.5, 0.75, 3, 2, 3)
+    coords = fem.jitter_interior(coords, cells, 0.25, 0.2, seed=6)
+    V = FunctionSpace(Mesh(coords, cells), order=order)
+    A = fem.assemble(coords, cells, order)
+    rng = np.random.default_rng(7)
+    E = rng.standard_normal(V.n) + 1j * rng.standard_normal(V.n)
+    gv = rng.standard_normal(V.n) + 1j * rng.standard_normal(V.n)
+    eps = rng.uniform(1, 4, V.nt)
+    mu = rng.uniform(1, 2, V.nt)
+    dom = rng.integers(0, 3, V.nt)
+    f = CalcEMFunctional(V)
+    f.set_k0(5.5)
+    f.set_E_dofs(E)
+    f.set_g_dofs(gv)
+    f.set_epsr_function(eps)
+    f.set_mur_function(mu)
+    f.set_cell_domains(dom, 2)
+    got = f.calc_functional()
+    ref = postproc.calc_em_functional(coords, cells, order, A.dofmap, E, gv, 5.5, dom == 2, eps, mu)
+    assert abs(got - ref) < 1e-12 * abs(ref)
+
+
+def test_plane_wave_dofs_match_host_interpolant():
+    from sucemfem.mesh import Mesh
+    from sucemfem.space import FunctionSpace
+    from sucemfem.Interpolation import SurfaceInterpolant
+    from sucemfem.PostProcessing.variational_ntff import NTFF, TransformTestingExpression
+    coords, cells = fem.box_mesh(0.3, 0.2, 0.25, 3, 2, 3, origin=(-0.15, -0.1, -0.125))
+    V = FunctionSpace(Mesh(coords, cells), order=2)
+    rhat = np.array([0.3, -0.5, 0.8]) / np.linalg.norm([0.3, -0.5, 0.8])
+    ahat = np.array([0.0, 0.8, 0.5])
+    dut = NTFF(V)
+    dut.set_k0(21.0)
+    g = dut._testing_dofs(rhat[None], ahat[None])[0].cpu().numpy()
+    t = TransformTestingExpression()
+    t.set_parms(rhat, ahat, 21.0)
+    si = SurfaceInterpolant(V)
+    si.set_interpolant_expression(*t.get_expression())
+    ref = si.calculate_interpolation()
+    assert np.abs(g - ref).max() < 1e-13 * np.abs(ref).max()
