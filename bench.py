@@ -552,6 +552,93 @@ def run_precision(args):
     print(json.dumps(out))
 
 
+def run_postproc(args):
+    """Post-processing case on the --cubes^3 order --order box (default 20^3
+    order 2): a seeded random complex field, then, device-timed with CUDA
+    events after a warm-up, the surface power flux, the surface NTFF over
+    360 directions in one launch pair, the variational NTFF over 36
+    directions, the variational flux, the field at 100,000 points and the
+    EM functional; beside them the FP64 oracle on a bounded sample (the
+    same calls on the 6^3 box), timed on the host."""
+    import torch
+    from sucemfem import _device
+    from sucemfem.PostProcessing import CalcEMFunctional, Reconstruct
+    from sucemfem.PostProcessing.power_flux import SurfaceFlux, VariationalSurfaceFlux
+    from sucemfem.PostProcessing.surface_ntff import NTFF
+    from sucemfem.PostProcessing.variational_ntff import NTFF as VNTFF
+    from sucemfem.space import FunctionSpace
+    dev = _device.device()
+    stream = torch.cuda.current_stream(dev)
+    mesh, eps, k0 = workload(args.cubes)
+    V = FunctionSpace(mesh, order=args.order)
+    rng = np.random.default_rng(0)
+    x = torch.as_tensor(rng.standard_normal(V.n) + 1j * rng.standard_normal(V.n), device=dev)
+    freq = k0 * C0 / (2 * np.pi)
+    th360 = np.linspace(0.5, 179.5, 360)
+    ph360 = np.linspace(0.0, 359.0, 360)
+    pts = rng.uniform(0.01, 0.99, (100000, 3))
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    sf = SurfaceFlux(V)
+    sf.set_k0(k0)
+    sf.set_dofs(x)
+    vf = VariationalSurfaceFlux(V)
+    vf.set_k0(k0)
+    vf.set_dofs(x)
+    nt = NTFF(V)
+    nt.set_frequency(freq)
+    nt.set_dofs(x)
+    vn = VNTFF(V)
+    vn.set_frequency(freq)
+    vn.set_dofs(x)
+    rc = Reconstruct(V)
+    rc.set_dof_values(x)
+    fu = CalcEMFunctional(V)
+    fu.set_k0(k0)
+    fu.set_E_dofs(x)
+    fu.set_g_dofs(x)
+    out = {"case": "postproc", "cubes": args.cubes, "order": args.order, "n_dofs": V.n,
+           "tets": V.nt, "exterior_facets": V.n_ext_facets,
+           "data": "synthetic (seeded random complex field)"}
+    ms = timed(sf.calc_flux)
+    out["surface_flux"] = {"ms": ms, "facets_per_s": V.n_ext_facets / (ms * 1e-3)}
+    ms = timed(lambda: nt.calc_pts(th360, ph360))
+    out["surface_ntff_360_directions"] = {"ms": ms, "directions_per_s": 360 / (ms * 1e-3)}
+    ms = timed(lambda: vn.calc_pts(th360[::10], ph360[::10]), reps=1)
+    out["variational_ntff_36_directions"] = {"ms": ms, "directions_per_s": 36 / (ms * 1e-3)}
+    ms = timed(vf.calc_flux)
+    out["variational_flux"] = {"ms": ms}
+    ms = timed(lambda: rc.reconstruct_points(pts))
+    out["reconstruct_100k_points"] = {"ms": ms, "points_per_s": 1e5 / (ms * 1e-3)}
+    ms = timed(fu.calc_functional)
+    out["em_functional"] = {"ms": ms, "tets_per_s": V.nt / (ms * 1e-3)}
+    if not args.no_cpu_baseline:
+        from oracle import fem as ofem, postproc as opp
+        cm, _, _ = workload(6)
+        A = ofem.assemble(cm.coordinates(), cm.cells(), args.order)
+        xs = rng.standard_normal(A.n) + 1j * rng.standard_normal(A.n)
+        t0 = time.perf_counter()
+        opp.surface_flux(cm.coordinates(), cm.cells(), args.order, A.topo, A.dofmap, xs, k0)
+        t1 = time.perf_counter()
+        opp.ntff(cm.coordinates(), cm.cells(), args.order, A.topo, A.dofmap, xs, freq,
+                 th360[:36], ph360[:36])
+        t2 = time.perf_counter()
+        out["cpu_baseline"] = {"kind": "port", "cores": 1,
+                               "sample": "FP64 oracle on the 6^3 box (%d tets)" % len(cm.cells()),
+                               "surface_flux_s": t1 - t0, "surface_ntff_36_directions_s": t2 - t1}
+    print(json.dumps(out))
+
+
 def run_eigen_batch(args):
     """Batched cavities: 256 PEC boxes, sides U[0.3,1.5] m, divisions U{4..24}
     per axis, order 1, eps_r U[1,4] per cell; one space, one assembly launch,
@@ -628,7 +715,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", default="solve",
                     choices=["solve", "factor", "lu-solve", "assemble", "serve", "precision",
-                             "eigen-batch"],
+                             "eigen-batch", "postproc"],
                     help="profiling cases: factor / assemble at --cubes, --order; serve; precision")
     ap.add_argument("--precision-solve-cubes", type=int, default=30)
     ap.add_argument("--cavities", type=int, default=256)
@@ -658,6 +745,8 @@ def main():
         run_precision(args)
     elif args.only == "eigen-batch":
         run_eigen_batch(args)
+    elif args.only == "postproc":
+        run_postproc(args)
     elif args.only != "solve":
         run_kernel_case(args)
     else:

@@ -60,7 +60,8 @@ void free_device_space(DeviceSpace* d) {
                   d->ent_ptr, d->inc_cell, d->inc_rec,  d->indptr,        d->indices,
                   d->cell_dofs, d->boundary_dofs, d->kc_f, d->km_f, d->kt_f,
                   d->kc_d,    d->km_d,    d->kt_d, d->bidx, d->g_f, d->g_d, d->h_f, d->h_d,
-                  d->kab_f, d->kab_d, d->ext_facets, d->ntff_pts, d->bdof_pt};
+                  d->kab_f, d->kab_d, d->ext_facets, d->ntff_pts, d->bdof_pt,
+                  d->bin_ptr, d->bin_cells};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   cudaSetDevice(prev);

@@ -35,6 +35,11 @@ struct DeviceSpace {
   // dual functional (physical point, tangent) of every boundary DOF, for
   // interpolating expressions onto the boundary (allocated on first use)
   double* bdof_pt = nullptr;      // n_boundary*6
+  // point location: uniform grid of cell bounding boxes (built on first use)
+  int32_t* bin_ptr = nullptr;     // nbins+1
+  int32_t* bin_cells = nullptr;   // cells overlapping each bin
+  int grid_n[3] = {0, 0, 0};
+  double grid_lo[3] = {0, 0, 0}, grid_inv[3] = {0, 0, 0};
   int64_t nb = 0;                 // number of cells with exterior facets
   // per-cell coefficient scratch of the assembly (allocated on first use)
   float* g_f = nullptr;           // nt*12

@@ -13,7 +13,9 @@
 // reference takes whichever cell its CGAL search returns first.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cstdint>
 #include <vector>
 
@@ -56,25 +58,46 @@ __device__ void inv3(const double J[3][3], double Ji[3][3]) {
   Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
 }
 
-// one thread per cell, loop over points; lowest containing cell wins
-__global__ void locate_kernel(int64_t nt, const int4* __restrict__ cells,
+// one thread per point: the cells of the point's grid bin are tested
+// (barycentric coordinates >= -1e-12); the lowest containing cell wins,
+// 0x7f7f7f7f when none contains it
+struct Grid {
+  const int32_t* ptr;
+  const int32_t* cells;
+  int n[3];
+  double lo[3], inv[3];
+};
+
+__global__ void locate_kernel(Grid g, const int4* __restrict__ cells,
                               const double* __restrict__ xyz, const double* __restrict__ pts,
                               int npts, int* __restrict__ cell_out) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nt) return;
-  const int4 v = cells[c];
-  double J[3][3], Ji[3][3], x0[3];
-  jac(xyz, v, J, x0);
-  inv3(J, Ji);
-  for (int p = 0; p < npts; ++p) {
-    const double d0 = pts[3 * p] - x0[0], d1 = pts[3 * p + 1] - x0[1], d2 = pts[3 * p + 2] - x0[2];
-    const double l1 = Ji[0][0] * d0 + Ji[0][1] * d1 + Ji[0][2] * d2;
-    const double l2 = Ji[1][0] * d0 + Ji[1][1] * d1 + Ji[1][2] * d2;
-    const double l3 = Ji[2][0] * d0 + Ji[2][1] * d1 + Ji[2][2] * d2;
-    const double l0 = 1.0 - l1 - l2 - l3;
-    const double tol = -1e-12;
-    if (l0 >= tol && l1 >= tol && l2 >= tol && l3 >= tol) atomicMin(&cell_out[p], (int)c);
+  const int p = (int)((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  if (p >= npts) return;
+  const double P[3] = {pts[3 * p], pts[3 * p + 1], pts[3 * p + 2]};
+  int b[3];
+  for (int r = 0; r < 3; ++r) {
+    const double f = (P[r] - g.lo[r]) * g.inv[r];
+    b[r] = f < 0 ? -1 : (f >= g.n[r] ? g.n[r] : (int)f);
   }
+  int best = 0x7f7f7f7f;
+  if (b[0] >= 0 && b[0] < g.n[0] && b[1] >= 0 && b[1] < g.n[1] && b[2] >= 0 && b[2] < g.n[2]) {
+    const int64_t bin = ((int64_t)b[2] * g.n[1] + b[1]) * g.n[0] + b[0];
+    for (int32_t k = g.ptr[bin]; k < g.ptr[bin + 1]; ++k) {
+      const int c = g.cells[k];
+      if (c >= best) continue;
+      double J[3][3], Ji[3][3], x0[3];
+      jac(xyz, cells[c], J, x0);
+      inv3(J, Ji);
+      const double d0 = P[0] - x0[0], d1 = P[1] - x0[1], d2 = P[2] - x0[2];
+      const double l1 = Ji[0][0] * d0 + Ji[0][1] * d1 + Ji[0][2] * d2;
+      const double l2 = Ji[1][0] * d0 + Ji[1][1] * d1 + Ji[1][2] * d2;
+      const double l3 = Ji[2][0] * d0 + Ji[2][1] * d1 + Ji[2][2] * d2;
+      const double l0 = 1.0 - l1 - l2 - l3;
+      const double tol = -1e-12;
+      if (l0 >= tol && l1 >= tol && l2 >= tol && l3 >= tol) best = c;
+    }
+  }
+  cell_out[p] = best;
 }
 
 // one warp per point, lane = local basis function
@@ -451,6 +474,100 @@ __global__ void __launch_bounds__(256) ntff_dir_kernel(int64_t npts, const doubl
   }
 }
 
+// the location grid of a space: about two cells per bin, every cell listed
+// in each bin its (slightly padded) bounding box overlaps
+cudaError_t build_grid(const Space& hs, DeviceSpace* d) {
+  if (d->bin_ptr) return cudaSuccess;
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int64_t v = 0; v < hs.nv; ++v)
+    for (int r = 0; r < 3; ++r) {
+      lo[r] = std::min(lo[r], hs.coords[3 * v + r]);
+      hi[r] = std::max(hi[r], hs.coords[3 * v + r]);
+    }
+  double ext[3], vol = 1.0;
+  for (int r = 0; r < 3; ++r) {
+    ext[r] = std::max(hi[r] - lo[r], 1e-300);
+    const double pad = 1e-9 * ext[r] + 1e-300;
+    lo[r] -= pad;
+    hi[r] += pad;
+    ext[r] = hi[r] - lo[r];
+    vol *= ext[r];
+  }
+  const double target = std::max(1.0, (double)hs.nt / 2.0);
+  const double h = std::cbrt(vol / target);
+  int n[3];
+  for (int r = 0; r < 3; ++r) n[r] = std::max(1, std::min(1024, (int)std::ceil(ext[r] / h)));
+  const int64_t nbins = (int64_t)n[0] * n[1] * n[2];
+  std::vector<int32_t> cnt(nbins + 1, 0);
+  auto range = [&](int64_t c, int b0[3], int b1[3]) {
+    double cl[3] = {1e300, 1e300, 1e300}, ch[3] = {-1e300, -1e300, -1e300};
+    for (int k = 0; k < 4; ++k)
+      for (int r = 0; r < 3; ++r) {
+        const double x = hs.coords[3 * (int64_t)hs.cells[4 * c + k] + r];
+        cl[r] = std::min(cl[r], x);
+        ch[r] = std::max(ch[r], x);
+      }
+    for (int r = 0; r < 3; ++r) {
+      const double pad = 1e-9 * ext[r];
+      b0[r] = std::max(0, std::min(n[r] - 1, (int)((cl[r] - pad - lo[r]) / ext[r] * n[r])));
+      b1[r] = std::max(0, std::min(n[r] - 1, (int)((ch[r] + pad - lo[r]) / ext[r] * n[r])));
+    }
+  };
+  for (int pass = 0; pass < 2; ++pass) {
+    std::vector<int32_t> fill;
+    if (pass == 1) {
+      for (int64_t i = 0; i < nbins; ++i) cnt[i + 1] += cnt[i];
+      fill.assign(cnt.begin(), cnt.end() - 1);
+    }
+    std::vector<int32_t> out(pass == 1 ? cnt[nbins] : 0);
+    for (int64_t c = 0; c < hs.nt; ++c) {
+      int b0[3], b1[3];
+      range(c, b0, b1);
+      for (int z = b0[2]; z <= b1[2]; ++z)
+        for (int y = b0[1]; y <= b1[1]; ++y)
+          for (int x = b0[0]; x <= b1[0]; ++x) {
+            const int64_t bin = ((int64_t)z * n[1] + y) * n[0] + x;
+            if (pass == 0)
+              cnt[bin + 1]++;
+            else
+              out[fill[bin]++] = (int32_t)c;
+          }
+    }
+    if (pass == 1) {
+      cudaError_t e = cudaMalloc((void**)&d->bin_ptr, cnt.size() * sizeof(int32_t));
+      if (e == cudaSuccess)
+        e = cudaMemcpy(d->bin_ptr, cnt.data(), cnt.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+      if (e == cudaSuccess) e = cudaMalloc((void**)&d->bin_cells, std::max<size_t>(1, out.size()) * sizeof(int32_t));
+      if (e == cudaSuccess && !out.empty())
+        e = cudaMemcpy(d->bin_cells, out.data(), out.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) {
+        if (d->bin_ptr) cudaFree(d->bin_ptr);
+        if (d->bin_cells) cudaFree(d->bin_cells);
+        d->bin_ptr = d->bin_cells = nullptr;
+        return e;
+      }
+    }
+  }
+  for (int r = 0; r < 3; ++r) {
+    d->grid_n[r] = n[r];
+    d->grid_lo[r] = lo[r];
+    d->grid_inv[r] = n[r] / ext[r];
+  }
+  return cudaSuccess;
+}
+
+Grid grid_of(const DeviceSpace* d) {
+  Grid g;
+  g.ptr = d->bin_ptr;
+  g.cells = d->bin_cells;
+  for (int r = 0; r < 3; ++r) {
+    g.n[r] = d->grid_n[r];
+    g.lo[r] = d->grid_lo[r];
+    g.inv[r] = d->grid_inv[r];
+  }
+  return g;
+}
+
 cudaError_t load_point_tables(int dev) {
   if (dev < 64 && g_tables_loaded[dev]) return cudaSuccess;
   cudaError_t e = cudaMemcpyToSymbol(c_nb1, NB1, sizeof(NB1));
@@ -489,12 +606,12 @@ extern "C" int sucem_point_sources(const sucem_space* sp, const double* pts,
   cudaGetDevice(&dev);
   cudaError_t e = load_point_tables(dev);
   if (e != cudaSuccess) return cuda_fail(e, "sucem_point_sources tables");
-  e = cudaMemsetAsync(cells_out, 0x7f, sizeof(int32_t) * npts, s);
-  if (e != cudaSuccess) return cuda_fail(e, "sucem_point_sources memset");
+  e = build_grid(sp->s, const_cast<DeviceSpace*>(d));
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_point_sources grid");
   // 0x7f7f7f7f (>= nt for any supported mesh) marks a point outside the mesh
   const int threads = 256;
-  locate_kernel<<<(unsigned)((d->nt + threads - 1) / threads), threads, 0, s>>>(
-      d->nt, d->cells, d->xyz, pts, npts, cells_out);
+  locate_kernel<<<(unsigned)((npts + threads - 1) / threads), threads, 0, s>>>(
+      grid_of(d), d->cells, d->xyz, pts, npts, cells_out);
   const unsigned eb = (unsigned)(((int64_t)npts * 32 + threads - 1) / threads);
   if (d->nd == 6)
     evaluate_kernel<6><<<eb, threads, 0, s>>>(d->nt, d->cells, d->xyz, pts, values, npts, cells_out,
@@ -522,11 +639,11 @@ extern "C" int sucem_reconstruct_points(const sucem_space* sp, int dtype, const 
   cudaGetDevice(&dev);
   cudaError_t e = load_point_tables(dev);
   if (e != cudaSuccess) return cuda_fail(e, "sucem_reconstruct_points tables");
-  e = cudaMemsetAsync(cells_out, 0x7f, sizeof(int32_t) * npts, s);
-  if (e != cudaSuccess) return cuda_fail(e, "sucem_reconstruct_points memset");
+  e = build_grid(sp->s, const_cast<DeviceSpace*>(d));
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_reconstruct_points grid");
   const int threads = 256;
-  locate_kernel<<<(unsigned)((d->nt + threads - 1) / threads), threads, 0, s>>>(
-      d->nt, d->cells, d->xyz, pts, npts, cells_out);
+  locate_kernel<<<(unsigned)((npts + threads - 1) / threads), threads, 0, s>>>(
+      grid_of(d), d->cells, d->xyz, pts, npts, cells_out);
   const unsigned eb = (unsigned)(((int64_t)npts * 32 + threads - 1) / threads);
   if (d->nd == 6 && dtype == SUCEM_C128)
     reconstruct_kernel<6, double2><<<eb, threads, 0, s>>>(d->nt, d->cells, d->xyz, d->cell_dofs,
