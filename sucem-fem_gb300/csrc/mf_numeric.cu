@@ -844,9 +844,9 @@ __global__ void permute_out_kernel(int64_t n, const int64_t* __restrict__ perm,
 // one tensor-core trailing update: the fronts of a level whose super-panel
 // ends with the panel at p0
 struct TcLaunch {
-  int p0 = 0, count = 0, tpd = 0;   // tpd: tiles per side of the largest block
+  int p0 = 0, ntiles = 0;
   double flops = 0;                 // algorithmic flops (8 per complex MAC)
-  int32_t* d_list = nullptr;        // node ids
+  int32_t* d_tiles = nullptr;       // per tile: node id, ti << 16 | tj
 };
 
 struct MFLevel {
@@ -879,6 +879,7 @@ struct MFDevice {
   cudaGraphExec_t solve_exec = nullptr;
   int solve_n = 0;                  // kernel launches in the solve graph
   int tc_sp = 0;                    // super-panel width of the tensor-core path (complex64)
+  int sm_count = 1;                 // multiprocessors of the device
   std::vector<MFLevel> levels;
   bool factored = false;
   int perturbed = 0;
@@ -920,7 +921,7 @@ void free_dev(MFDevice& d) {
   for (auto& L : d.levels) {
     if (L.d_nodes) cudaFree(L.d_nodes);
     for (auto& t : L.tcl)
-      if (t.d_list) cudaFree(t.d_list);
+      if (t.d_tiles) cudaFree(t.d_tiles);
     for (int s = 0; s < 2; ++s)
       if (L.d_kids[s]) cudaFree(L.d_kids[s]);
   }
@@ -983,6 +984,7 @@ constexpr int kTcPanel = 64;  // panel width of the complex64 factorisation
 
 cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s) {
   d.tc_sp = kTcSuperPanel;
+  cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, d.device);
   if (const char* v = getenv("SUCEM_LU_SUPERPANEL")) {
     const int w = atoi(v);
     if (w >= kTcPanel && w % kTcPanel == 0) d.tc_sp = w;
@@ -1006,19 +1008,21 @@ cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s) {
       size_t b = a;
       TcLaunch t;
       t.p0 = ends[a].first;
-      std::vector<int32_t> ids;
-      int max_mn = 0;
+      std::vector<int32_t> tl;  // the tiles of every front, front by front
       for (; b < ends.size() && ends[b].first == t.p0; ++b) {
         const MFNode& nd = s.nodes[ends[b].second];
         const int64_t sp0 = (t.p0 / sp) * (int64_t)sp;
         const int64_t bnd = std::min<int64_t>(nd.k, sp0 + sp);
-        ids.push_back(ends[b].second);
-        max_mn = std::max<int>(max_mn, (int)(nd.f - bnd));
+        const int tpd = (int)((nd.f - bnd + tc::BM - 1) / tc::BM);
+        for (int ti = 0; ti < tpd; ++ti)
+          for (int tj = 0; tj < tpd; ++tj) {
+            tl.push_back(ends[b].second);
+            tl.push_back((ti << 16) | tj);
+          }
         t.flops += 8.0 * (double)(nd.f - bnd) * (double)(nd.f - bnd) * (double)(bnd - sp0);
       }
-      t.count = (int)ids.size();
-      t.tpd = (max_mn + tc::BM - 1) / tc::BM;
-      cudaError_t e = upv(&t.d_list, ids);
+      t.ntiles = (int)(tl.size() / 2);
+      cudaError_t e = upv(&t.d_tiles, tl);
       if (e != cudaSuccess) return e;
       L.tcl.push_back(t);
       a = b;
@@ -1195,11 +1199,12 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
         // the tensor cores, one launch over exactly those fronts
         while (next_tc < L.tcl.size() && L.tcl[next_tc].p0 == p0) {
           const TcLaunch& t = L.tcl[next_tc++];
-          dim3 g4(t.tpd * t.tpd, t.count);
+          // persistent: one CTA per SM (at most one per tile)
+          const int grid = std::max(1, std::min(t.ntiles, d.sm_count));
           e = tc_event(d, d.tc_n, 0, st);
           if (e != cudaSuccess) return e;
-          tc_update_kernel<<<g4, tc::THREADS, tc::SMEM_BYTES, st>>>(
-              t.d_list, t.count, d.d_nodes, reinterpret_cast<float2*>(arena), p0, spw, NBT,
+          tc_update_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, st>>>(
+              t.d_tiles, t.ntiles, d.d_nodes, reinterpret_cast<float2*>(arena), p0, spw,
               d.d_flag + 1);
           e = tc_event(d, d.tc_n, 1, st);
           if (e != cudaSuccess) return e;

@@ -4,37 +4,55 @@
 //
 // Complex64 fronts are factorised in super-panels; when the super-panel
 // [sp0, bnd) of a front is finished (its last 64-column panel factorised),
-// the trailing block takes, over one 128 x 128 tile per CTA,
+// the trailing block takes
 //   F[bnd:f, bnd:f] -= F[bnd:f, sp0:bnd] * F[sp0:bnd, bnd:f]
-// (the last super-panel's trailing block is the Schur complement).
+// (the last super-panel's trailing block is the Schur complement).  One
+// launch covers the 128 x 128 output tiles of every front whose super-panel
+// ends with the same panel (a tile list planned on the host).
 //
 // Arithmetic: complex FP32 operands are split into TF32 pairs x = hi + lo
-// (hi = x rounded to TF32, lo = x - hi), and every real product is formed as
-// hi*hi + hi*lo + lo*hi (the 3xTF32 scheme, ~2^-21 relative), so one complex
-// K-step is 12 tcgen05.mma.kind::tf32 instructions (M = 128, N = 128, K = 8)
-// accumulating Re and Im in two FP32 TMEM blocks; the -Im*Im terms use the
-// instruction's A-negation bit.
+// (hi = x rounded to TF32, lo = x - hi rounded to TF32), and every real
+// product is formed as hi*hi + hi*lo + lo*hi (the 3xTF32 scheme, ~2^-21
+// relative), so one complex K-step is 12 tcgen05.mma.kind::tf32
+// instructions (M = 128, N = 128, K = 8) accumulating Re and Im in two FP32
+// TMEM blocks; the -Im*Im terms use the instruction's A-negation bit.
 //
-// Pipeline: K is consumed in chunks of 16; all 256 threads load a chunk
-// (A: 128 rows x 16, B: 16 x 128 columns; two chunks ahead, through two
-// register buffers), split it and store eight K-major
-// operand planes (Re/Im x hi/lo for A and B) in the canonical no-swizzle
-// core-matrix layout (8 rows x 16 bytes per core matrix, 128 bytes apart
-// along K, 512 bytes apart along M/N) into one of three stages; one thread
-// issues the chunk's 24 MMAs and commits them to the stage's mbarrier, which
-// gates the stage's reuse three chunks later.  Every wait is bounded: on a
-// timeout the kernel raises *err and skips the write-back.
+// Structure: a persistent, warp-specialised kernel, one CTA per SM walking
+// the tile list round-robin.
+//   warps 4-11 (producers): load a K-chunk of 16 (A: 128 rows, B: 128
+//     columns; half a row and half a column per thread, two chunks ahead
+//     through two register buffers), split it and store eight K-major
+//     operand planes (Re/Im x hi/lo of A and B)
+//     in the canonical no-swizzle core-matrix layout (8 rows x 16 bytes per
+//     core matrix, 128 bytes apart along K, 512 bytes apart along M/N) into
+//     one of three stages, then arrive on the stage's "full" barrier;
+//   warp 12, one thread (MMA issuer): per chunk, waits for "full", issues
+//     the 24 MMAs into the tile's TMEM accumulator and commits them to the
+//     stage's "empty" barrier (the producers' permission to refill it);
+//     after a tile's last chunk it commits to the accumulator's "acc_full"
+//     barrier;
+//   warps 0-3 (epilogue): wait for "acc_full", read their 32 TMEM lanes
+//     (tile rows) of both accumulators 16 columns at a time, turn them
+//     through shared memory so that a warp's accesses to C cover two rows of
+//     16 consecutive columns, apply C -= D and arrive on "acc_empty".
+// Two accumulators (all 512 TMEM columns) let the epilogue of one tile run
+// under the main loop of the next.  Every wait is bounded: on a timeout the
+// kernel raises *err, every role stops, and all meet at the final barrier.
 namespace tc {
 
 constexpr int BM = 128;                        // tile rows (TMEM lanes)
 constexpr int BN = 128;                        // tile columns (complex)
 constexpr int KC = 16;                         // K per chunk
 constexpr int STAGES = 3;
-constexpr int THREADS = 256;
+constexpr int THREADS = 416;                   // 4 epilogue + 8 producer warps + 1 MMA warp
+constexpr int PRODUCERS = 256;
+constexpr int MMA_WARP = 12;
 constexpr int PLANE = BM * KC * 4;             // bytes of one operand plane (BN == BM)
 constexpr int STAGE_BYTES = 8 * PLANE;         // A: Re hi/lo, Im hi/lo; then B likewise
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 256;
-constexpr int TMEM_COLS = 2 * BN;              // Re then Im accumulators
+constexpr int EPI_BYTES = 4 * 32 * 17 * 8;     // per epilogue warp: 32 rows x 16 (+1) complex
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EPI_BYTES + 512;
+constexpr int ACC_COLS = 2 * BN;               // Re then Im accumulators of one tile
+constexpr int TMEM_COLS = 2 * ACC_COLS;        // two tiles in flight
 constexpr int kWaitLimit = 1 << 24;            // polls of one mbarrier before giving up
 static_assert(BN == BM, "planes share one size");
 
@@ -42,7 +60,8 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// byte offset of element (r, k) in a K-major no-swizzle plane of KC columns
+// byte offset of row r, K-group kgroup (4 consecutive K) in a K-major
+// no-swizzle plane of KC columns
 __device__ __forceinline__ int core_off(int r, int kgroup) {
   return ((r >> 3) * (KC / 4) + kgroup) * 128 + (r & 7) * 16;
 }
@@ -68,7 +87,18 @@ __device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t
       "l"(a), "l"(b), "r"(id), "r"(acc));
 }
 
-__device__ __forceinline__ bool wait_parity(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ void commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar));
+}
+
+__device__ __forceinline__ void arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar));
+}
+
+// bounded wait for the phase with the given parity; with backoff, a failed
+// poll sleeps briefly (for waiters that are not on the critical path)
+__device__ __forceinline__ bool wait_parity(uint32_t bar, uint32_t parity, bool backoff = false) {
   uint32_t done = 0;
   for (int it = 0; it < kWaitLimit; ++it) {
     asm volatile(
@@ -77,6 +107,7 @@ __device__ __forceinline__ bool wait_parity(uint32_t bar, uint32_t parity) {
         : "=r"(done)
         : "r"(bar), "r"(parity));
     if (done) return true;
+    if (backoff) __nanosleep(256);
   }
   return false;
 }
@@ -114,66 +145,56 @@ struct Tile {
   int row0, nrow, col0, ncol, kk0, K;
 };
 
-// tile `bx` of the trailing block [bnd, f)^2 with K = bnd - sp0 of the
-// super-panel [sp0, bnd) of width sp that ends with the panel at p0 (false:
-// the front's super-panel does not end there, or no such tile)
-__device__ __forceinline__ bool tile_of(const DNode& nd, int p0, int sp, int nbt, int bx,
-                                        Tile& t) {
-  if (p0 >= nd.k) return false;
+// tile (ti, tj) of the trailing block [bnd, f)^2 with K = bnd - sp0 of the
+// super-panel [sp0, bnd) of width sp that ends with the panel at p0
+__device__ __forceinline__ Tile tile_of(const DNode& nd, int p0, int sp, int ti, int tj) {
   const int sp0 = (p0 / sp) * sp;
   const int bnd = min(nd.k, sp0 + sp);
-  if (p0 + min(nbt, nd.k - p0) != bnd) return false;
+  Tile t;
   t.kk0 = sp0;
-  t.K = bnd - sp0;
-  const int mn = nd.f - bnd;
-  if (mn <= 0 || t.K <= 0) return false;
-  const int tpd = (mn + BM - 1) / BM;
-  if (bx >= tpd * tpd) return false;
-  t.row0 = bnd + (bx / tpd) * BM;
-  t.col0 = bnd + (bx % tpd) * BN;
-  t.nrow = min(BM, nd.f - t.row0);
-  t.ncol = min(BN, nd.f - t.col0);
-  return true;
+  t.K = max(0, bnd - sp0);
+  t.row0 = bnd + ti * BM;
+  t.col0 = bnd + tj * BN;
+  t.nrow = max(0, min(BM, nd.f - t.row0));
+  t.ncol = max(0, min(BN, nd.f - t.col0));
+  return t;
 }
 
 }  // namespace tc
 
-// the trailing update of every listed front, one 128 x 128 output tile per
-// block (blockIdx.x: tile, blockIdx.y: front)
+// the listed tiles (tiles[2i] = node id, tiles[2i+1] = ti << 16 | tj), each
+// CTA taking tiles blockIdx.x, blockIdx.x + gridDim.x, ...
 __global__ void __launch_bounds__(tc::THREADS, 1)
-    tc_update_kernel(const int32_t* __restrict__ list, int count, const DNode* __restrict__ nodes,
-                     float2* __restrict__ arena, int p0, int sp, int nbt, int* __restrict__ err) {
+    tc_update_kernel(const int32_t* __restrict__ tiles, int ntiles,
+                     const DNode* __restrict__ nodes, float2* __restrict__ arena, int p0, int sp,
+                     int* __restrict__ err) {
   using namespace tc;
   extern __shared__ __align__(128) uint8_t tc_smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(tc_smem_raw) + 127) & ~(uintptr_t)127);
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + STAGES);
-
-  const int fi = blockIdx.y;
-  if (fi >= count) return;
-  const DNode nd = nodes[list[fi]];
-  Tile tl;
-  if (!tile_of(nd, p0, sp, nbt, (int)blockIdx.x, tl)) return;
-  const int kk0 = tl.kk0, K = tl.K;
-  float2* F = arena + nd.off;
+  float2* epi = reinterpret_cast<float2*>(smem + STAGES * STAGE_BYTES);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES + EPI_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* acc_full = empty + STAGES;
+  uint64_t* acc_empty = acc_full + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+  volatile int* fail = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // staging roles: A row ar (8 consecutive k from akh*8), B column bn (8
-  // consecutive k from bkh*8)
-  const int ar = tid % BM, akh = tid / BM;
-  const int bn = tid % BN, bkh = tid / BN;
-  const bool arow_ok = ar < tl.nrow, bcol_ok = bn < tl.ncol;
-  const float2* Arow = F + (int64_t)(tl.row0 + (arow_ok ? ar : 0)) * nd.f + kk0;
-  const float2* Bcol = F + (int64_t)kk0 * nd.f + tl.col0 + (bcol_ok ? bn : 0);
-
   if (tid == 0) {
-#pragma unroll
-    for (int s = 0; s < STAGES; ++s)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[s])));
+    for (int s = 0; s < STAGES; ++s) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full[s])),
+                   "r"(PRODUCERS));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[s])));
+    }
+    for (int b = 0; b < 2; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_full[b])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(smem_u32(&acc_empty[b])));
+    }
+    *fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
-  if (warp == 0) {
+  if (warp == MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
                  "r"(TMEM_COLS));
@@ -183,119 +204,187 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tmem_slot;
+  auto raise = [&]() {
+    *fail = 1;
+    atomicExch(err, 1);
+  };
 
-  const int nchunks = (K + KC - 1) / KC;
-  const float2 zero = make_float2(0.f, 0.f);
-  // two register buffers: chunk c + 2 is loaded while chunk c is stored
-  float2 av0[8], bv0[8], av1[8], bv1[8];
-  auto gload = [&](float2* av, float2* bv, int c) {
-    const int ka = c * KC + akh * 8, kb = c * KC + bkh * 8;
+  if (warp >= 4 && warp < MMA_WARP) {
+    // ---- producers: thread p stages half (K 8*h .. 8*h+7) of A row q and
+    // of B column q, q = p % 128, h = p / 128 ----
+    const int p = tid - 128, q = p % 128, h = p / 128;
+    const float2 zero = make_float2(0.f, 0.f);
+    float2 av0[8], bv0[8], av1[8], bv1[8];
+    int g = 0;  // chunk counter over all tiles of this CTA
+    bool ok = true;
+    for (int it = blockIdx.x; it < ntiles && ok; it += gridDim.x) {
+      const DNode nd = nodes[tiles[2 * it]];
+      const int tt = tiles[2 * it + 1];
+      const Tile tl = tile_of(nd, p0, sp, tt >> 16, tt & 0xffff);
+      const float2* F = arena + nd.off;
+      const bool arow = q < tl.nrow, bcol = q < tl.ncol;
+      const float2* Arow = F + (int64_t)(tl.row0 + (arow ? q : 0)) * nd.f + tl.kk0;
+      const float2* Bcol = F + (int64_t)tl.kk0 * nd.f + tl.col0 + (bcol ? q : 0);
+      const int nch = (tl.K + KC - 1) / KC;
+      auto load = [&](float2* a, float2* b, int c) {
 #pragma unroll
-    for (int j = 0; j < 8; ++j) av[j] = (arow_ok && ka + j < K) ? Arow[ka + j] : zero;
-#pragma unroll
-    for (int j = 0; j < 8; ++j)
-      bv[j] = (bcol_ok && kb + j < K) ? Bcol[(int64_t)(kb + j) * nd.f] : zero;
-  };
-  bool ok = true;
-  auto step = [&](float2* av, float2* bv, int c) {
-    const int s = c % STAGES;
-    if (c >= STAGES) ok = wait_parity(smem_u32(&mbar[s]), ((c / STAGES) - 1) & 1) && ok;
-    uint8_t* st = smem + s * STAGE_BYTES;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      store_split(st, core_off(ar, akh * 2 + h), av + 4 * h);
-      store_split(st + 4 * PLANE, core_off(bn, bkh * 2 + h), bv + 4 * h);
-    }
-    if (c + 2 < nchunks) gload(av, bv, c + 2);
-    asm volatile("fence.proxy.async.shared::cta;");
-    __syncthreads();
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t base = smem_u32(st);
-#pragma unroll
-      for (int ks = 0; ks < KC / 8; ++ks) {
-        uint64_t a[4], b[4];
-#pragma unroll
-        for (int p = 0; p < 4; ++p) {
-          a[p] = sdesc(base + p * PLANE + ks * 256);
-          b[p] = sdesc(base + (4 + p) * PLANE + ks * 256);
+        for (int j = 0; j < 8; ++j) {
+          const int k = c * KC + 8 * h + j;
+          a[j] = (arow && k < tl.K) ? Arow[k] : zero;
+          b[j] = (bcol && k < tl.K) ? Bcol[(int64_t)k * nd.f] : zero;
         }
-        const uint32_t first = (c > 0 || ks > 0) ? 1u : 0u;
-        const uint32_t pos = idesc(false), neg = idesc(true);
-        const uint32_t dre = tmem, dim = tmem + BN;
-        // Re += Are*Bre - Aim*Bim
-        mma(dre, a[0], b[0], pos, first);
-        mma(dre, a[0], b[1], pos, 1);
-        mma(dre, a[1], b[0], pos, 1);
-        mma(dre, a[2], b[2], neg, 1);
-        mma(dre, a[2], b[3], neg, 1);
-        mma(dre, a[3], b[2], neg, 1);
-        // Im += Are*Bim + Aim*Bre
-        mma(dim, a[0], b[2], pos, first);
-        mma(dim, a[0], b[3], pos, 1);
-        mma(dim, a[1], b[2], pos, 1);
-        mma(dim, a[2], b[0], pos, 1);
-        mma(dim, a[2], b[1], pos, 1);
-        mma(dim, a[3], b[0], pos, 1);
-      }
-      asm volatile(
-          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-              smem_u32(&mbar[s])));
-    }
-  };
-  gload(av0, bv0, 0);
-  if (nchunks > 1) gload(av1, bv1, 1);
-  for (int c = 0; c < nchunks; c += 2) {
-    step(av0, bv0, c);
-    if (c + 1 < nchunks) step(av1, bv1, c + 1);
-  }
-  // the last commit covers every MMA of the tile
-  const int cl = nchunks - 1;
-  ok = wait_parity(smem_u32(&mbar[cl % STAGES]), (cl / STAGES) & 1) && ok;
-  ok = __syncthreads_and(ok);  // uniform: the TMEM loads below are warp-collective
-  if (!ok && tid == 0) atomicExch(err, 1);
-  asm volatile("tcgen05.fence::after_thread_sync;");
-  if (ok) {
-    // warp w reads TMEM lanes 32 (w % 4) .. +31 (tile rows) and columns
-    // 64 (w / 4) .. +63 of both accumulators, 16 at a time
-    const int q = warp & 3, half = warp >> 2;
-    const int row = q * 32 + lane;
-    float2* Crow = F + (int64_t)(tl.row0 + (row < tl.nrow ? row : 0)) * nd.f + tl.col0;
-#pragma unroll 1
-    for (int cc = 0; cc < 4; ++cc) {
-      const int col0 = half * 64 + cc * 16;
-      uint32_t re[16], im[16];
-      const uint32_t tre = tmem + ((uint32_t)(q * 32) << 16) + col0;
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(re[0]), "=r"(re[1]), "=r"(re[2]), "=r"(re[3]), "=r"(re[4]), "=r"(re[5]),
-            "=r"(re[6]), "=r"(re[7]), "=r"(re[8]), "=r"(re[9]), "=r"(re[10]), "=r"(re[11]),
-            "=r"(re[12]), "=r"(re[13]), "=r"(re[14]), "=r"(re[15])
-          : "r"(tre));
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(im[0]), "=r"(im[1]), "=r"(im[2]), "=r"(im[3]), "=r"(im[4]), "=r"(im[5]),
-            "=r"(im[6]), "=r"(im[7]), "=r"(im[8]), "=r"(im[9]), "=r"(im[10]), "=r"(im[11]),
-            "=r"(im[12]), "=r"(im[13]), "=r"(im[14]), "=r"(im[15])
-          : "r"(tre + BN));
-      asm volatile("tcgen05.wait::ld.sync.aligned;");
-      if (row < tl.nrow) {
+      };
+      // store a chunk's half into its stage, then reuse the registers for
+      // the chunk two ahead
+      auto stage = [&](float2* a, float2* b, int c) -> bool {
+        const int s = g % STAGES;
+        if (g >= STAGES && !wait_parity(smem_u32(&empty[s]), ((g / STAGES) - 1) & 1)) return false;
+        uint8_t* st = smem + s * STAGE_BYTES;
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int col = col0 + j;
-          if (col < tl.ncol) {
-            float2 v = Crow[col];
-            v.x -= __uint_as_float(re[j]);
-            v.y -= __uint_as_float(im[j]);
-            Crow[col] = v;
+        for (int kg = 0; kg < 2; ++kg) {
+          store_split(st, core_off(q, 2 * h + kg), a + 4 * kg);
+          store_split(st + 4 * PLANE, core_off(q, 2 * h + kg), b + 4 * kg);
+        }
+        asm volatile("fence.proxy.async.shared::cta;");
+        arrive(smem_u32(&full[s]));
+        ++g;
+        if (c + 2 < nch) load(a, b, c + 2);
+        return true;
+      };
+      if (nch > 0) load(av0, bv0, 0);
+      if (nch > 1) load(av1, bv1, 1);
+      for (int c = 0; c < nch && ok; c += 2) {
+        ok = stage(av0, bv0, c);
+        if (ok && c + 1 < nch) ok = stage(av1, bv1, c + 1);
+      }
+      if (!ok) raise();
+      if (*fail) ok = false;
+    }
+  } else if (warp == MMA_WARP) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      int g = 0, i = 0;
+      bool ok = true;
+      const uint32_t pos = idesc(false), neg = idesc(true);
+      for (int it = blockIdx.x; it < ntiles && ok; it += gridDim.x, ++i) {
+        const DNode nd = nodes[tiles[2 * it]];
+        const int tt = tiles[2 * it + 1];
+        const Tile tl = tile_of(nd, p0, sp, tt >> 16, tt & 0xffff);
+        const int nch = (tl.K + KC - 1) / KC;
+        const int b = i & 1;
+        if (i >= 2 && !wait_parity(smem_u32(&acc_empty[b]), ((i / 2) - 1) & 1)) {
+          ok = false;
+          raise();
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t dre = tmem + b * ACC_COLS, dim = dre + BN;
+        for (int c = 0; c < nch; ++c, ++g) {
+          const int s = g % STAGES;
+          if (!wait_parity(smem_u32(&full[s]), (g / STAGES) & 1)) {
+            ok = false;
+            raise();
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t base = smem_u32(smem + s * STAGE_BYTES);
+#pragma unroll
+          for (int ks = 0; ks < KC / 8; ++ks) {
+            uint64_t a[4], bb[4];
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+              a[p] = sdesc(base + p * PLANE + ks * 256);
+              bb[p] = sdesc(base + (4 + p) * PLANE + ks * 256);
+            }
+            const uint32_t first = (c > 0 || ks > 0) ? 1u : 0u;
+            // Re += Are*Bre - Aim*Bim
+            mma(dre, a[0], bb[0], pos, first);
+            mma(dre, a[0], bb[1], pos, 1);
+            mma(dre, a[1], bb[0], pos, 1);
+            mma(dre, a[2], bb[2], neg, 1);
+            mma(dre, a[2], bb[3], neg, 1);
+            mma(dre, a[3], bb[2], neg, 1);
+            // Im += Are*Bim + Aim*Bre
+            mma(dim, a[0], bb[2], pos, first);
+            mma(dim, a[0], bb[3], pos, 1);
+            mma(dim, a[1], bb[2], pos, 1);
+            mma(dim, a[2], bb[0], pos, 1);
+            mma(dim, a[2], bb[1], pos, 1);
+            mma(dim, a[3], bb[0], pos, 1);
+          }
+          commit(smem_u32(&empty[s]));
+        }
+        if (!ok) break;
+        commit(smem_u32(&acc_full[b]));
+        if (*fail) ok = false;
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---- epilogue: warp w reads TMEM lanes 32w .. 32w + 31 (tile rows) ----
+    int i = 0;
+    for (int it = blockIdx.x; it < ntiles; it += gridDim.x, ++i) {
+      const DNode nd = nodes[tiles[2 * it]];
+      const int tt = tiles[2 * it + 1];
+      const Tile tl = tile_of(nd, p0, sp, tt >> 16, tt & 0xffff);
+      const int b = i & 1;
+      // uniform per warp: the TMEM loads below are warp-collective
+      const bool got =
+          __all_sync(~0u, wait_parity(smem_u32(&acc_full[b]), (i / 2) & 1, true));
+      if (!got || *fail) {
+        if (lane == 0) raise();
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t tre = tmem + b * ACC_COLS + ((uint32_t)(warp * 32) << 16);
+      float2* buf = epi + warp * 32 * 17;  // [32 rows][17]
+      float2* Cw = arena + nd.off + (int64_t)(tl.row0 + warp * 32) * nd.f + tl.col0;
+#pragma unroll 1
+      for (int cc = 0; cc < BN / 16; ++cc) {
+        uint32_t re[16], im[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(re[0]), "=r"(re[1]), "=r"(re[2]), "=r"(re[3]), "=r"(re[4]), "=r"(re[5]),
+              "=r"(re[6]), "=r"(re[7]), "=r"(re[8]), "=r"(re[9]), "=r"(re[10]), "=r"(re[11]),
+              "=r"(re[12]), "=r"(re[13]), "=r"(re[14]), "=r"(re[15])
+            : "r"(tre + cc * 16));
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(im[0]), "=r"(im[1]), "=r"(im[2]), "=r"(im[3]), "=r"(im[4]), "=r"(im[5]),
+              "=r"(im[6]), "=r"(im[7]), "=r"(im[8]), "=r"(im[9]), "=r"(im[10]), "=r"(im[11]),
+              "=r"(im[12]), "=r"(im[13]), "=r"(im[14]), "=r"(im[15])
+            : "r"(tre + BN + cc * 16));
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+        // lane = row: park the 16 values, then read them back column-major
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          buf[lane * 17 + j] = make_float2(__uint_as_float(re[j]), __uint_as_float(im[j]));
+        __syncwarp();
+        float2 cv[16];
+#pragma unroll
+        for (int t = 0; t < 16; ++t) {
+          const int r = 2 * t + (lane >> 4), col = cc * 16 + (lane & 15);
+          cv[t] = (warp * 32 + r < tl.nrow && col < tl.ncol) ? Cw[(int64_t)r * nd.f + col]
+                                                           : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int t = 0; t < 16; ++t) {
+          const int r = 2 * t + (lane >> 4), col = cc * 16 + (lane & 15);
+          if (warp * 32 + r < tl.nrow && col < tl.ncol) {
+            const float2 dv = buf[r * 17 + (lane & 15)];
+            Cw[(int64_t)r * nd.f + col] = make_float2(cv[t].x - dv.x, cv[t].y - dv.y);
           }
         }
+        __syncwarp();
       }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      arrive(smem_u32(&acc_empty[b]));
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
-  if (warp == 0)
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (warp == MMA_WARP)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(TMEM_COLS));
 }
