@@ -846,12 +846,13 @@ __global__ void permute_out_kernel(int64_t n, const int64_t* __restrict__ perm,
 struct TcLaunch {
   int p0 = 0, ntiles = 0;
   double flops = 0;                 // algorithmic flops (8 per complex MAC)
-  int32_t* d_tiles = nullptr;       // per tile: node id, ti << 16 | tj
+  int32_t* d_tiles = nullptr;       // 8 ints per tile: node, row0, col0, nrow, ncol, kk0, K, 0
 };
 
 struct MFLevel {
   std::vector<int32_t> nodes_by_k;  // node ids sorted by k descending
-  std::vector<TcLaunch> tcl;        // complex64 only, ordered by p0
+  std::vector<TcLaunch> tcl;        // complex64 only: trailing updates, ordered by p0
+  std::vector<TcLaunch> tcp;        // complex64 only: panel updates, one per panel (or none)
   std::vector<int32_t> kids[2];     // children by slot
   int max_k = 0, max_rest = 0, max_u = 0;
   int32_t* d_nodes = nullptr;
@@ -880,6 +881,7 @@ struct MFDevice {
   int solve_n = 0;                  // kernel launches in the solve graph
   int tc_sp = 0;                    // super-panel width of the tensor-core path (complex64)
   int sm_count = 1;                 // multiprocessors of the device
+  int tc_panel_k = 0;               // see kTcPanelMinK
   std::vector<MFLevel> levels;
   bool factored = false;
   int perturbed = 0;
@@ -921,6 +923,8 @@ void free_dev(MFDevice& d) {
   for (auto& L : d.levels) {
     if (L.d_nodes) cudaFree(L.d_nodes);
     for (auto& t : L.tcl)
+      if (t.d_tiles) cudaFree(t.d_tiles);
+    for (auto& t : L.tcp)
       if (t.d_tiles) cudaFree(t.d_tiles);
     for (int s = 0; s < 2; ++s)
       if (L.d_kids[s]) cudaFree(L.d_kids[s]);
@@ -976,14 +980,36 @@ constexpr int kSuperPanel = 512;
 // level; for each level, the panels p0 at which some fronts' super-panel
 // ends get one tensor-core launch over exactly those fronts (list on the
 // device).  Narrower super-panels move panel work onto the tensor cores
-// but re-read and re-write the trailing block once per super-panel; 512
-// measured best (20^3 order-2 box: 128 -> 107 ms, 256 -> 87 ms, 512 -> 82 ms
-// per factorisation).  SUCEM_LU_SUPERPANEL overrides it (a multiple of 64).
+// but re-read and re-write the trailing block once per super-panel; on the
+// 20^3 order-2 box the factorisation takes 78, 72, 73, 73, 74, 77 ms for
+// widths 192, 256, 384, 512, 768, 1024.  SUCEM_LU_SUPERPANEL overrides it (a
+// multiple of 64).
 constexpr int kTcSuperPanel = 512;
+// levels of at least two fronts whose largest pivot block has at least this
+// many columns apply the K = 64 panel updates on the tensor cores as well (a
+// single front's panel has too few tiles to fill the GPU; on the 20^3
+// order-2 box this takes the factorisation from 73 to 69 ms);
+// SUCEM_LU_TC_PANEL_K overrides the column threshold
+constexpr int kTcPanelMinK = 64;
 constexpr int kTcPanel = 64;  // panel width of the complex64 factorisation
+
+// 128 x 128 tiles of rows [r0, r1) x columns [c0, c1) of front `node`, K
+// range [kk0, kk0 + K), appended as 8-int descriptors
+void add_tiles(std::vector<int32_t>& tl, int32_t node, int64_t r0, int64_t r1, int64_t c0,
+               int64_t c1, int64_t kk0, int64_t K) {
+  if (r1 <= r0 || c1 <= c0 || K <= 0) return;
+  for (int64_t r = r0; r < r1; r += tc::BM)
+    for (int64_t c = c0; c < c1; c += tc::BN) {
+      const int32_t v[8] = {node, (int32_t)r, (int32_t)c, (int32_t)std::min<int64_t>(tc::BM, r1 - r),
+                            (int32_t)std::min<int64_t>(tc::BN, c1 - c), (int32_t)kk0, (int32_t)K, 0};
+      tl.insert(tl.end(), v, v + 8);
+    }
+}
 
 cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s) {
   d.tc_sp = kTcSuperPanel;
+  d.tc_panel_k = kTcPanelMinK;
+  if (const char* v = getenv("SUCEM_LU_TC_PANEL_K")) d.tc_panel_k = atoi(v);
   cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, d.device);
   if (const char* v = getenv("SUCEM_LU_SUPERPANEL")) {
     const int w = atoi(v);
@@ -1013,19 +1039,36 @@ cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s) {
         const MFNode& nd = s.nodes[ends[b].second];
         const int64_t sp0 = (t.p0 / sp) * (int64_t)sp;
         const int64_t bnd = std::min<int64_t>(nd.k, sp0 + sp);
-        const int tpd = (int)((nd.f - bnd + tc::BM - 1) / tc::BM);
-        for (int ti = 0; ti < tpd; ++ti)
-          for (int tj = 0; tj < tpd; ++tj) {
-            tl.push_back(ends[b].second);
-            tl.push_back((ti << 16) | tj);
-          }
+        add_tiles(tl, ends[b].second, bnd, nd.f, bnd, nd.f, sp0, bnd - sp0);
         t.flops += 8.0 * (double)(nd.f - bnd) * (double)(nd.f - bnd) * (double)(bnd - sp0);
       }
-      t.ntiles = (int)(tl.size() / 2);
+      t.ntiles = (int)(tl.size() / 8);
       cudaError_t e = upv(&t.d_tiles, tl);
       if (e != cudaSuccess) return e;
       L.tcl.push_back(t);
       a = b;
+    }
+    // panel updates on the tensor cores
+    if (L.max_k < d.tc_panel_k || L.nodes_by_k.size() < 2) continue;
+    for (int p0 = 0; p0 < L.max_k; p0 += kTcPanel) {
+      TcLaunch t;
+      t.p0 = p0;
+      std::vector<int32_t> tl;
+      for (int32_t i : L.nodes_by_k) {
+        const MFNode& nd = s.nodes[i];
+        if (nd.k <= p0) break;  // k-descending
+        const int64_t nb = std::min<int64_t>(kTcPanel, nd.k - p0), lo = p0 + nb;
+        const int64_t bnd = std::min<int64_t>(nd.k, (p0 / sp) * (int64_t)sp + sp);
+        if (bnd <= lo) continue;
+        add_tiles(tl, i, lo, nd.f, lo, bnd, p0, nb);   // rows [lo, f) x cols [lo, bnd)
+        add_tiles(tl, i, lo, bnd, bnd, nd.f, p0, nb);  // rows [lo, bnd) x cols [bnd, f)
+        t.flops += 8.0 * (double)nb *
+                   ((double)(nd.f - lo) * (bnd - lo) + (double)(bnd - lo) * (nd.f - bnd));
+      }
+      t.ntiles = (int)(tl.size() / 8);
+      cudaError_t e = upv(&t.d_tiles, tl);
+      if (e != cudaSuccess) return e;
+      L.tcp.push_back(t);
     }
   }
   return cudaSuccess;
@@ -1103,6 +1146,23 @@ cudaError_t tc_event(MFDevice& d, int i, int which, cudaStream_t st) {
   return cudaEventRecord(d.tc_ev[2 * i + which], st);
 }
 
+// one tensor-core update launch (persistent: one CTA per SM, at most one per
+// tile), with events around it for sucem_lu_kernel_stats
+template <typename S>
+cudaError_t tc_launch(MFDevice& d, const TcLaunch& t, S* arena, cudaStream_t st) {
+  const int grid = std::max(1, std::min(t.ntiles, d.sm_count));
+  cudaError_t e = tc_event(d, d.tc_n, 0, st);
+  if (e != cudaSuccess) return e;
+  tc_update_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, st>>>(
+      t.d_tiles, t.ntiles, d.d_nodes, reinterpret_cast<float2*>(arena), d.d_flag + 1);
+  e = tc_event(d, d.tc_n, 1, st);
+  if (e != cudaSuccess) return e;
+  d.tc_n++;
+  d.tc_flops += t.flops;
+  count_launch(1);
+  return cudaSuccess;
+}
+
 template <typename S>
 cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st) {
   // panel width 64 (32 for complex double, whose tiles would not fit)
@@ -1145,14 +1205,31 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
                                                                    (const S*)vals, arena);
     count_launch(1);
   }
-  // SUCEM_LU_PROFILE=1 prints the device time of every tree level (stderr)
-  const bool prof = getenv("SUCEM_LU_PROFILE") != nullptr;
-  cudaEvent_t ev[2];
+  // SUCEM_LU_PROFILE=1 prints the device time of every tree level (stderr);
+  // =2 also splits it by kernel kind (every launch then synchronises, so the
+  // split includes each launch's latency)
+  const char* prof_env = getenv("SUCEM_LU_PROFILE");
+  const bool prof = prof_env != nullptr;
+  const bool prof2 = prof && atoi(prof_env) >= 2;
+  cudaEvent_t ev[2], kev[2];
+  double kind_ms[6] = {0, 0, 0, 0, 0, 0};  // extend-add, diag, trsm, gemm, tensor core, schur
   if (prof) {
     cudaEventCreate(&ev[0]);
     cudaEventCreate(&ev[1]);
+    cudaEventCreate(&kev[0]);
+    cudaEventCreate(&kev[1]);
     cudaEventRecord(ev[0], st);
+    cudaEventRecord(kev[0], st);
   }
+  auto mark = [&](int kind) {
+    if (!prof2) return;
+    cudaEventRecord(kev[1], st);
+    cudaEventSynchronize(kev[1]);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, kev[0], kev[1]);
+    kind_ms[kind] += ms;
+    cudaEventRecord(kev[0], st);
+  };
   for (size_t lv = 0; lv < d.levels.size(); ++lv) {
     const MFLevel& L = d.levels[lv];
     for (int c = 0; c < 2; ++c) {
@@ -1161,6 +1238,7 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
       dim3 grid(std::max(16, std::min(1024, 8192 / nk)), nk);
       extend_add_kernel<S><<<grid, 256, 0, st>>>(L.d_kids[c], nk, d.d_nodes, d.d_ea, arena);
       count_launch(1);
+      mark(0);
     }
     // complex64: every level in super-panels of d.tc_sp columns, the
     // trailing blocks on the tensor cores (precomputed launch lists);
@@ -1179,6 +1257,7 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
       diag_lu_kernel<S, NBT><<<cnt, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0, amax,
                                                   tau, d.d_flag);
       count_launch(1);
+      mark(1);
       const int rest = std::max(0, L.max_rest - p0 - 1);
       const int tiles = (rest + 63) / 64;
       if (tiles > 0) {
@@ -1186,31 +1265,32 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
         panel_trsm_kernel<S, NBT><<<g1, 256, trsm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena,
                                                                p0);
         count_launch(1);
-        // K = nb panel update outside the deferred block: CUDA cores (the
-        // panel steps are latency-bound; tensor-core tiles do not pay off)
-        const int tpd = (rest + 63) / 64;
-        dim3 g2(tpd * tpd, cnt);
-        gemm_update_kernel<S, NBT><<<g2, 256, gemm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena,
-                                                                p0, spw);
-        count_launch(1);
+        mark(2);
+        // K = nb panel update outside the deferred block
+        const size_t pi = (size_t)(p0 / NBT);
+        if (tc_level && pi < L.tcp.size()) {
+          const TcLaunch& t = L.tcp[pi];
+          if (t.ntiles > 0) {
+            e = tc_launch(d, t, arena, st);
+            if (e != cudaSuccess) return e;
+          }
+          mark(4);
+        } else {
+          const int tpd = (rest + 63) / 64;
+          dim3 g2(tpd * tpd, cnt);
+          gemm_update_kernel<S, NBT><<<g2, 256, gemm_smem, st>>>(L.d_nodes, cnt, d.d_nodes,
+                                                                  arena, p0, spw);
+          count_launch(1);
+          mark(3);
+        }
       }
       if (tc_level) {
         // fronts whose super-panel ends with this panel: trailing block on
         // the tensor cores, one launch over exactly those fronts
         while (next_tc < L.tcl.size() && L.tcl[next_tc].p0 == p0) {
-          const TcLaunch& t = L.tcl[next_tc++];
-          // persistent: one CTA per SM (at most one per tile)
-          const int grid = std::max(1, std::min(t.ntiles, d.sm_count));
-          e = tc_event(d, d.tc_n, 0, st);
+          e = tc_launch(d, L.tcl[next_tc++], arena, st);
           if (e != cudaSuccess) return e;
-          tc_update_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, st>>>(
-              t.d_tiles, t.ntiles, d.d_nodes, reinterpret_cast<float2*>(arena), p0, spw,
-              d.d_flag + 1);
-          e = tc_event(d, d.tc_n, 1, st);
-          if (e != cudaSuccess) return e;
-          d.tc_n++;
-          d.tc_flops += t.flops;
-          count_launch(1);
+          mark(4);
         }
       } else if (use_blas && tiles > 0) {
         // fronts whose super-panel ends with this panel: trailing GEMM
@@ -1238,20 +1318,28 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
       schur_update_kernel<S, kSchurKC><<<g3, 256, schur_smem, st>>>(L.d_nodes, nall, d.d_nodes,
                                                                      arena);
       count_launch(1);
+      mark(5);
     }
     if (prof) {
       cudaEventRecord(ev[1], st);
       cudaEventSynchronize(ev[1]);
       float ms = 0;
       cudaEventElapsedTime(&ms, ev[0], ev[1]);
-      fprintf(stderr, "[sucem lu] level %zu fronts %zu max_k %d max_f %d  %.3f ms\n", lv,
+      fprintf(stderr, "[sucem lu] level %zu fronts %zu max_k %d max_f %d  %.3f ms", lv,
               L.nodes_by_k.size(), L.max_k, L.max_rest, ms);
+      if (prof2)
+        fprintf(stderr, "  (extend %.3f diag %.3f trsm %.3f gemm %.3f tc %.3f schur %.3f)", kind_ms[0],
+                kind_ms[1], kind_ms[2], kind_ms[3], kind_ms[4], kind_ms[5]);
+      fprintf(stderr, "\n");
+      for (double& k : kind_ms) k = 0;
       cudaEventRecord(ev[0], st);
     }
   }
   if (prof) {
     cudaEventDestroy(ev[0]);
     cudaEventDestroy(ev[1]);
+    cudaEventDestroy(kev[0]);
+    cudaEventDestroy(kev[1]);
   }
   return cudaGetLastError();
 }

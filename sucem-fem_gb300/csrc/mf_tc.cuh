@@ -6,9 +6,12 @@
 // [sp0, bnd) of a front is finished (its last 64-column panel factorised),
 // the trailing block takes
 //   F[bnd:f, bnd:f] -= F[bnd:f, sp0:bnd] * F[sp0:bnd, bnd:f]
-// (the last super-panel's trailing block is the Schur complement).  One
-// launch covers the 128 x 128 output tiles of every front whose super-panel
-// ends with the same panel (a tile list planned on the host).
+// (the last super-panel's trailing block is the Schur complement), and on
+// levels with large pivot blocks every 64-column panel p0 applies its
+// K = 64 update to the rows and columns of its super-panel outside the
+// deferred block.  A launch covers a list of 128 x 128 output tiles, each
+// given by its own descriptor (front, rows, columns, K range), planned on
+// the host.
 //
 // Arithmetic: complex FP32 operands are split into TF32 pairs x = hi + lo
 // (hi = x rounded to TF32, lo = x - hi rounded to TF32), and every real
@@ -145,28 +148,26 @@ struct Tile {
   int row0, nrow, col0, ncol, kk0, K;
 };
 
-// tile (ti, tj) of the trailing block [bnd, f)^2 with K = bnd - sp0 of the
-// super-panel [sp0, bnd) of width sp that ends with the panel at p0
-__device__ __forceinline__ Tile tile_of(const DNode& nd, int p0, int sp, int ti, int tj) {
-  const int sp0 = (p0 / sp) * sp;
-  const int bnd = min(nd.k, sp0 + sp);
+// a tile from its descriptor: 8 ints {front node, row0, col0, nrow, ncol,
+// kk0, K, unused}
+__device__ __forceinline__ Tile tile_of(const int32_t* td) {
   Tile t;
-  t.kk0 = sp0;
-  t.K = max(0, bnd - sp0);
-  t.row0 = bnd + ti * BM;
-  t.col0 = bnd + tj * BN;
-  t.nrow = max(0, min(BM, nd.f - t.row0));
-  t.ncol = max(0, min(BN, nd.f - t.col0));
+  t.row0 = td[1];
+  t.col0 = td[2];
+  t.nrow = td[3];
+  t.ncol = td[4];
+  t.kk0 = td[5];
+  t.K = td[6];
   return t;
 }
 
 }  // namespace tc
 
-// the listed tiles (tiles[2i] = node id, tiles[2i+1] = ti << 16 | tj), each
-// CTA taking tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+// the listed tiles (8-int descriptors, see tile_of), each CTA taking tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ...
 __global__ void __launch_bounds__(tc::THREADS, 1)
     tc_update_kernel(const int32_t* __restrict__ tiles, int ntiles,
-                     const DNode* __restrict__ nodes, float2* __restrict__ arena, int p0, int sp,
+                     const DNode* __restrict__ nodes, float2* __restrict__ arena,
                      int* __restrict__ err) {
   using namespace tc;
   extern __shared__ __align__(128) uint8_t tc_smem_raw[];
@@ -218,9 +219,8 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
     int g = 0;  // chunk counter over all tiles of this CTA
     bool ok = true;
     for (int it = blockIdx.x; it < ntiles && ok; it += gridDim.x) {
-      const DNode nd = nodes[tiles[2 * it]];
-      const int tt = tiles[2 * it + 1];
-      const Tile tl = tile_of(nd, p0, sp, tt >> 16, tt & 0xffff);
+      const DNode nd = nodes[tiles[8 * it]];
+      const Tile tl = tile_of(tiles + 8 * it);
       const float2* F = arena + nd.off;
       const bool arow = q < tl.nrow, bcol = q < tl.ncol;
       const float2* Arow = F + (int64_t)(tl.row0 + (arow ? q : 0)) * nd.f + tl.kk0;
@@ -267,9 +267,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
       bool ok = true;
       const uint32_t pos = idesc(false), neg = idesc(true);
       for (int it = blockIdx.x; it < ntiles && ok; it += gridDim.x, ++i) {
-        const DNode nd = nodes[tiles[2 * it]];
-        const int tt = tiles[2 * it + 1];
-        const Tile tl = tile_of(nd, p0, sp, tt >> 16, tt & 0xffff);
+        const Tile tl = tile_of(tiles + 8 * it);
         const int nch = (tl.K + KC - 1) / KC;
         const int b = i & 1;
         if (i >= 2 && !wait_parity(smem_u32(&acc_empty[b]), ((i / 2) - 1) & 1)) {
@@ -324,9 +322,8 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
     // ---- epilogue: warp w reads TMEM lanes 32w .. 32w + 31 (tile rows) ----
     int i = 0;
     for (int it = blockIdx.x; it < ntiles; it += gridDim.x, ++i) {
-      const DNode nd = nodes[tiles[2 * it]];
-      const int tt = tiles[2 * it + 1];
-      const Tile tl = tile_of(nd, p0, sp, tt >> 16, tt & 0xffff);
+      const DNode nd = nodes[tiles[8 * it]];
+      const Tile tl = tile_of(tiles + 8 * it);
       const int b = i & 1;
       // uniform per warp: the TMEM loads below are warp-collective
       const bool got =
