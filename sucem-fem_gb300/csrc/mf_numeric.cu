@@ -98,6 +98,26 @@ __device__ __forceinline__ float s_real(float, double v) { return (float)v; }
 __device__ __forceinline__ double s_real(double, double v) { return v; }
 __device__ __forceinline__ float2 s_real(float2, double v) { return make_float2((float)v, 0.f); }
 __device__ __forceinline__ double2 s_real(double2, double v) { return make_double2(v, 0.0); }
+// squared magnitude in the working precision and the reciprocal of a pivot
+// from it: 1/p = conj(p) / |p|^2, with a correctly rounded 1/|p|^2
+__device__ __forceinline__ float s_mag2s(float v) { return v * v; }
+__device__ __forceinline__ double s_mag2s(double v) { return v * v; }
+__device__ __forceinline__ float s_mag2s(float2 v) { return fmaf(v.x, v.x, v.y * v.y); }
+__device__ __forceinline__ double s_mag2s(double2 v) { return fma(v.x, v.x, v.y * v.y); }
+__device__ __forceinline__ float s_recip(float v, float) { return __frcp_rn(v); }
+__device__ __forceinline__ double s_recip(double v, double) { return 1.0 / v; }
+__device__ __forceinline__ float2 s_recip(float2 v, float m2) {
+  const float r = __frcp_rn(m2);
+  return make_float2(v.x * r, -v.y * r);
+}
+__device__ __forceinline__ double2 s_recip(double2 v, double m2) {
+  const double r = 1.0 / m2;
+  return make_double2(v.x * r, -v.y * r);
+}
+// barrier over the first `threads` threads that reach it (a multiple of 32)
+__device__ __forceinline__ void named_barrier(int id, int threads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
 __device__ __forceinline__ void s_atomic_sub(float* p, float v) { atomicAdd(p, -v); }
 __device__ __forceinline__ void s_atomic_sub(double* p, double v) { atomicAdd(p, -v); }
 __device__ __forceinline__ void s_atomic_sub(float2* p, float2 v) {
@@ -199,21 +219,27 @@ __global__ void max_abs_kernel(int64_t m, const S* __restrict__ v,
 }
 
 // LU (no pivoting, static pivot replacement) of the nb x nb diagonal block;
-// pivots below rel_tol * max|a_ij| are replaced by that value.  16 x 16
-// threads, thread (tx, ty) holding rows tx + 16a and columns ty + 16b in
-// registers (the identity beyond nb).  At step i the owner of a_ii checks
-// and inverts the pivot, the owners of column i and row i publish them
-// through shared memory (double-buffered: one barrier per step), and every
-// thread updates its own entries.
+// pivots with |p| below rel_tol * max|a_ij| are replaced by that value.
+// Rows live in registers, LPR lanes per row (column q + LPR*s in slot s of
+// lane q), warp w owning rows [w*RPW, (w+1)*RPW).  Step i: the lanes of row
+// i publish it through shared memory (permuted so each lane's columns are
+// contiguous, double-buffered) and the owner of a_ii its reciprocal; one
+// named barrier over the warps that still own rows below i; the multiplier
+// of every lower row is shuffled from the lane holding column i.  A warp
+// whose rows are all final stores them and leaves, so the barrier shrinks
+// with the remaining triangle.
 template <typename S, int NBT>
 __global__ void __launch_bounds__(256) diag_lu_kernel(const int32_t* __restrict__ list,
                                                       int count, const DNode* __restrict__ nodes,
                                                       S* __restrict__ arena, int p0,
                                                       const unsigned long long* __restrict__ amax,
                                                       double rel_tol, int* __restrict__ n_perturbed) {
-  constexpr int RB = NBT / 16;
-  __shared__ S colbuf[2][NBT];
-  __shared__ S rowbuf[2][NBT];
+  constexpr int LPR = 256 / NBT;  // lanes per row
+  constexpr int CPL = NBT / LPR;  // columns per lane
+  constexpr int RPW = 32 / LPR;   // rows per warp
+  constexpr int NW = 8;
+  using R = decltype(s_mag2s(S()));
+  __shared__ __align__(16) S rowbuf[2][LPR][CPL + 2];
   __shared__ S pinv[2];
   const int fi = blockIdx.x;
   if (fi >= count) return;
@@ -222,71 +248,61 @@ __global__ void __launch_bounds__(256) diag_lu_kernel(const int32_t* __restrict_
   if (nb <= 0) return;
   const double am = __longlong_as_double((long long)*amax);
   const double tau = rel_tol * (am > 0 ? am : 1.0);
+  const R tau2 = (R)(tau * tau);
   S* base = arena + nd.off + (int64_t)p0 * nd.f + p0;
   const S zero = s_zero(S()), one = s_one(S());
-  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  S R[RB][RB];  // R[a][b] = A[tx + 16a][ty + 16b]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = lane % LPR, grp = lane - q;
+  const int r = warp * RPW + lane / LPR;
+  S v[CPL];
 #pragma unroll
-  for (int a = 0; a < RB; ++a)
+  for (int s = 0; s < CPL; ++s) {
+    const int c = q + LPR * s;
+    v[s] = (r < nb && c < nb) ? base[(int64_t)r * nd.f + c] : (r == c ? one : zero);
+  }
+  // the column groups are unrolled (register slots stay static), the steps
+  // inside a group are not (keeps the kernel within the instruction cache)
 #pragma unroll
-    for (int b = 0; b < RB; ++b) {
-      const int r = tx + 16 * a, c = ty + 16 * b;
-      R[a][b] = (r < nb && c < nb) ? base[(int64_t)r * nd.f + c] : (r == c ? one : zero);
-    }
-  // the 16-column groups are unrolled (register indices stay static), the
-  // steps inside a group are not (a fully unrolled kernel misses the
-  // instruction cache)
-#pragma unroll
-  for (int bi = 0; bi < RB; ++bi)
+  for (int sj = 0; sj < CPL; ++sj) {
 #pragma unroll 1
-  for (int ii = 0; ii < 16; ++ii) {
-    const int i = bi * 16 + ii;
-    if (i >= nb) break;
-    const int par = i & 1;
-    if (tx == ii && ty == ii) {
-      S piv = R[bi][bi];
-      if (s_abs(piv) < tau) {
-        piv = s_real(piv, tau);
-        R[bi][bi] = piv;
-        atomicAdd(n_perturbed, 1);
+    for (int jq = 0; jq < LPR; ++jq) {
+      const int i = LPR * sj + jq;
+      if (i >= nb || i / RPW > warp) goto finished;
+      const int par = i & 1;
+      if (r == i) {
+        if (q == jq) {
+          S piv = v[sj];
+          R m2 = s_mag2s(piv);
+          if (m2 < tau2) {
+            piv = s_real(piv, tau);
+            m2 = tau2;
+            v[sj] = piv;
+            atomicAdd(n_perturbed, 1);
+          }
+          pinv[par] = s_recip(piv, m2);
+        }
+#pragma unroll
+        for (int s = sj; s < CPL; ++s) rowbuf[par][q][s] = v[s];
       }
-      pinv[par] = s_div(one, piv);
-    }
-    if (ty == ii) {
+      named_barrier(1, (NW - i / RPW) * 32);
+      const S ci = s_shfl(v[sj], grp | jq);
+      if (r > i) {
+        const S l = s_mul(ci, pinv[par]);
+        if (q == jq) v[sj] = l;
 #pragma unroll
-      for (int a = 0; a < RB; ++a) colbuf[par][tx + 16 * a] = R[a][bi];
-    }
-    if (tx == ii) {
-#pragma unroll
-      for (int b = 0; b < RB; ++b) rowbuf[par][ty + 16 * b] = R[bi][b];
-    }
-    __syncthreads();
-    const S rinv = pinv[par];
-    S u[RB];
-#pragma unroll
-    for (int b = 0; b < RB; ++b) u[b] = rowbuf[par][ty + 16 * b];
-#pragma unroll
-    for (int a = 0; a < RB; ++a) {
-      const int r = tx + 16 * a;
-      if (r <= i) continue;
-      const S l = s_mul(colbuf[par][r], rinv);
-#pragma unroll
-      for (int b = 0; b < RB; ++b) {
-        const int c = ty + 16 * b;
-        if (c > i)
-          R[a][b] = s_fms(R[a][b], l, u[b]);
-        else if (c == i)
-          R[a][b] = l;
+        for (int s = sj; s < CPL; ++s)
+          if (q + LPR * s > i) v[s] = s_fms(v[s], l, rowbuf[par][q][s]);
       }
     }
   }
+finished:
+  if (r < nb) {
 #pragma unroll
-  for (int a = 0; a < RB; ++a)
-#pragma unroll
-    for (int b = 0; b < RB; ++b) {
-      const int r = tx + 16 * a, c = ty + 16 * b;
-      if (r < nb && c < nb) base[(int64_t)r * nd.f + c] = R[a][b];
+    for (int s = 0; s < CPL; ++s) {
+      const int c = q + LPR * s;
+      if (c < nb) base[(int64_t)r * nd.f + c] = v[s];
     }
+  }
 }
 
 // panel solves by substitution: rows below the diagonal block
@@ -295,7 +311,8 @@ __global__ void __launch_bounds__(256) diag_lu_kernel(const int32_t* __restrict_
 // holds the entries q, q+4, ... in registers; at step j the owner of entry j
 // finishes it and hands it to the other three by a shuffle, so no block
 // barrier is needed inside the substitution.
-// Dynamic shared memory: D[NBT][NBT+1] (the factored block) then T[64][NBT+1].
+// Dynamic shared memory: D[NBT][NBT+1] (the factored block), T[64][NBT+1],
+// then the NBT pivot reciprocals.
 template <typename S, int NBT>
 __global__ void __launch_bounds__(256) panel_trsm_kernel(const int32_t* __restrict__ list,
                                                          int count,
@@ -356,6 +373,14 @@ __global__ void __launch_bounds__(256) panel_trsm_kernel(const int32_t* __restri
     }
   }
   __syncthreads();
+  S* rinv = reinterpret_cast<S*>(T + 64);  // reciprocals of the pivots
+  if (rows) {
+    if (threadIdx.x < NBT) {
+      const S p = D[threadIdx.x][threadIdx.x];
+      rinv[threadIdx.x] = s_recip(p, s_mag2s(p));
+    }
+    __syncthreads();
+  }
   const int r = threadIdx.x >> 2, q = threadIdx.x & 3;
   const int lane = threadIdx.x & 31, grp = lane & ~3;
   S v[CPT];
@@ -371,7 +396,7 @@ __global__ void __launch_bounds__(256) panel_trsm_kernel(const int32_t* __restri
       for (int jq = 0; jq < 4; ++jq) {
         const int j = 4 * sj + jq;
         if (j >= nb) break;
-        if (q == jq) v[sj] = s_div(v[sj], D[j][j]);
+        if (q == jq) v[sj] = s_mul(v[sj], rinv[j]);
         const S xj = s_shfl(v[sj], grp | jq);
 #pragma unroll
         for (int s = sj; s < CPT; ++s)
@@ -1168,13 +1193,20 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
   // panel width 64 (32 for complex double, whose tiles would not fit)
   constexpr int NBT = sizeof(S) <= 8 ? 64 : 32;
   static_assert(!kTensorCore<S> || NBT == kTcPanel, "tensor-core plan assumes this panel width");
-  const size_t trsm_smem = sizeof(S) * (size_t)(NBT + 64) * (NBT + 1);
+  const size_t trsm_smem = sizeof(S) * ((size_t)(NBT + 64) * (NBT + 1) + NBT);
+  // grids of at most one block per SM request this much shared memory so
+  // that no two of their (latency-bound) blocks share an SM
+  constexpr size_t kSoloSmem = 116 * 1024;
   const size_t gemm_smem = sizeof(S) * (size_t)NBT * (65 + 64);
   constexpr int kSchurKC = 32;
   const size_t schur_smem = sizeof(S) * (size_t)kSchurKC * (65 + 64);
   {
     cudaError_t ea = cudaFuncSetAttribute(panel_trsm_kernel<S, NBT>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trsm_smem);
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)std::max(trsm_smem, kSoloSmem));
+    if (ea == cudaSuccess)
+      ea = cudaFuncSetAttribute(diag_lu_kernel<S, NBT>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSoloSmem);
     if (ea == cudaSuccess)
       ea = cudaFuncSetAttribute(gemm_update_kernel<S, NBT>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem);
@@ -1254,16 +1286,17 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
       int cnt = 0;
       while (cnt < (int)L.k_sorted.size() && L.k_sorted[cnt] > p0) ++cnt;
       if (cnt == 0) break;
-      diag_lu_kernel<S, NBT><<<cnt, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0, amax,
-                                                  tau, d.d_flag);
+      diag_lu_kernel<S, NBT><<<cnt, 256, cnt <= d.sm_count ? kSoloSmem : 0, st>>>(
+          L.d_nodes, cnt, d.d_nodes, arena, p0, amax, tau, d.d_flag);
       count_launch(1);
       mark(1);
       const int rest = std::max(0, L.max_rest - p0 - 1);
       const int tiles = (rest + 63) / 64;
       if (tiles > 0) {
         dim3 g1(2 * tiles, cnt);
-        panel_trsm_kernel<S, NBT><<<g1, 256, trsm_smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena,
-                                                               p0);
+        const size_t tsm = (int64_t)g1.x * g1.y <= d.sm_count ? std::max(trsm_smem, kSoloSmem)
+                                                               : trsm_smem;
+        panel_trsm_kernel<S, NBT><<<g1, 256, tsm, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0);
         count_launch(1);
         mark(2);
         // K = nb panel update outside the deferred block
