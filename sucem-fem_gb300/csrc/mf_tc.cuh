@@ -23,8 +23,9 @@
 // Structure: a persistent, warp-specialised kernel, one CTA per SM walking
 // the tile list round-robin.
 //   warps 4-11 (producers): load a K-chunk of 16 (A: 128 rows, B: 128
-//     columns; half a row and half a column per thread, two chunks ahead
-//     through two register buffers), split it and store eight K-major
+//     columns; two quarter rows and half a column per thread, loads
+//     coalesced along the rows of the front, two chunks ahead through two
+//     register buffers), split it and store eight K-major
 //     operand planes (Re/Im x hi/lo of A and B)
 //     in the canonical no-swizzle core-matrix layout (8 rows x 16 bytes per
 //     core matrix, 128 bytes apart along K, 512 bytes apart along M/N) into
@@ -211,9 +212,12 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
   };
 
   if (warp >= 4 && warp < MMA_WARP) {
-    // ---- producers: thread p stages half (K 8*h .. 8*h+7) of A row q and
-    // of B column q, q = p % 128, h = p / 128 ----
+    // ---- producers: thread p stages K-groups akg (four consecutive K) of
+    // A rows ar and ar + 64 (four lanes cover a row's 128 bytes, so a warp's
+    // loads touch eight rows), and half h (K 8*h .. 8*h+7) of B column q
+    // (a warp's loads are 32 consecutive columns of one row) ----
     const int p = tid - 128, q = p % 128, h = p / 128;
+    const int ar = p >> 2, akg = p & 3;
     const float2 zero = make_float2(0.f, 0.f);
     float2 av0[8], bv0[8], av1[8], bv1[8];
     int g = 0;  // chunk counter over all tiles of this CTA
@@ -222,15 +226,22 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
       const DNode nd = nodes[tiles[8 * it]];
       const Tile tl = tile_of(tiles + 8 * it);
       const float2* F = arena + nd.off;
-      const bool arow = q < tl.nrow, bcol = q < tl.ncol;
-      const float2* Arow = F + (int64_t)(tl.row0 + (arow ? q : 0)) * nd.f + tl.kk0;
+      const bool arow0 = ar < tl.nrow, arow1 = ar + 64 < tl.nrow, bcol = q < tl.ncol;
+      const float2* Arow0 = F + (int64_t)(tl.row0 + (arow0 ? ar : 0)) * nd.f + tl.kk0 + 4 * akg;
+      const float2* Arow1 =
+          F + (int64_t)(tl.row0 + (arow1 ? ar + 64 : 0)) * nd.f + tl.kk0 + 4 * akg;
       const float2* Bcol = F + (int64_t)tl.kk0 * nd.f + tl.col0 + (bcol ? q : 0);
       const int nch = (tl.K + KC - 1) / KC;
       auto load = [&](float2* a, float2* b, int c) {
 #pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int k = c * KC + 4 * akg + j;
+          a[j] = (arow0 && k < tl.K) ? Arow0[c * KC + j] : zero;
+          a[4 + j] = (arow1 && k < tl.K) ? Arow1[c * KC + j] : zero;
+        }
+#pragma unroll
         for (int j = 0; j < 8; ++j) {
           const int k = c * KC + 8 * h + j;
-          a[j] = (arow && k < tl.K) ? Arow[k] : zero;
           b[j] = (bcol && k < tl.K) ? Bcol[(int64_t)k * nd.f] : zero;
         }
       };
@@ -240,11 +251,10 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
         const int s = g % STAGES;
         if (g >= STAGES && !wait_parity(smem_u32(&empty[s]), ((g / STAGES) - 1) & 1)) return false;
         uint8_t* st = smem + s * STAGE_BYTES;
+        store_split(st, core_off(ar, akg), a);
+        store_split(st, core_off(ar + 64, akg), a + 4);
 #pragma unroll
-        for (int kg = 0; kg < 2; ++kg) {
-          store_split(st, core_off(q, 2 * h + kg), a + 4 * kg);
-          store_split(st + 4 * PLANE, core_off(q, 2 * h + kg), b + 4 * kg);
-        }
+        for (int kg = 0; kg < 2; ++kg) store_split(st + 4 * PLANE, core_off(q, 2 * h + kg), b + 4 * kg);
         asm volatile("fence.proxy.async.shared::cta;");
         arrive(smem_u32(&full[s]));
         ++g;
