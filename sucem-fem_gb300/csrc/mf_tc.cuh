@@ -212,12 +212,14 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
   };
 
   if (warp >= 4 && warp < MMA_WARP) {
-    // ---- producers: thread p stages K-groups akg (four consecutive K) of
-    // A rows ar and ar + 64 (four lanes cover a row's 128 bytes, so a warp's
-    // loads touch eight rows), and half h (K 8*h .. 8*h+7) of B column q
-    // (a warp's loads are 32 consecutive columns of one row) ----
+    // ---- producers: thread p stages K-group akg (four consecutive K) of
+    // A rows ar and ar + 64 (a warp's loads cover 128 bytes of each of
+    // eight rows), and half h (K 8*h .. 8*h+7) of B column q (a warp's
+    // loads are 32 consecutive columns of one row) ----
     const int p = tid - 128, q = p % 128, h = p / 128;
-    const int ar = p >> 2, akg = p & 3;
+    // lanes 8a .. 8a+7 of a warp take K-group a of eight consecutive rows,
+    // so each quarter-warp's 16-byte stores fill 128 contiguous bytes
+    const int ar = 8 * (p >> 5) + (p & 7), akg = (p >> 3) & 3;
     const float2 zero = make_float2(0.f, 0.f);
     float2 av0[8], bv0[8], av1[8], bv1[8];
     int g = 0;  // chunk counter over all tiles of this CTA
