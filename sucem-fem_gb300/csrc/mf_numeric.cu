@@ -610,7 +610,7 @@ __global__ void __launch_bounds__(256) schur_update_kernel(const int32_t* __rest
 // independent partial sums so four loads per lane are in flight; the result
 // is complete in lane 0.  IDX: y is gathered through idx (y[idx[j]]).
 template <typename S, bool IDX>
-__device__ __forceinline__ S warp_row_dot(const S* __restrict__ row, const S* __restrict__ y,
+__device__ __forceinline__ S warp_row_dot(const S* __restrict__ row, const S* y,
                                           const int32_t* __restrict__ idx, int lo, int hi,
                                           int lane) {
   S a0 = s_zero(S()), a1 = s_zero(S()), a2 = s_zero(S()), a3 = s_zero(S());
@@ -646,21 +646,17 @@ constexpr int kTrsvThreads = 1024;      // block size of the sub-panel solves
 constexpr int kBwdChunk = 1024;         // columns per warp in the backward products
 
 // forward, sub-step j: y[c0:c1] = L[c0:c1, c0:c1]^-1 y[c0:c1] (unit lower),
-// one block per front: the strictly lower tile and y[c0:c1] are loaded into
-// shared memory, then 32 rows at a time: their products with the solved
-// rows (a warp per row), then the 32 x 32 diagonal part by one warp.
-// Dynamic shared memory: Dt[P][P+1], ys[P].
+// by one whole block for one front: the strictly lower tile and y[c0:c1] are
+// loaded into shared memory, then 32 rows at a time: their products with
+// the solved rows (a warp per row), then the 32 x 32 diagonal part by one
+// warp.  Shared memory (smem): Dt[P][P+1], ys[P].  Uniform over the block;
+// the caller separates two calls with a barrier.
 template <typename S>
-__global__ void __launch_bounds__(1024) fwd_trsv_kernel(const int32_t* __restrict__ list, int count,
-                                const DNode* __restrict__ nodes, const S* __restrict__ arena,
-                                S* __restrict__ x, int j) {
+__device__ __forceinline__ void fwd_trsv_front(const DNode& nd, const S* __restrict__ arena,
+                                               S* __restrict__ x, int j, unsigned char* smem) {
   constexpr int P = solve_panel<S>();
-  extern __shared__ __align__(16) unsigned char trsv_smem[];
-  S(*Dt)[P + 1] = reinterpret_cast<S(*)[P + 1]>(trsv_smem);
-  S* ys = reinterpret_cast<S*>(trsv_smem + sizeof(S) * P * (P + 1));
-  const int fi = blockIdx.x;
-  if (fi >= count) return;
-  const DNode nd = nodes[list[fi]];
+  S(*Dt)[P + 1] = reinterpret_cast<S(*)[P + 1]>(smem);
+  S* ys = reinterpret_cast<S*>(smem + sizeof(S) * P * (P + 1));
   const int c0 = j * P;
   if (nd.k <= c0) return;
   const int m = min(nd.k, c0 + P) - c0;
@@ -701,94 +697,63 @@ __global__ void __launch_bounds__(1024) fwd_trsv_kernel(const int32_t* __restric
   for (int t = threadIdx.x; t < m; t += kTrsvThreads) y[t] = ys[t];
 }
 
-// forward, sub-step j: rows r in [c1, f) of the front take
-// -= L[r, c0:c1] . y[c0:c1]; rows inside the pivot block update y (one
-// writer), rows of the update set go to the ancestors' x[U[r - k]]
-// (atomic, sibling fronts share ancestors); a warp per row
+// forward, sub-step j, row q of the rows [c1, f) of the front outside the
+// sub-panel (one warp): row r takes -= L[r, c0:c1] . y[c0:c1]; rows inside
+// the pivot block update y (one writer), rows of the update set go to the
+// ancestors' x[U[r - k]] (atomic, sibling fronts share ancestors)
 template <typename S>
-__global__ void fwd_gemv_kernel(const int32_t* __restrict__ list, int count,
-                                const DNode* __restrict__ nodes, const int32_t* __restrict__ U,
-                                const S* __restrict__ arena, S* __restrict__ x, int j) {
-  constexpr int P = solve_panel<S>();
-  const int fi = blockIdx.y;
-  if (fi >= count) return;
-  const DNode nd = nodes[list[fi]];
-  const int c0 = j * P;
-  if (nd.k <= c0) return;
-  const int c1 = min(nd.k, c0 + P);
-  const int rows = nd.f - c1;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+__device__ __forceinline__ void fwd_gemv_row(const DNode& nd, const int32_t* __restrict__ U,
+                                             const S* __restrict__ arena, S* __restrict__ x,
+                                             int c0, int c1, int q, int lane) {
   S* y = x + nd.start;
-  for (int q = warp; q < rows; q += nwarps) {
-    const int r = c1 + q;
-    const S* row = arena + nd.off + (int64_t)r * nd.f;
-    const S acc = warp_row_dot<S, false>(row, y, nullptr, c0, c1, lane);
-    if (lane == 0) {
-      if (r < nd.k)
-        y[r] = s_add(y[r], acc);
-      else
-        s_atomic_sub(&x[U[nd.u_off + r - nd.k]], s_fms(s_zero(S()), acc, s_real(S(), 1.0)));
-    }
+  const int r = c1 + q;
+  const S* row = arena + nd.off + (int64_t)r * nd.f;
+  const S acc = warp_row_dot<S, false>(row, y, nullptr, c0, c1, lane);
+  if (lane == 0) {
+    if (r < nd.k)
+      y[r] = s_add(y[r], acc);
+    else
+      s_atomic_sub(&x[U[nd.u_off + r - nd.k]], s_fms(s_zero(S()), acc, s_real(S(), 1.0)));
   }
 }
 
-// backward, sub-step j: rows r in [c0, c1) take -= U[r, c1:f] . x over the
-// columns outside the sub-panel (own variables y[c] for c < k, the
-// ancestors' x[U[c - k]] beyond); a warp per (row, kBwdChunk columns),
-// partial sums added atomically
+// backward, sub-step j, work item w of rows [c0, c1) x chunks of kBwdChunk
+// columns outside the sub-panel (one warp): row r takes -= U[r, c1:f] . x
+// over its chunk (own variables y[c] for c < k, the ancestors' x[U[c - k]]
+// beyond); with several chunks the partial sums are added atomically
 template <typename S>
-__global__ void bwd_gemv_kernel(const int32_t* __restrict__ list, int count,
-                                const DNode* __restrict__ nodes, const int32_t* __restrict__ U,
-                                const S* __restrict__ arena, S* __restrict__ x, int j) {
-  constexpr int P = solve_panel<S>();
-  const int fi = blockIdx.y;
-  if (fi >= count) return;
-  const DNode nd = nodes[list[fi]];
-  const int c0 = j * P;
-  if (nd.k <= c0) return;
-  const int c1 = min(nd.k, c0 + P);
-  if (c1 >= nd.f) return;
-  const int rows = c1 - c0, ncol = nd.f - c1;
-  const int nch = (ncol + kBwdChunk - 1) / kBwdChunk;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+__device__ __forceinline__ void bwd_gemv_item(const DNode& nd, const int32_t* __restrict__ U,
+                                              const S* __restrict__ arena, S* __restrict__ x,
+                                              int c0, int c1, int nch, int w, int lane) {
   S* y = x + nd.start;
-  const int32_t* Ui = U + nd.u_off;
-  for (int w = warp; w < rows * nch; w += nwarps) {
-    const int r = c0 + w % rows, ch = w / rows;
-    const int lo = c1 + ch * kBwdChunk, hi = min(nd.f, lo + kBwdChunk);
-    const S* row = arena + nd.off + (int64_t)r * nd.f;
-    S acc = s_zero(S());
-    if (lo < nd.k) acc = warp_row_dot<S, false>(row, y, nullptr, lo, min(hi, nd.k), lane);
-    if (hi > nd.k)
-      acc = s_add(acc, warp_row_dot<S, true>(row + nd.k, x, Ui, max(lo, nd.k) - nd.k,
-                                             hi - nd.k, lane));
-    if (lane == 0) {
-      if (nch == 1)
-        y[r] = s_add(y[r], acc);
-      else
-        s_atomic_sub(&y[r], s_fms(s_zero(S()), acc, s_real(S(), 1.0)));
-    }
+  const int rows = c1 - c0;
+  const int r = c0 + w % rows, ch = w / rows;
+  const int lo = c1 + ch * kBwdChunk, hi = min(nd.f, lo + kBwdChunk);
+  const S* row = arena + nd.off + (int64_t)r * nd.f;
+  S acc = s_zero(S());
+  if (lo < nd.k) acc = warp_row_dot<S, false>(row, y, nullptr, lo, min(hi, nd.k), lane);
+  if (hi > nd.k)
+    acc = s_add(acc, warp_row_dot<S, true>(row + nd.k, x, U + nd.u_off, max(lo, nd.k) - nd.k,
+                                           hi - nd.k, lane));
+  if (lane == 0) {
+    if (nch == 1)
+      y[r] = s_add(y[r], acc);
+    else
+      s_atomic_sub(&y[r], s_fms(s_zero(S()), acc, s_real(S(), 1.0)));
   }
 }
 
 // backward, sub-step j: y[c0:c1] = U[c0:c1, c0:c1]^-1 y[c0:c1] (upper,
-// non-unit), one block per front, the upper tile and y in shared memory,
-// 32 rows at a time from the bottom; the reciprocals of the diagonal are
-// formed in parallel before each 32-row chain.
-// Dynamic shared memory: Dt[P][P+1], ys[P].
+// non-unit), by one whole block for one front, the upper tile and y in
+// shared memory, 32 rows at a time from the bottom; the reciprocals of the
+// diagonal are formed in parallel before each 32-row chain.
+// Shared memory (smem): Dt[P][P+1], ys[P].
 template <typename S>
-__global__ void __launch_bounds__(1024) bwd_trsv_kernel(const int32_t* __restrict__ list, int count,
-                                const DNode* __restrict__ nodes, const S* __restrict__ arena,
-                                S* __restrict__ x, int j) {
+__device__ __forceinline__ void bwd_trsv_front(const DNode& nd, const S* __restrict__ arena,
+                                               S* __restrict__ x, int j, unsigned char* smem) {
   constexpr int P = solve_panel<S>();
-  extern __shared__ __align__(16) unsigned char trsv_smem[];
-  S(*Dt)[P + 1] = reinterpret_cast<S(*)[P + 1]>(trsv_smem);
-  S* ys = reinterpret_cast<S*>(trsv_smem + sizeof(S) * P * (P + 1));
-  const int fi = blockIdx.x;
-  if (fi >= count) return;
-  const DNode nd = nodes[list[fi]];
+  S(*Dt)[P + 1] = reinterpret_cast<S(*)[P + 1]>(smem);
+  S* ys = reinterpret_cast<S*>(smem + sizeof(S) * P * (P + 1));
   const int c0 = j * P;
   if (nd.k <= c0) return;
   const int m = min(nd.k, c0 + P) - c0;
@@ -832,6 +797,64 @@ __global__ void __launch_bounds__(1024) bwd_trsv_kernel(const int32_t* __restric
     __syncthreads();
   }
   for (int t = threadIdx.x; t < m; t += kTrsvThreads) y[t] = ys[t];
+}
+
+// one block per listed front (dynamic shared memory Dt[P][P+1], ys[P])
+template <typename S>
+__global__ void __launch_bounds__(1024) fwd_trsv_kernel(const int32_t* __restrict__ list, int count,
+                                const DNode* __restrict__ nodes, const S* __restrict__ arena,
+                                S* __restrict__ x, int j) {
+  extern __shared__ __align__(16) unsigned char trsv_smem[];
+  if ((int)blockIdx.x >= count) return;
+  fwd_trsv_front<S>(nodes[list[blockIdx.x]], arena, x, j, trsv_smem);
+}
+
+// a warp per row of the listed front blockIdx.y
+template <typename S>
+__global__ void fwd_gemv_kernel(const int32_t* __restrict__ list, int count,
+                                const DNode* __restrict__ nodes, const int32_t* __restrict__ U,
+                                const S* __restrict__ arena, S* __restrict__ x, int j) {
+  constexpr int P = solve_panel<S>();
+  const int fi = blockIdx.y;
+  if (fi >= count) return;
+  const DNode nd = nodes[list[fi]];
+  const int c0 = j * P;
+  if (nd.k <= c0) return;
+  const int c1 = min(nd.k, c0 + P);
+  const int rows = nd.f - c1;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int q = warp; q < rows; q += nwarps) fwd_gemv_row<S>(nd, U, arena, x, c0, c1, q, lane);
+}
+
+// a warp per (row, kBwdChunk columns) of the listed front blockIdx.y
+template <typename S>
+__global__ void bwd_gemv_kernel(const int32_t* __restrict__ list, int count,
+                                const DNode* __restrict__ nodes, const int32_t* __restrict__ U,
+                                const S* __restrict__ arena, S* __restrict__ x, int j) {
+  constexpr int P = solve_panel<S>();
+  const int fi = blockIdx.y;
+  if (fi >= count) return;
+  const DNode nd = nodes[list[fi]];
+  const int c0 = j * P;
+  if (nd.k <= c0) return;
+  const int c1 = min(nd.k, c0 + P);
+  if (c1 >= nd.f) return;
+  const int rows = c1 - c0, ncol = nd.f - c1;
+  const int nch = (ncol + kBwdChunk - 1) / kBwdChunk;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int w = warp; w < rows * nch; w += nwarps)
+    bwd_gemv_item<S>(nd, U, arena, x, c0, c1, nch, w, lane);
+}
+
+template <typename S>
+__global__ void __launch_bounds__(1024) bwd_trsv_kernel(const int32_t* __restrict__ list, int count,
+                                const DNode* __restrict__ nodes, const S* __restrict__ arena,
+                                S* __restrict__ x, int j) {
+  extern __shared__ __align__(16) unsigned char trsv_smem[];
+  if ((int)blockIdx.x >= count) return;
+  bwd_trsv_front<S>(nodes[list[blockIdx.x]], arena, x, j, trsv_smem);
 }
 
 template <typename S, typename T>
