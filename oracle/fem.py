@@ -11,7 +11,9 @@ What it restates, with the reference call sites it follows:
   edges and faces are numbered by first encounter while walking the cells in
   order and each cell's local entities in UFC order (DOLFIN
   TopologyComputation), order-1 DOFs are the edges, order-2 DOFs are
-  2*edge+{0,1} followed by 2*E + 2*face+{0,1} (the FFC dof map layout);
+  2*edge+{0,1} followed by 2*E + 2*face+{0,1} (the FFC dof map layout),
+  orders 3 and 4 continue that entity-major layout (k per edge, k(k-1) per
+  face, then the k(k-1)(k-2)/2 interior DOFs of every cell);
 * the element forms: mass ``eps_r*inner(v,u)*dx`` and curl-curl
   ``dot(curl(v),curl(u))/mu_r*dx`` (sucemfem/Forms.py:71-85) and the ABC
   form ``inner(cross(n,v),cross(n,u))*ds`` over every exterior facet
@@ -152,18 +154,25 @@ class Topology:
 
 
 def dofmap(topo, order):
-    if order == 1:
-        return topo.cell_edges.copy(), topo.ne
-    if order == 2:
-        e = topo.cell_edges
-        f = topo.cell_faces
-        dm = np.empty((topo.nt, 20), dtype=np.int64)
-        dm[:, 0:12:2] = 2 * e
-        dm[:, 1:12:2] = 2 * e + 1
-        dm[:, 12::2] = 2 * topo.ne + 2 * f
-        dm[:, 13::2] = 2 * topo.ne + 2 * f + 1
-        return dm, 2 * topo.ne + 2 * topo.nf
-    raise ValueError("order must be 1 or 2")
+    """Cell DOF map of degree ``order``: k DOFs per edge (k*edge + j), then
+    k(k-1) per face, then k(k-1)(k-2)/2 per cell interior, entity by entity
+    (orders 1 and 2 are the FFC layouts above; orders 3 and 4 continue the
+    same entity-major pattern, their interior DOFs being cell-local)."""
+    if order not in (1, 2, 3, 4):
+        raise ValueError("order must be 1, 2, 3 or 4")
+    k = order
+    de, df, dc = k, k * (k - 1), k * (k - 1) * (k - 2) // 2
+    face0 = de * topo.ne
+    cell0 = face0 + df * topo.nf
+    nd = 6 * de + 4 * df + dc
+    dm = np.empty((topo.nt, nd), dtype=np.int64)
+    for j in range(de):
+        dm[:, j:6 * de:de] = de * topo.cell_edges + j
+    for j in range(df):
+        dm[:, 6 * de + j:6 * de + 4 * df:df] = face0 + df * topo.cell_faces + j
+    for j in range(dc):
+        dm[:, 6 * de + 4 * df + j] = cell0 + dc * np.arange(topo.nt) + j
+    return dm, cell0 + dc * topo.nt
 
 
 def sparsity(dm, n):
@@ -292,11 +301,11 @@ def pec_dofs(topo, order):
             if set(ev[c, le]) <= verts:
                 edge_set.add(int(topo.cell_edges[c, le]))
     edges = np.array(sorted(edge_set), dtype=np.int64)
-    if order == 1:
-        return edges
-    faces = np.unique(topo.cell_faces[fc, flf])
-    return np.sort(np.concatenate([2 * edges, 2 * edges + 1,
-                                   2 * topo.ne + 2 * faces, 2 * topo.ne + 2 * faces + 1]))
+    faces = np.unique(topo.cell_faces[fc, flf]).astype(np.int64)
+    k = order
+    de, df = k, k * (k - 1)
+    parts = [de * edges + j for j in range(de)] + [de * topo.ne + df * faces + j for j in range(df)]
+    return np.sort(np.concatenate(parts))
 
 
 def apply_pec(A, dofs):

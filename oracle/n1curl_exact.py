@@ -17,12 +17,19 @@ element is restated here:
 * dual basis: tangential point evaluations u(p).t on every edge at the
   interior points of a lattice with k+1 intervals (t = v1 - v0 of the edge,
   not normalised), then for k >= 2 two tangential evaluations per face at
-  the interior lattice points (tangents v1-v0 and v2-v0 of the face);
+  the interior lattice points (tangents v1-v0 and v2-v0 of the face), then
+  for k >= 3 the three Cartesian components at every interior point of the
+  cell lattice (cell-local DOFs: any fixed order is a valid convention);
 * physical basis through the covariant Piola map N = J^-T N_hat.
 
-The basis is computed in exact rational arithmetic with sympy, the
-reference tensors by exact-degree Gauss quadrature of it; the result and is
-pinned against the reference's golden fixtures by tests/test_oracle_golden.py.
+For orders 1 and 2 the basis is computed in exact rational arithmetic with
+sympy, the reference tensors by exact-degree Gauss quadrature of it; the
+result is pinned against the reference's golden fixtures by
+tests/test_oracle_golden.py.  Orders 3 and 4 use an independent float64
+construction (``numeric_basis``); their pins are the reference's own
+higher-order functional tests (cavity eigenvalues,
+functional_tests/test_EigenProblems.py:86,150), run on this oracle in
+tests/test_high_order_cpu.py.
 """
 from functools import lru_cache
 
@@ -90,7 +97,15 @@ def dof_functionals(order):
                 dofs.append((p, t0))
                 dofs.append((p, t1))
     if order >= 3:
-        raise NotImplementedError("orders above 2 are outside the oracle")
+        # interior points, the three Cartesian components each
+        for l in range(1, n):
+            for j in range(1, n - l):
+                for i in range(1, n - l - j):
+                    p = sp.Matrix([sp.Rational(i, n), sp.Rational(j, n), sp.Rational(l, n)])
+                    for d in range(3):
+                        e = [0, 0, 0]
+                        e[d] = 1
+                        dofs.append((p, sp.Matrix(e)))
     return dofs
 
 
@@ -169,9 +184,85 @@ def _gauss_tri(npts=6):
     return s.ravel(), t.ravel(), wt.ravel()
 
 
+# ---- orders 3 and 4: float64 construction (sympy is too slow there) ----
+def _monos(deg):
+    return [(a, b, c) for a in range(deg + 1) for b in range(deg + 1 - a) for c in range(deg + 1 - a - b)]
+
+
+@lru_cache(maxsize=None)
+def numeric_basis(order):
+    """Reference basis of degree ``order`` in float64: coefficients
+    coef[a, p, m] of component p of basis function a over the monomials
+    _monos(order)[m].  The space P_{k-1}^3 + x cross homog P_{k-1}^3 is
+    spanned by an orthonormal basis of its coefficient vectors (SVD), then
+    made dual to ``dof_functionals`` by inverting the functional matrix."""
+    import numpy as np
+    k = order
+    mons = _monos(k)
+    idx = {m: i for i, m in enumerate(mons)}
+    nm = len(mons)
+    vecs = []
+    for m in mons:
+        if sum(m) <= k - 1:
+            for d in range(3):
+                v = np.zeros((3, nm))
+                v[d, idx[m]] = 1.0
+                vecs.append(v)
+    for m in mons:
+        if sum(m) == k - 1:
+            for d in range(3):
+                # x cross (e_d m): component i gets eps_{i j d} x_j m
+                v = np.zeros((3, nm))
+                for i in range(3):
+                    for j in range(3):
+                        eps = np.linalg.det(np.eye(3)[[i, j, d]]) if len({i, j, d}) == 3 else 0.0
+                        if eps:
+                            e = list(m)
+                            e[j] += 1
+                            v[i, idx[tuple(e)]] += eps
+                vecs.append(v)
+    A = np.array(vecs).reshape(len(vecs), 3 * nm)
+    _, sv, vt = np.linalg.svd(A, full_matrices=False)
+    r = int((sv > 1e-10 * sv[0]).sum())
+    span = vt[:r].reshape(r, 3, nm)
+    dofs = dof_functionals(order)
+    assert r == len(dofs), (r, len(dofs))
+    P = np.array([[float(x) for x in p] for p, _ in dofs])
+    T = np.array([[float(x) for x in t] for _, t in dofs])
+    mv = np.array([[np.prod(np.asarray(p) ** np.asarray(m)) for m in mons] for p in P])  # (n, nm)
+    D = np.einsum("id,jdm,im->ij", T, span, mv)
+    C = np.linalg.inv(D)           # basis_a = sum_j C[j, a] span_j
+    return np.einsum("ja,jdm->adm", C, span), mons
+
+
+def _numeric_eval(coef, mons, x, y, z):
+    import numpy as np
+    mv = np.array([x ** m[0] * y ** m[1] * z ** m[2] for m in mons])   # (nm, nq)
+    return np.einsum("adm,mq->adq", coef, mv)
+
+
+def _numeric_curl(coef, mons):
+    import numpy as np
+    idx = {m: i for i, m in enumerate(mons)}
+    def deriv(c, d):
+        out = np.zeros_like(c)
+        for m, i in idx.items():
+            if m[d] > 0:
+                e = list(m)
+                e[d] -= 1
+                out[..., idx[tuple(e)]] += m[d] * c[..., i]
+        return out
+    cx = deriv(coef[:, 2], 1) - deriv(coef[:, 1], 2)
+    cy = deriv(coef[:, 0], 2) - deriv(coef[:, 2], 0)
+    cz = deriv(coef[:, 1], 0) - deriv(coef[:, 0], 1)
+    return np.stack([cx, cy, cz], axis=1)
+
+
 @lru_cache(maxsize=None)
 def reference_tensors(order):
-    """Reference tensors by exact-degree quadrature of the exact basis.
+    """Reference tensors by exact-degree quadrature of the basis (exact
+    sympy basis for orders 1-2, the float64 one of ``numeric_basis`` for
+    orders 3-4).
 
     Returns numpy arrays
       'mass'[a,b,p,q]   = int_ref N_a,p N_b,q dX
@@ -179,11 +270,20 @@ def reference_tensors(order):
       'face'[f,a,b,p,q] = int_{face f, (s,t) measure} N_a,p N_b,q
     """
     import numpy as np
-    fb, fc = basis_lambdas(order)
+    if order >= 3:
+        coef, mons = numeric_basis(order)
+        ccoef = _numeric_curl(coef, mons)
+        fb = lambda x, y, z: _numeric_eval(coef, mons, x, y, z)
+        fc = lambda x, y, z: _numeric_eval(ccoef, mons, x, y, z)
+        ev = lambda f, x, y, z: f(np.asarray(x, float), np.asarray(y, float), np.asarray(z, float))
+    else:
+        fb, fc = basis_lambdas(order)
+
+        def ev(f, x, y, z):
+            vals = f(x, y, z)
+            return np.array([[np.broadcast_to(np.asarray(c, dtype=float), x.shape) for c in v]
+                             for v in vals])
     pts, wt = _gauss_tet()
-    def ev(f, x, y, z):
-        vals = f(x, y, z)
-        return np.array([[np.broadcast_to(np.asarray(c, dtype=float), x.shape) for c in v] for v in vals])
     Nv = ev(fb, *pts)            # (n, 3, nq)
     Cv = ev(fc, *pts)
     mass = np.einsum("apk,bqk,k->abpq", Nv, Nv, wt)

@@ -36,8 +36,9 @@ def _run(cmd):
 def build(verbose=False, force=False):
     os.makedirs(BUILD, exist_ok=True)
     tables = os.path.join(CSRC, "n1curl_tables.h")
-    if not os.path.exists(tables):
-        _run([sys.executable, os.path.join(CSRC, "gen_tables.py"), tables])
+    tables_hi = os.path.join(CSRC, "n1curl_tables_hi.h")
+    if not os.path.exists(tables) or not os.path.exists(tables_hi):
+        _run([sys.executable, os.path.join(CSRC, "gen_tables.py"), tables, tables_hi])
     srcs = _sources()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
     headers.append(os.path.join(ROOT, "include", "sucem_gb300.h"))

@@ -17,6 +17,7 @@
 
 namespace sucem {
 void boundary_dual(const Space& hs, std::vector<double>& pt);
+const double* n1curl_table_hi(int order, int which);
 thread_local std::string g_last_error;
 static std::atomic<long long> g_launches{0};
 void count_launch(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
@@ -61,7 +62,7 @@ void free_device_space(DeviceSpace* d) {
                   d->cell_dofs, d->boundary_dofs, d->kc_f, d->km_f, d->kt_f,
                   d->kc_d,    d->km_d,    d->kt_d, d->bidx, d->g_f, d->g_d, d->h_f, d->h_d,
                   d->kab_f, d->kab_d, d->ext_facets, d->ntff_pts, d->bdof_pt,
-                  d->bin_ptr, d->bin_cells};
+                  d->bin_ptr, d->bin_cells, d->cell_pos};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   cudaSetDevice(prev);
@@ -103,10 +104,23 @@ std::string upload_space(Space& s, int device) {
   std::vector<int32_t> indptr32(s.n + 1);
   for (int64_t r = 0; r <= s.n; ++r) indptr32[r] = (int32_t)s.indptr[r];
   std::vector<double> kc, km, kf;
-  if (s.order == 1)
+  if (s.order == 1) {
     flatten_tables<6>(KC1, KM1, KT1, kc, km, kf);
-  else
+  } else if (s.order == 2) {
     flatten_tables<20>(KC2, KM2, KT2, kc, km, kf);
+  } else {
+    const size_t nn = (size_t)s.ndof_cell * s.ndof_cell;
+    const double* tc = n1curl_table_hi(s.order, 0);
+    const double* tm = n1curl_table_hi(s.order, 1);
+    const double* tf = n1curl_table_hi(s.order, 2);
+    if (!tc || !tm || !tf) {
+      delete d;
+      return "no reference tables for this order";
+    }
+    kc.assign(tc, tc + 6 * nn);
+    km.assign(tm, tm + 6 * nn);
+    kf.assign(tf, tf + 12 * nn);
+  }
   std::vector<float> kcf(kc.begin(), kc.end()), kmf(km.begin(), km.end()),
       kff(kf.begin(), kf.end());
   const int nd = s.ndof_cell;
@@ -151,6 +165,7 @@ std::string upload_space(Space& s, int device) {
   UP(kab_f, kabf.data(), kabf.size());
   UP(kab_d, kab.data(), kab.size());
   UP(bidx, bidx.data(), bidx.size());
+  UP(cell_pos, s.cell_pos.data(), s.cell_pos.size());
   d->nb = nb;
 #undef UP
   d->n_boundary = (int64_t)s.boundary_dofs.size();
@@ -234,6 +249,7 @@ int sucem_space_copy(const sucem_space* sp, int what, void* dst) {
     case SUCEM_COPY_CELL_FACES: return cp(s.cell_faces.data(), s.cell_faces.size() * 4);
     case SUCEM_COPY_DOF_XYZ: return cp(s.dof_xyz.data(), s.dof_xyz.size() * 8);
     case SUCEM_COPY_BOUNDARY_DUAL: {
+      if (s.order > 2) return fail("boundary dual functionals: basis orders 1 and 2 only", SUCEM_ERR_ARG);
       std::vector<double> pt;
       sucem::boundary_dual(s, pt);
       return cp(pt.data(), pt.size() * 8);

@@ -24,6 +24,7 @@ struct DeviceSpace {
   int32_t* indptr = nullptr;      // n+1
   int32_t* indices = nullptr;     // nnz
   int32_t* cell_dofs = nullptr;   // nt*nd
+  int32_t* cell_pos = nullptr;    // orders 3-4: nt*nd*nd CSR positions of the cell entries
   int32_t* boundary_dofs = nullptr;
   int64_t n_boundary = 0;
   int32_t* bidx = nullptr;        // nt: index among cells with exterior facets, -1 otherwise
@@ -62,7 +63,9 @@ struct DeviceSpace {
 std::string upload_space(Space& s, int device);
 void free_device_space(DeviceSpace* d);
 
-// Row-gather assembly.  real_bytes = 4 (float) or 8 (double).
+// Assembly: row-gather for orders 1-2, cell-based (atomic adds at the
+// precomputed CSR positions) for orders 3-4.  real_bytes = 4 (float) or 8
+// (double).
 //   mode 0: S, T, B written to separate real arrays (any may be null)
 //   mode 1: A = S - k0^2 T + j k0 B written as interleaved complex
 struct AssembleArgs {

@@ -28,6 +28,10 @@ void count_launch(int k);
 // it, mapped by that cell: p = x0 + J p_hat, t = J t_hat (6 doubles each)
 void boundary_dual(const Space& hs, std::vector<double>& pt) {
   const int nd = hs.ndof_cell;
+  if (hs.order > 2) {
+    pt.clear();
+    return;
+  }
   const double(*dual)[6] = hs.order == 1 ? DUAL1 : DUAL2;
   std::vector<int64_t> owner(hs.n, -1);
   for (int64_t i = 0; i < hs.nt * nd; ++i)
@@ -200,6 +204,7 @@ extern "C" int sucem_em_functional(const sucem_space* sp, const double* E, const
   using namespace sucem;
   const DeviceSpace* d = sp ? sp->s.dev : nullptr;
   if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  if (d->nd > 20) return fail("supported for basis orders 1 and 2 only", SUCEM_ERR_ARG);
   if (!E || !g || !part || !out) return fail("null argument", SUCEM_ERR_ARG);
   cudaStream_t s = (cudaStream_t)stream;
   const int threads = 128;
@@ -223,6 +228,7 @@ extern "C" int sucem_plane_wave_dofs(const sucem_space* sp, int npw, const doubl
   using namespace sucem;
   DeviceSpace* d = sp ? sp->s.dev : nullptr;
   if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  if (d->nd > 20) return fail("supported for basis orders 1 and 2 only", SUCEM_ERR_ARG);
   if (npw < 0) return fail("negative wave count", SUCEM_ERR_ARG);
   if (npw == 0 || d->n_boundary == 0) return SUCEM_OK;
   if (!rhat || !cf || !g) return fail("null argument", SUCEM_ERR_ARG);

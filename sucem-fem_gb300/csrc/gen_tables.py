@@ -144,19 +144,36 @@ def span(order):
 
 
 def dofs(order):
+    """FIAT's dual basis of the degree-k element as (point, vector) pairs,
+    DOF(u) = u(point) . vector: tangential evaluations at the interior
+    points of a (k+1)-interval lattice on every edge (tangent v1-v0), two
+    per interior face-lattice point (face tangents v1-v0, v2-v0) for k >= 2,
+    and the three Cartesian components at every interior cell-lattice point
+    for k >= 3 (these are cell-local, so their order inside the cell is a
+    local convention)."""
     n = order + 1
     out = []
     for a, b in EDGES:
         t = [VERTS[b][d] - VERTS[a][d] for d in range(3)]
         for i in range(1, n):
             out.append(([VERTS[a][d] + F(i, n) * t[d] for d in range(3)], t))
-    if order == 2:
+    if order >= 2:
         for a, b, c in FACES:
             t0 = [VERTS[b][d] - VERTS[a][d] for d in range(3)]
             t1 = [VERTS[c][d] - VERTS[a][d] for d in range(3)]
-            p = [VERTS[a][d] + F(1, 3) * t0[d] + F(1, 3) * t1[d] for d in range(3)]
-            out.append((p, t0))
-            out.append((p, t1))
+            for j in range(1, n):
+                for i in range(1, n - j):
+                    p = [VERTS[a][d] + F(i, n) * t0[d] + F(j, n) * t1[d] for d in range(3)]
+                    out.append((p, t0))
+                    out.append((p, t1))
+    if order >= 3:
+        for l in range(1, n):
+            for j in range(1, n - l):
+                for i in range(1, n - l - j):
+                    for d in range(3):
+                        e = [0, 0, 0]
+                        e[d] = 1
+                        out.append(([F(i, n), F(j, n), F(l, n)], e))
     return out
 
 
@@ -259,14 +276,83 @@ def tables(order):
     return KC, KM, KT, NB
 
 
+def monos(deg):
+    """Monomial exponents of total degree <= deg."""
+    return [(a, b, s - a - b) for s in range(deg + 1) for a in range(s, -1, -1)
+            for b in range(s - a, -1, -1)]
+
+
+def matmul(A, B):
+    Bt = list(zip(*B))
+    return [[sum(x * y for x, y in zip(r, col) if x and y) for col in Bt] for r in A]
+
+
+def tables_moments(order):
+    """KC, KM, KT of any order through exact monomial moment matrices: with
+    C the coefficients of the basis components over the monomials m_i and
+    M_ij = int m_i m_j, every table is a product C M C^T (orders 1 and 2
+    give exactly the tables of ``tables``)."""
+    N = basis(order)
+    n = len(N)
+    Cu = [curl(v) for v in N]
+    mN, mC = monos(order), monos(order - 1)
+
+    def coef(polys, ms):
+        idx = {m: i for i, m in enumerate(ms)}
+        rows = []
+        for v in polys:
+            for p in range(3):
+                r = [F(0)] * len(ms)
+                for e, c in v[p].items():
+                    r[idx[e]] = c
+                rows.append(r)
+        return rows  # row 3a + p
+
+    def moments(ms):
+        return [[F(factorial(a[0] + b[0]) * factorial(a[1] + b[1]) * factorial(a[2] + b[2]),
+                   factorial(sum(a) + sum(b) + 3)) for b in ms] for a in ms]
+
+    CN, CC = coef(N, mN), coef(Cu, mC)
+    PN = matmul(matmul(CN, moments(mN)), [list(r) for r in zip(*CN)])
+    PC = matmul(matmul(CC, moments(mC)), [list(r) for r in zip(*CC)])
+
+    def sym6(P):
+        out = [[[F(0)] * n for _ in range(n)] for _ in range(6)]
+        for m, (p, q) in enumerate(SYM):
+            for a in range(n):
+                for b in range(n):
+                    val = P[3 * a + p][3 * b + q]
+                    if p != q:
+                        val += P[3 * a + q][3 * b + p]
+                    out[m][a][b] = val
+        return out
+
+    KT = []
+    for f in range(4):
+        va, vb, vc = (VERTS[i] for i in FACES[f])
+        ta = [vb[d] - va[d] for d in range(3)]
+        tb = [vc[d] - va[d] for d in range(3)]
+        Mf = [[int_face(mono(tuple(x + y for x, y in zip(a, b))), f) for b in mN] for a in mN]
+        Ta = [[sum(CN[3 * a + d][i] * ta[d] for d in range(3)) for i in range(len(mN))]
+              for a in range(n)]
+        Tb = [[sum(CN[3 * a + d][i] * tb[d] for d in range(3)) for i in range(len(mN))]
+              for a in range(n)]
+        TaM, TbM = matmul(Ta, Mf), matmul(Tb, Mf)
+        TaT, TbT = [list(r) for r in zip(*Ta)], [list(r) for r in zip(*Tb)]
+        ab1 = matmul(TaM, TbT)
+        KT.append([matmul(TaM, TaT), [[ab1[a][b] + ab1[b][a] for b in range(n)] for a in range(n)],
+                   matmul(TbM, TbT)])
+    return sym6(PC), sym6(PN), KT
+
+
 def _fmt(x, depth):
     if isinstance(x, list):
         inner = ",".join(_fmt(y, depth + 1) for y in x)
         return "{" + inner + "}" + ("\n" if depth <= 1 else "")
-    return repr(float(x))
+    return "0" if x == 0 else repr(float(x))
 
 
-def main(path):
+def main(path, path_hi):
     lines = ["// Generated by gen_tables.py: N1curl reference-element constants.",
              "// Do not edit; rerun the generator.", "#pragma once", ""]
     for order in (1, 2):
@@ -281,8 +367,21 @@ def main(path):
         lines.append("")
     with open(path, "w") as f:
         f.write("\n".join(lines))
+    # orders 3 and 4: the assembly tables only (their own translation unit)
+    lines = ["// Generated by gen_tables.py: N1curl reference-element constants of",
+             "// orders 3 and 4.  Do not edit; rerun the generator.", "#pragma once", ""]
+    for order in (3, 4):
+        KC, KM, KT = tables_moments(order)
+        n = len(KC[0])
+        lines.append("static const double KC%d[6][%d][%d] = %s;" % (order, n, n, _fmt(KC, 0)))
+        lines.append("static const double KM%d[6][%d][%d] = %s;" % (order, n, n, _fmt(KM, 0)))
+        lines.append("static const double KT%d[4][3][%d][%d] = %s;" % (order, n, n, _fmt(KT, 0)))
+        lines.append("")
+    with open(path_hi, "w") as f:
+        f.write("\n".join(lines))
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else
-         os.path.join(os.path.dirname(os.path.abspath(__file__)), "n1curl_tables.h"))
+    here = os.path.dirname(os.path.abspath(__file__))
+    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(here, "n1curl_tables.h"),
+         sys.argv[2] if len(sys.argv) > 2 else os.path.join(here, "n1curl_tables_hi.h"))

@@ -598,6 +598,7 @@ extern "C" int sucem_point_sources(const sucem_space* sp, const double* pts,
   using namespace sucem;
   const DeviceSpace* d = sp ? sp->s.dev : nullptr;
   if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  if (d->nd > 20) return fail("supported for basis orders 1 and 2 only", SUCEM_ERR_ARG);
   if (npts < 0) return fail("negative point count", SUCEM_ERR_ARG);
   if (npts == 0) return SUCEM_OK;
   if (!pts || !values || !cells_out || !contrib) return fail("null argument", SUCEM_ERR_ARG);
@@ -630,6 +631,7 @@ extern "C" int sucem_reconstruct_points(const sucem_space* sp, int dtype, const 
   using namespace sucem;
   const DeviceSpace* d = sp ? sp->s.dev : nullptr;
   if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  if (d->nd > 20) return fail("supported for basis orders 1 and 2 only", SUCEM_ERR_ARG);
   if (dtype != SUCEM_C64 && dtype != SUCEM_C128) return fail("dtype must be complex", SUCEM_ERR_ARG);
   if (npts < 0) return fail("negative point count", SUCEM_ERR_ARG);
   if (npts == 0) return SUCEM_OK;
@@ -667,6 +669,7 @@ extern "C" int sucem_surface_flux(const sucem_space* sp, int dtype, const void* 
   using namespace sucem;
   const DeviceSpace* d = sp ? sp->s.dev : nullptr;
   if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  if (d->nd > 20) return fail("supported for basis orders 1 and 2 only", SUCEM_ERR_ARG);
   if (dtype != SUCEM_C64 && dtype != SUCEM_C128) return fail("dtype must be complex", SUCEM_ERR_ARG);
   if (!(k0 > 0)) return fail("k0 must be positive", SUCEM_ERR_ARG);
   if (!x || !part || !out) return fail("null argument", SUCEM_ERR_ARG);
@@ -703,6 +706,7 @@ extern "C" int sucem_ntff(const sucem_space* sp, int dtype, const void* x, doubl
   using namespace sucem;
   DeviceSpace* d = sp ? sp->s.dev : nullptr;
   if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  if (d->nd > 20) return fail("supported for basis orders 1 and 2 only", SUCEM_ERR_ARG);
   if (dtype != SUCEM_C64 && dtype != SUCEM_C128) return fail("dtype must be complex", SUCEM_ERR_ARG);
   if (!(k0 > 0)) return fail("k0 must be positive", SUCEM_ERR_ARG);
   if (ndir < 0) return fail("negative direction count", SUCEM_ERR_ARG);

@@ -8,7 +8,9 @@
 //  * edges and faces are numbered by first encounter while walking the cells
 //    in order and each cell's local entities in UFC order;
 //  * order 1: dof = edge; order 2: dofs 2e, 2e+1 per edge, then
-//    2E + 2f, 2E + 2f + 1 per face.
+//    2E + 2f, 2E + 2f + 1 per face; order k in general: k DOFs per edge,
+//    then k(k-1) per face, then k(k-1)(k-2)/2 per cell, entity by entity
+//    (the numbering above for k <= 2).
 // The CSR pattern is the union of all cell-pair couplings with sorted
 // columns (explicit zeros kept), i.e. DOLFIN's cell sparsity pattern.
 #include "space.h"
@@ -44,13 +46,16 @@ struct EntityTable {
 
 std::string build_space(Space& s, const double* coords, int64_t nv, const int64_t* cells,
                         int64_t nt, int order) {
-  if (order != 1 && order != 2) return "order must be 1 or 2";
+  if (order < 1 || order > 4) return "order must be 1, 2, 3 or 4";
   if (nv <= 0 || nt <= 0) return "empty mesh";
   if (nv >= (int64_t(1) << 31) || nt >= (int64_t(1) << 31)) return "mesh too large for int32 ids";
   s.order = order;
-  s.ndof_cell = order == 1 ? 6 : 20;
-  s.dofs_per_entity = order == 1 ? 1 : 2;
-  s.rec_bytes = order == 1 ? 8 : 24;
+  s.ndof_cell = order * (order + 2) * (order + 3) / 2;
+  s.dofs_per_entity = order <= 2 ? order : 0;
+  s.dofs_edge = order;
+  s.dofs_face = order * (order - 1);
+  s.dofs_cell = order * (order - 1) * (order - 2) / 2;
+  s.rec_bytes = order == 1 ? 8 : (order == 2 ? 24 : 0);
   s.nv = nv;
   s.nt = nt;
   s.coords.assign(coords, coords + nv * 3);
@@ -120,32 +125,36 @@ std::string build_space(Space& s, const double* coords, int64_t nv, const int64_
 
   // ---- DOF map ----
   const int nd = s.ndof_cell;
-  s.n = order == 1 ? s.ne : 2 * s.ne + 2 * s.nf;
+  const int de = s.dofs_edge, df = s.dofs_face, dc = s.dofs_cell;
+  const int64_t face0 = de * s.ne, cell0 = face0 + df * s.nf;
+  s.n = cell0 + dc * nt;
   if (s.n >= (int64_t(1) << 31)) return "too many DOFs for int32 indices";
   s.cell_dofs.resize(nt * nd);
   for (int64_t c = 0; c < nt; ++c) {
     int32_t* d = &s.cell_dofs[c * nd];
-    if (order == 1) {
-      for (int le = 0; le < 6; ++le) d[le] = s.cell_edges[c * 6 + le];
-    } else {
-      for (int le = 0; le < 6; ++le) {
-        d[2 * le] = 2 * s.cell_edges[c * 6 + le];
-        d[2 * le + 1] = 2 * s.cell_edges[c * 6 + le] + 1;
-      }
-      for (int lf = 0; lf < 4; ++lf) {
-        d[12 + 2 * lf] = int32_t(2 * s.ne + 2 * s.cell_faces[c * 4 + lf]);
-        d[13 + 2 * lf] = int32_t(2 * s.ne + 2 * s.cell_faces[c * 4 + lf] + 1);
-      }
-    }
+    for (int le = 0; le < 6; ++le)
+      for (int j = 0; j < de; ++j) d[de * le + j] = int32_t(de * s.cell_edges[c * 6 + le] + j);
+    for (int lf = 0; lf < 4; ++lf)
+      for (int j = 0; j < df; ++j)
+        d[6 * de + df * lf + j] = int32_t(face0 + df * int64_t(s.cell_faces[c * 4 + lf]) + j);
+    for (int j = 0; j < dc; ++j) d[6 * de + 4 * df + j] = int32_t(cell0 + dc * c + j);
   }
 
   // ---- entity -> incident cells (in cell order) ----
-  s.n_ent = order == 1 ? s.ne : s.ne + s.nf;
+  // entities: edges, then faces (order >= 2), then cells (order >= 3)
+  s.n_ent = s.ne + (order >= 2 ? s.nf : 0) + (order >= 3 ? nt : 0);
+  auto ent_first_dof = [&](int64_t k) -> int64_t {
+    if (k < s.ne) return de * k;
+    if (k < s.ne + s.nf) return face0 + df * (k - s.ne);
+    return cell0 + dc * (k - s.ne - s.nf);
+  };
+  auto ent_ndof = [&](int64_t k) -> int { return k < s.ne ? de : (k < s.ne + s.nf ? df : dc); };
   s.ent_ptr.assign(s.n_ent + 1, 0);
   for (int64_t c = 0; c < nt; ++c) {
     for (int le = 0; le < 6; ++le) s.ent_ptr[s.cell_edges[c * 6 + le] + 1]++;
-    if (order == 2)
+    if (order >= 2)
       for (int lf = 0; lf < 4; ++lf) s.ent_ptr[s.ne + s.cell_faces[c * 4 + lf] + 1]++;
+    if (order >= 3) s.ent_ptr[s.ne + s.nf + c + 1]++;
   }
   for (int64_t k = 0; k < s.n_ent; ++k) s.ent_ptr[k + 1] += s.ent_ptr[k];
   const int64_t ninc = s.ent_ptr[s.n_ent];
@@ -160,18 +169,22 @@ std::string build_space(Space& s, const double* coords, int64_t nv, const int64_
         s.inc_cell[pos] = int32_t(c);
         inc_local[pos] = uint8_t(le);
       }
-      if (order == 2)
+      if (order >= 2)
         for (int lf = 0; lf < 4; ++lf) {
           int64_t k = s.ne + s.cell_faces[c * 4 + lf];
           int32_t pos = fill[k]++;
           s.inc_cell[pos] = int32_t(c);
           inc_local[pos] = uint8_t(6 + lf);
         }
+      if (order >= 3) {
+        int32_t pos = fill[s.ne + s.nf + c]++;
+        s.inc_cell[pos] = int32_t(c);
+        inc_local[pos] = uint8_t(10);
+      }
     }
   }
 
   // ---- pattern: column list per entity (shared by its rows) ----
-  const int dpe = s.dofs_per_entity;
   std::vector<int64_t> ent_len(s.n_ent, 0);
   std::vector<int64_t> ent_col_ptr(s.n_ent + 1, 0);
   std::vector<int32_t> ent_cols;
@@ -195,7 +208,7 @@ std::string build_space(Space& s, const double* coords, int64_t nv, const int64_
     ent_cols.resize(ent_col_ptr[s.n_ent]);
     int64_t maxlen = 0;
     for (int64_t k = 0; k < s.n_ent; ++k) maxlen = std::max(maxlen, ent_len[k]);
-    if (maxlen > 255)
+    if (order <= 2 && maxlen > 255)
       return "a CSR row has more than 255 columns (cell valence too high for the 8-bit slot tables)";
     s.max_row = int(maxlen);
     s.inc_rec.assign(ninc * s.rec_bytes, 0);
@@ -213,6 +226,7 @@ std::string build_space(Space& s, const double* coords, int64_t nv, const int64_
         std::sort(buf.begin(), buf.end());
         buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
         std::copy(buf.begin(), buf.end(), ent_cols.begin() + ent_col_ptr[k]);
+        if (order >= 3) continue;
         for (int32_t i = s.ent_ptr[k]; i < s.ent_ptr[k + 1]; ++i) {
           uint8_t* rec = &s.inc_rec[int64_t(i) * s.rec_bytes];
           rec[0] = inc_local[i];
@@ -223,34 +237,61 @@ std::string build_space(Space& s, const double* coords, int64_t nv, const int64_
       }
     }
   }
-  // rows: entity k owns rows dpe*k .. dpe*k+dpe-1
+  // rows: entity k owns the rows of its DOFs (consecutive, in entity order)
   s.indptr.assign(s.n + 1, 0);
   for (int64_t k = 0; k < s.n_ent; ++k)
-    for (int j = 0; j < dpe; ++j) s.indptr[dpe * k + j + 1] = ent_len[k];
+    for (int j = 0; j < ent_ndof(k); ++j) s.indptr[ent_first_dof(k) + j + 1] = ent_len[k];
   for (int64_t r = 0; r < s.n; ++r) s.indptr[r + 1] += s.indptr[r];
   s.nnz = s.indptr[s.n];
   if (s.nnz >= (int64_t(1) << 31)) return "pattern has 2^31 or more entries";
   s.indices.resize(s.nnz);
 #pragma omp parallel for schedule(static)
   for (int64_t k = 0; k < s.n_ent; ++k)
-    for (int j = 0; j < dpe; ++j)
+    for (int j = 0; j < ent_ndof(k); ++j)
       std::copy(ent_cols.begin() + ent_col_ptr[k], ent_cols.begin() + ent_col_ptr[k + 1],
-                s.indices.begin() + s.indptr[dpe * k + j]);
+                s.indices.begin() + s.indptr[ent_first_dof(k) + j]);
+
+  // ---- orders 3-4: CSR position of every local entry of every cell ----
+  if (order >= 3) {
+    if (nt * int64_t(nd) * nd >= (int64_t(1) << 31))
+      return "mesh too large for the order-3/4 position table (2^31 cell entries)";
+    s.cell_pos.resize(nt * int64_t(nd) * nd);
+    std::vector<int64_t> dof_ent(s.n);
+    for (int64_t k = 0; k < s.n_ent; ++k)
+      for (int j = 0; j < ent_ndof(k); ++j) dof_ent[ent_first_dof(k) + j] = k;
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < nt; ++c) {
+      const int32_t* d = &s.cell_dofs[c * nd];
+      for (int a = 0; a < nd; ++a) {
+        const int64_t k = dof_ent[d[a]];
+        const auto b0 = ent_cols.begin() + ent_col_ptr[k], b1 = ent_cols.begin() + ent_col_ptr[k + 1];
+        for (int b = 0; b < nd; ++b)
+          s.cell_pos[(c * nd + a) * nd + b] =
+              int32_t(s.indptr[d[a]] + (std::lower_bound(b0, b1, d[b]) - b0));
+      }
+    }
+  }
 
   // ---- DOF locations (used by the nested-dissection ordering) ----
   s.dof_xyz.assign(s.n * 3, 0.0);
   for (int64_t e = 0; e < s.ne; ++e)
-    for (int j = 0; j < dpe; ++j)
+    for (int j = 0; j < de; ++j)
       for (int d = 0; d < 3; ++d)
-        s.dof_xyz[(dpe * e + j) * 3 + d] =
+        s.dof_xyz[(de * e + j) * 3 + d] =
             0.5 * (s.coords[s.edges[2 * e] * 3 + d] + s.coords[s.edges[2 * e + 1] * 3 + d]);
-  if (order == 2)
-    for (int64_t f = 0; f < s.nf; ++f)
-      for (int j = 0; j < 2; ++j)
-        for (int d = 0; d < 3; ++d)
-          s.dof_xyz[(2 * s.ne + 2 * f + j) * 3 + d] =
-              (s.coords[s.faces[3 * f] * 3 + d] + s.coords[s.faces[3 * f + 1] * 3 + d] +
-               s.coords[s.faces[3 * f + 2] * 3 + d]) / 3.0;
+  for (int64_t f = 0; f < s.nf; ++f)
+    for (int j = 0; j < df; ++j)
+      for (int d = 0; d < 3; ++d)
+        s.dof_xyz[(face0 + df * f + j) * 3 + d] =
+            (s.coords[s.faces[3 * f] * 3 + d] + s.coords[s.faces[3 * f + 1] * 3 + d] +
+             s.coords[s.faces[3 * f + 2] * 3 + d]) / 3.0;
+  for (int64_t c = 0; c < nt; ++c)
+    for (int j = 0; j < dc; ++j)
+      for (int d = 0; d < 3; ++d) {
+        double x = 0;
+        for (int v = 0; v < 4; ++v) x += s.coords[s.cells[c * 4 + v] * 3 + d];
+        s.dof_xyz[(cell0 + dc * c + j) * 3 + d] = 0.25 * x;
+      }
 
   // ---- boundary DOFs (closure of the exterior facets) ----
   {
@@ -261,10 +302,9 @@ std::string build_space(Space& s, const double* coords, int64_t nv, const int64_
         if (!(s.ext_mask[c] >> lf & 1)) continue;
         for (int le = 0; le < 6; ++le) {
           if (kEdgeVerts[le][0] == lf || kEdgeVerts[le][1] == lf) continue;  // edge not on face lf
-          for (int j = 0; j < dpe; ++j) mark[s.cell_dofs[c * nd + dpe * le + j]] = 1;
+          for (int j = 0; j < de; ++j) mark[s.cell_dofs[c * nd + de * le + j]] = 1;
         }
-        if (order == 2)
-          for (int j = 0; j < dpe; ++j) mark[s.cell_dofs[c * nd + 12 + 2 * lf + j]] = 1;
+        for (int j = 0; j < df; ++j) mark[s.cell_dofs[c * nd + 6 * de + df * lf + j]] = 1;
       }
     }
     s.boundary_dofs.clear();

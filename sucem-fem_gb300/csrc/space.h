@@ -15,8 +15,9 @@ struct DeviceSpace;  // device copies, defined in the CUDA sources
 
 struct Space {
   int order = 1;
-  int ndof_cell = 6;        // 6 (order 1) or 20 (order 2)
-  int dofs_per_entity = 1;  // 1 (order 1) or 2 (order 2)
+  int ndof_cell = 6;        // k(k+2)(k+3)/2: 6, 20, 45, 84 for orders 1-4
+  int dofs_per_entity = 1;  // 1 (order 1) or 2 (order 2); orders 3-4: per edge
+  int dofs_edge = 1, dofs_face = 0, dofs_cell = 0;  // k, k(k-1), k(k-1)(k-2)/2
   int64_t nv = 0, nt = 0, ne = 0, nf = 0;
   int64_t n = 0;            // global dimension
   int64_t nnz = 0;
@@ -37,8 +38,9 @@ struct Space {
   std::vector<int32_t> indices;        // nnz
 
   // Row-gather tables.  Entities are the edges (order 1) or the edges
-  // followed by the faces (order 2); entity k owns dofs_per_entity
-  // consecutive rows that share one column list.
+  // followed by the faces (order 2; orders 3-4 add the cells); entity k
+  // owns the consecutive rows of its DOFs, which share one column list.
+  // inc_rec is built for orders 1-2 only.
   int64_t n_ent = 0;
   std::vector<int32_t> ent_ptr;        // n_ent+1
   std::vector<int32_t> inc_cell;       // per incidence: the cell
@@ -46,6 +48,10 @@ struct Space {
                                        //   [0] local entity index (0..5 edge, 6..9 face)
                                        //   [1..ndof_cell] column slot of each local dof
   int rec_bytes = 8;
+
+  // orders 3-4 (cell-based assembly): CSR position of every local entry,
+  // cell_pos[(c * ndof_cell + a) * ndof_cell + b] = index of (dof a, dof b)
+  std::vector<int32_t> cell_pos;
 
   std::vector<int32_t> boundary_dofs;  // closure of the exterior facets, sorted
   std::vector<double> dof_xyz;         // n*3: edge midpoint / face centroid of each DOF

@@ -38,11 +38,13 @@ class FunctionSpace:
     def __init__(self, mesh, family=ELEMENT_FAMILY, order=1):
         if family not in (ELEMENT_FAMILY, "N1curl"):
             raise ValueError("only the %r family is provided" % ELEMENT_FAMILY)
-        if order not in (1, 2):
-            raise ValueError("basis order must be 1 or 2")
+        if order not in (1, 2, 3, 4):
+            raise ValueError("basis order must be 1, 2, 3 or 4")
         self._mesh = mesh
-        self.order = int(order)
-        self.ndof_cell = 6 if order == 1 else 20
+        self.order = k = int(order)
+        self.ndof_cell = k * (k + 2) * (k + 3) // 2
+        # DOFs per edge, per face and per cell interior
+        self.dofs_edge, self.dofs_face, self.dofs_cell = k, k * (k - 1), k * (k - 1) * (k - 2) // 2
         coords = np.ascontiguousarray(mesh.coordinates(), dtype=np.float64)
         cells = np.ascontiguousarray(mesh.cells(), dtype=np.int64)
         h = ctypes.c_void_p()
@@ -120,12 +122,12 @@ class FunctionSpace:
         # local edges of local face lf are those not touching local vertex lf
         edge_verts = np.array([(2, 3), (1, 3), (1, 2), (0, 3), (0, 2), (0, 1)])
         on_face = (edge_verts[None, :, 0] != lf[:, None]) & (edge_verts[None, :, 1] != lf[:, None])
-        edges = np.unique(self.cell_edges[c][on_face])
-        if self.order == 1:
-            return edges.astype(np.int32)
-        fids = np.unique(cf[c, lf])
-        return np.sort(np.concatenate([2 * edges, 2 * edges + 1, 2 * self.ne + 2 * fids,
-                                       2 * self.ne + 2 * fids + 1])).astype(np.int32)
+        edges = np.unique(self.cell_edges[c][on_face]).astype(np.int64)
+        fids = np.unique(cf[c, lf]).astype(np.int64)
+        de, df = self.dofs_edge, self.dofs_face
+        parts = [de * edges + j for j in range(de)]
+        parts += [de * self.ne + df * fids + j for j in range(df)]
+        return np.sort(np.concatenate(parts)).astype(np.int32)
 
     def mesh(self):
         return self._mesh

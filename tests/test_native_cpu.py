@@ -70,7 +70,9 @@ def test_builder_rejects_bad_input():
     with pytest.raises(ValueError, match="out of range"):
         FunctionSpace(Mesh(coords, bad), order=1)
     with pytest.raises(ValueError):
-        FunctionSpace(Mesh(coords, cells), order=3)
+        FunctionSpace(Mesh(coords, cells), order=5)
+    with pytest.raises(ValueError):
+        FunctionSpace(Mesh(coords, cells), order=0)
     rep = cells.copy()
     rep[0, 1] = rep[0, 0]
     with pytest.raises(ValueError, match="degenerate"):
