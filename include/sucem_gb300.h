@@ -50,8 +50,14 @@ long long sucem_launch_count(void);
  * dolfin.assemble (sucemfem/ProblemConfigurations/EMProblem.py:100-105,
  * sucemfem/SystemMatrices.py:54).  coords: nv*3 doubles; cells: nt*4
  * vertex ids (any vertex order; sorted internally as DOLFIN orders meshes);
- * order 1 or 2.  Builds entities, the DOF map (DOLFIN numbering), the CSR
- * pattern and the row-gather tables on the host. */
+ * order 1, 2, 3 or 4 (6, 20, 45, 84 DOFs per cell; orders 3 and 4 are the
+ * degrees of functional_tests/test_EigenProblems.py:86,150).  Builds
+ * entities, the DOF map (DOLFIN numbering for orders 1-2; k DOFs per edge,
+ * k(k-1) per face, then the cell interiors for order k), the CSR pattern
+ * and the row-gather tables (orders 1-2) or the per-cell CSR positions
+ * (orders 3-4) on the host.  Point sources, field reconstruction, flux,
+ * NTFF, EM functional and boundary interpolation take orders 1 and 2 and
+ * return SUCEM_ERR_ARG on order-3/4 spaces. */
 int sucem_space_create(const double* coords, int64_t nv, const int64_t* cells, int64_t nt,
                        int order, sucem_space** out);
 void sucem_space_destroy(sucem_space* sp);
@@ -71,7 +77,8 @@ int sucem_space_sizes(const sucem_space* sp, int64_t* out);
 #define SUCEM_COPY_EXT_MASK 7       /* uint8[nt] exterior-facet bit mask */
 #define SUCEM_COPY_CELL_EDGES 8     /* int32[nt*6] cell -> edge ids (UFC local order) */
 #define SUCEM_COPY_CELL_FACES 9     /* int32[nt*4] cell -> face ids (= facet numbering) */
-#define SUCEM_COPY_DOF_XYZ 10       /* double[n*3] DOF locations (edge midpoint / face centroid) */
+#define SUCEM_COPY_DOF_XYZ 10       /* double[n*3] DOF locations (edge midpoint / face or cell
+                                       centroid) */
 #define SUCEM_COPY_BOUNDARY_DUAL 11 /* double[n_boundary_dofs*6] dual functional of each boundary
                                        DOF: point, tangent (DOF(u) = u(point).tangent) */
 int sucem_space_copy(const sucem_space* sp, int what, void* host_dst);
@@ -96,7 +103,9 @@ int sucem_space_device_ptr(const sucem_space* sp, int what, void** out);
  * (double) selects the precision of the coefficients and outputs.
  * eps_r, mu_r_inv: device arrays of nt values (NULL = 1, the material
  * defaults of sucemfem/Materials.py:31).  S, T, B: device arrays of nnz
- * values; any may be NULL to skip that matrix. */
+ * values; any may be NULL to skip that matrix.  Orders 1-2 write every
+ * value once in a fixed summation order; orders 3-4 zero the outputs and
+ * add the cells' contributions atomically (summation order not fixed). */
 int sucem_assemble(const sucem_space* sp, int real_bytes, const void* eps_r,
                    const void* mu_r_inv, void* S, void* T, void* B, void* stream);
 
