@@ -1,5 +1,6 @@
-"""Generate ``n1curl_tables.h``: reference-element constants of the
-Nedelec first-kind H(curl) element of orders 1 and 2.
+"""Generate ``n1curl_tables.h`` (orders 1 and 2) and ``n1curl_tables_hi.h``
+(orders 3 and 4): reference-element constants of the Nedelec first-kind
+H(curl) element.
 
 The element is the one the reference requests with
 ``dolfin.FunctionSpace(mesh, "Nedelec 1st kind H(curl)", order)``
@@ -7,8 +8,10 @@ The element is the one the reference requests with
 definition: UFC reference tetrahedron, space P_{k-1}^3 + x cross
 homogeneous P_{k-1}^3, dual basis of tangential point evaluations on the
 edges (interior lattice points of k+1 intervals, unnormalised tangent
-v1-v0) and, for k=2, two tangential evaluations per face at the centroid
-(tangents v1-v0, v2-v0 of the face).
+v1-v0), for k >= 2 two tangential evaluations per interior face-lattice
+point (tangents v1-v0, v2-v0 of the face; the centroid for k = 2) and for
+k >= 3 the three components at every interior cell-lattice point (see
+``dofs``).  Orders 3 and 4 carry only the assembly tables KC, KM, KT.
 
 Everything is computed in exact rational arithmetic (``fractions``) with no
 third-party package, so the same script runs on any host.  Written tables
