@@ -143,3 +143,20 @@ def test_reference_prism_cavity_order4_on_the_oracle(tmp_path):
     res = oracle_cavity_k(m.coordinates(), m.cells(), 4)
     ref = analytic_k((1.0, 0.5, 0.25), 5)[:10]
     np.testing.assert_array_almost_equal(np.abs(res - ref) / ref, np.zeros(10), 4)
+
+
+def test_high_order_space_rejects_order_1_2_only_host_queries():
+    """The boundary dual functionals (interpolation onto the boundary) are
+    provided for orders 1 and 2; an order-3 space refuses the host copy."""
+    from sucemfem._native import COPY, call, ptr
+    from sucemfem.mesh import Mesh
+    from sucemfem.space import FunctionSpace
+    c, t = fem.unit_cube(1, 1, 1)
+    V = FunctionSpace(Mesh(c, t), order=3)
+    out = np.zeros(V.n_boundary * 6)
+    with pytest.raises(ValueError, match="orders 1 and 2"):
+        call("sucem_space_copy", V._h, COPY["boundary_dual"], ptr(out))
+    V2 = FunctionSpace(Mesh(c, t), order=2)
+    out = np.zeros(V2.n_boundary * 6)
+    call("sucem_space_copy", V2._h, COPY["boundary_dual"], ptr(out))
+    assert np.isfinite(out).all() and np.abs(out).max() > 0
