@@ -337,6 +337,21 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
       const DNode nd = nodes[tiles[8 * it]];
       const Tile tl = tile_of(tiles + 8 * it);
       const int b = i & 1;
+      float2* buf = epi + warp * 32 * 17;  // [32 rows][17]
+      float2* Cw = arena + nd.off + (int64_t)(tl.row0 + warp * 32) * nd.f + tl.col0;
+      // C of each 16-column block is requested before that block's TMEM
+      // reads (the first one before the accumulator is ready): C is not
+      // touched by the tile's main loop, so its load latency overlaps them
+      float2 cv[16];
+      auto load_c = [&](int cc) {
+#pragma unroll
+        for (int t = 0; t < 16; ++t) {
+          const int r = 2 * t + (lane >> 4), col = cc * 16 + (lane & 15);
+          cv[t] = (warp * 32 + r < tl.nrow && col < tl.ncol) ? Cw[(int64_t)r * nd.f + col]
+                                                           : make_float2(0.f, 0.f);
+        }
+      };
+      load_c(0);
       // uniform per warp: the TMEM loads below are warp-collective
       const bool got =
           __all_sync(~0u, wait_parity(smem_u32(&acc_full[b]), (i / 2) & 1, true));
@@ -346,10 +361,9 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
       const uint32_t tre = tmem + b * ACC_COLS + ((uint32_t)(warp * 32) << 16);
-      float2* buf = epi + warp * 32 * 17;  // [32 rows][17]
-      float2* Cw = arena + nd.off + (int64_t)(tl.row0 + warp * 32) * nd.f + tl.col0;
 #pragma unroll 1
       for (int cc = 0; cc < BN / 16; ++cc) {
+        if (cc > 0) load_c(cc);
         uint32_t re[16], im[16];
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -369,13 +383,6 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
         for (int j = 0; j < 16; ++j)
           buf[lane * 17 + j] = make_float2(__uint_as_float(re[j]), __uint_as_float(im[j]));
         __syncwarp();
-        float2 cv[16];
-#pragma unroll
-        for (int t = 0; t < 16; ++t) {
-          const int r = 2 * t + (lane >> 4), col = cc * 16 + (lane & 15);
-          cv[t] = (warp * 32 + r < tl.nrow && col < tl.ncol) ? Cw[(int64_t)r * nd.f + col]
-                                                           : make_float2(0.f, 0.f);
-        }
 #pragma unroll
         for (int t = 0; t < 16; ++t) {
           const int r = 2 * t + (lane >> 4), col = cc * 16 + (lane & 15);
