@@ -313,7 +313,11 @@ std::string mf_analyse(MFSymbolic& sym, int64_t n, const int32_t* indptr, const 
 }
 
 // Front structure, scatter lists and extend-add maps of an ordering whose
-// nodes are in postorder.
+// nodes are in postorder.  The update set U of a node needs only its
+// children's, so U is built level by level with the nodes of a level in
+// parallel; the scatter lists and extend-add maps are counted per node,
+// laid out by prefix sums in node order and filled in parallel, so the
+// result does not depend on the thread count.
 std::string mf_finish(MFSymbolic& sym, int64_t n, const int32_t* indptr, const int32_t* indices,
                       std::vector<int64_t>&& order, std::vector<MFNode>&& nodes) {
   sym.n = n;
@@ -322,44 +326,90 @@ std::string mf_finish(MFSymbolic& sym, int64_t n, const int32_t* indptr, const i
   sym.iperm.assign(n, 0);
   for (int64_t i = 0; i < n; ++i) sym.iperm[sym.perm[i]] = i;
   sym.nodes = std::move(nodes);
+  const int64_t nn = (int64_t)sym.nodes.size();
 
-  // ---- front structure, bottom-up (nodes are already in postorder) ----
+  // ---- update sets, level by level (children first) ----
+  int max_level = 0;
+  for (const MFNode& nd_s : sym.nodes) max_level = std::max(max_level, nd_s.level);
+  std::vector<std::vector<int64_t>> by_level(max_level + 1);
+  for (int64_t s = 0; s < nn; ++s) by_level[sym.nodes[s].level].push_back(s);
+  for (const auto& lv : by_level) {
+#pragma omp parallel
+    {
+      std::vector<int64_t> buf;
+#pragma omp for schedule(dynamic, 1)
+      for (int64_t t = 0; t < (int64_t)lv.size(); ++t) {
+        MFNode& nd_s = sym.nodes[lv[t]];
+        // only ancestors (new index >= end) enter U
+        buf.clear();
+        for (int c : nd_s.children)
+          for (int64_t u : sym.nodes[c].U)
+            if (u >= nd_s.end) buf.push_back(u);
+        for (int64_t i = nd_s.start; i < nd_s.end; ++i) {
+          const int64_t o = sym.perm[i];
+          for (int32_t q = indptr[o]; q < indptr[o + 1]; ++q) {
+            const int64_t jn = sym.iperm[indices[q]];
+            if (jn >= nd_s.end) buf.push_back(jn);
+          }
+        }
+        std::sort(buf.begin(), buf.end());
+        buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
+        nd_s.U.assign(buf.begin(), buf.end());
+        nd_s.f = nd_s.k + (int64_t)nd_s.U.size();
+      }
+    }
+  }
   sym.max_level = 0;
   sym.arena = 0;
   sym.max_front = 0;
   sym.flops = 0;
-  std::vector<int64_t> buf;
-  for (size_t s = 0; s < sym.nodes.size(); ++s) {
+  for (int64_t s = 0; s < nn; ++s) {
     MFNode& nd_s = sym.nodes[s];
-    buf.clear();
-    for (int c : nd_s.children) buf.insert(buf.end(), sym.nodes[c].U.begin(), sym.nodes[c].U.end());
-    for (int64_t i = nd_s.start; i < nd_s.end; ++i) {
-      const int64_t o = sym.perm[i];
-      for (int32_t q = indptr[o]; q < indptr[o + 1]; ++q) buf.push_back(sym.iperm[indices[q]]);
-    }
-    std::sort(buf.begin(), buf.end());
-    buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
-    auto it = std::lower_bound(buf.begin(), buf.end(), nd_s.end);
-    nd_s.U.assign(it, buf.end());
-    nd_s.f = nd_s.k + (int64_t)nd_s.U.size();
     nd_s.front_off = sym.arena;
     sym.arena += nd_s.f * nd_s.f;
     sym.max_front = std::max(sym.max_front, nd_s.f);
     sym.max_level = std::max(sym.max_level, nd_s.level);
     for (int64_t i = 0; i < nd_s.k; ++i) sym.flops += double(nd_s.f - i - 1) * double(nd_s.f - i - 1);
   }
+
   // ---- scatter lists and extend-add maps ----
   auto pos_in = [&](const MFNode& nd_s, int64_t jn) -> int64_t {
     if (jn < nd_s.end) return jn - nd_s.start;
     auto it = std::lower_bound(nd_s.U.begin(), nd_s.U.end(), jn);
     return nd_s.k + (it - nd_s.U.begin());
   };
-  sym.scat_src.clear();
-  sym.scat_dst.clear();
-  sym.ea_map.clear();
-  for (size_t s = 0; s < sym.nodes.size(); ++s) {
+  // pass 1: entries per node (an own-row entry, plus its transpose when the
+  // column belongs to an ancestor)
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t s = 0; s < nn; ++s) {
     MFNode& nd_s = sym.nodes[s];
-    nd_s.scat_off = (int64_t)sym.scat_src.size();
+    int64_t cnt = 0;
+    for (int64_t i = nd_s.start; i < nd_s.end; ++i) {
+      const int64_t o = sym.perm[i];
+      for (int32_t q = indptr[o]; q < indptr[o + 1]; ++q) {
+        const int64_t jn = sym.iperm[indices[q]];
+        if (jn >= nd_s.start) cnt += jn >= nd_s.end ? 2 : 1;
+      }
+    }
+    nd_s.scat_len = cnt;
+  }
+  int64_t tot = 0, ea_tot = 0;
+  for (int64_t s = 0; s < nn; ++s) {
+    MFNode& nd_s = sym.nodes[s];
+    nd_s.scat_off = tot;
+    tot += nd_s.scat_len;
+    nd_s.ea_off = ea_tot;
+    if (nd_s.parent >= 0) ea_tot += (int64_t)nd_s.U.size();
+  }
+  sym.scat_src.assign(tot, 0);
+  sym.scat_dst.assign(tot, 0);
+  sym.ea_map.assign(ea_tot, 0);
+  // pass 2: fill every node's segment in row order
+  int bad = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(| : bad)
+  for (int64_t s = 0; s < nn; ++s) {
+    const MFNode& nd_s = sym.nodes[s];
+    int64_t w = nd_s.scat_off;
     for (int64_t i = nd_s.start; i < nd_s.end; ++i) {
       const int64_t o = sym.perm[i];
       const int64_t pi = i - nd_s.start;
@@ -368,25 +418,29 @@ std::string mf_finish(MFSymbolic& sym, int64_t n, const int32_t* indptr, const i
         const int64_t jn = sym.iperm[jo];
         if (jn < nd_s.start) continue;  // eliminated in a descendant
         const int64_t pj = pos_in(nd_s, jn);
-        sym.scat_src.push_back(q);
-        sym.scat_dst.push_back(nd_s.front_off + pi * nd_s.f + pj);
+        sym.scat_src[w] = q;
+        sym.scat_dst[w++] = nd_s.front_off + pi * nd_s.f + pj;
         if (jn >= nd_s.end) {  // column entry A(j, i) of the ancestor row j
           const int32_t* b = indices + indptr[jo];
           const int32_t* e = indices + indptr[jo + 1];
           const int32_t* t = std::lower_bound(b, e, (int32_t)o);
-          if (t == e || *t != o) return "matrix pattern is not structurally symmetric";
-          sym.scat_src.push_back((int32_t)(t - indices));
-          sym.scat_dst.push_back(nd_s.front_off + pj * nd_s.f + pi);
+          if (t == e || *t != o) {
+            bad = 1;
+            sym.scat_src[w] = 0;
+          } else {
+            sym.scat_src[w] = (int32_t)(t - indices);
+          }
+          sym.scat_dst[w++] = nd_s.front_off + pj * nd_s.f + pi;
         }
       }
     }
-    nd_s.scat_len = (int64_t)sym.scat_src.size() - nd_s.scat_off;
-    nd_s.ea_off = (int64_t)sym.ea_map.size();
     if (nd_s.parent >= 0) {
       const MFNode& par = sym.nodes[nd_s.parent];
-      for (int64_t u : nd_s.U) sym.ea_map.push_back((int32_t)pos_in(par, u));
+      int64_t e = nd_s.ea_off;
+      for (int64_t u : nd_s.U) sym.ea_map[e++] = (int32_t)pos_in(par, u);
     }
   }
+  if (bad) return "matrix pattern is not structurally symmetric";
   return "";
 }
 
