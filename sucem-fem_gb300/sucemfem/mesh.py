@@ -97,6 +97,22 @@ class Mesh:
     def num_vertices(self):
         return len(self._x)
 
+    def topology_space(self):
+        """The order-1 function space of this mesh, built once: its edges
+        and faces carry DOLFIN's edge and facet numbering."""
+        if getattr(self, "_space1", None) is None:
+            from .space import FunctionSpace
+            self._space1 = FunctionSpace(self, order=1)
+        return self._space1
+
+    def num_edges(self):
+        return self.topology_space().ne
+
+    def num_faces(self):
+        return self.topology_space().nf
+
+    num_facets = num_faces
+
     class _Topology:
         def __init__(self, mesh):
             self._m = mesh
@@ -109,8 +125,9 @@ class Mesh:
 
 
 class MeshFunction:
-    """MeshFunction('uint', mesh, dim): an integer per cell (dim 3) or per
-    facet (dim 2, facets in the space's face numbering)."""
+    """MeshFunction('uint', mesh, dim): an integer per cell (dim 3), per
+    facet (dim 2, facets in the space's face numbering), per edge (dim 1,
+    the space's edge numbering) or per vertex (dim 0)."""
 
     def __init__(self, value_type, mesh, dim, value=0):
         self.mesh = mesh
@@ -132,8 +149,12 @@ class MeshFunction:
             size = mesh.num_cells()
         elif self.dim == 2:
             size = None  # sized lazily from the facet numbering
+        elif self.dim == 1:
+            size = mesh.num_edges()
+        elif self.dim == 0:
+            size = mesh.num_vertices()
         else:
-            raise ValueError("only cell (3) and facet (2) mesh functions are supported")
+            raise ValueError("mesh function dimension must be 0, 1, 2 or 3")
         self._a = None if size is None else np.full(size, value, dtype=np.int64)
         self._fill = value
 
@@ -154,6 +175,25 @@ class MeshFunction:
 
     def __setitem__(self, i, v):
         self._a[i] = v
+
+
+def VertexFunction(value_type, mesh, value=0):
+    return MeshFunction(value_type, mesh, 0, value)
+
+
+def EdgeFunction(value_type, mesh, value=0):
+    return MeshFunction(value_type, mesh, 1, value)
+
+
+def FaceFunction(value_type, mesh, value=0):
+    return MeshFunction(value_type, mesh, 2, value)
+
+
+FacetFunction = FaceFunction
+
+
+def CellFunction(value_type, mesh, value=0):
+    return MeshFunction(value_type, mesh, 3, value)
 
 
 class DomainBoundary:

@@ -222,3 +222,35 @@ def test_plane_wave_dofs_match_host_interpolant():
     si.set_interpolant_expression(*t.get_expression())
     ref = si.calculate_interpolation()
     assert np.abs(g - ref).max() < 1e-13 * np.abs(ref).max()
+
+
+def test_complex_voltage_along_line():
+    """Sources/PostProcess.py:46-66: the complex line integral of E . l_hat
+    with the field reconstructed on the GPU (each Romberg level's points in
+    one batch) against the same Romberg integration of the oracle's field,
+    real and imaginary parts as two separate integrals."""
+    import warnings
+    from sucemfem.mesh import Mesh
+    from sucemfem.space import FunctionSpace
+    from sucemfem.Sources.PostProcess import ComplexVoltageAlongLine, VoltageAlongLine
+    coords, cells = fem.box_mesh(1.0, 1.0, 1.0, 3, 3, 3)
+    coords = fem.jitter_interior(coords, cells, 1 / 3, 0.2, seed=4)
+    V = FunctionSpace(Mesh(coords, cells), order=2)
+    A = fem.assemble(coords, cells, 2)
+    rng = np.random.default_rng(8)
+    x = rng.standard_normal(V.n) + 1j * rng.standard_normal(V.n)
+    start, end = np.array([0.1, 0.2, 0.3]), np.array([0.8, 0.7, 0.9])
+
+    def oracle_E(part):
+        def E(px, py, pz):
+            e = postproc.reconstruct_points(coords, cells, 2, A.dofmap, x, np.array([[px, py, pz]]))[0]
+            return e.real if part == 0 else e.imag
+        return E
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        cv = ComplexVoltageAlongLine(V)
+        cv.set_dofs(x)
+        got = cv.calculate_voltage(start, end)
+        ref = (VoltageAlongLine(oracle_E(0)).calculate_voltage(start, end)
+               + 1j * VoltageAlongLine(oracle_E(1)).calculate_voltage(start, end))
+    assert abs(got - ref) <= 1e-9 * abs(ref), (got, ref)
