@@ -110,3 +110,28 @@ def test_voltage_along_line():
     # E = (y, x z, 1) from (0,0,0) to (1,2,3): integral of 2t + 6t^2 + 3 over [0, 1]
     v = VoltageAlongLine(lambda x, y, z: np.array([y, x * z, 1.0]))
     assert v.calculate_voltage(np.zeros(3), np.array([1.0, 2.0, 3.0])) == pytest.approx(6.0, rel=1e-10)
+
+
+def test_paths_and_filament_far_field(tmp_path):
+    from sucemfem.Consts import c0, mu0
+    from sucemfem.Testing import Paths
+    from sucemfem.Testing.Analytical.current_fillament_farfield import eval_E_theta
+    f = tmp_path / "data.txt"
+    f.write_text("x")
+    mod = str(tmp_path / "test_mod.py")
+    assert Paths.get_module_path(mod) == str(tmp_path)
+    assert Paths.get_module_path_filename("data.txt", mod) == str(f)
+    with Paths.get_module_path_file("data.txt", mod) as fo:
+        assert fo.read() == "x"
+    # broadside of a short filament: the Hertzian dipole j omega mu I L / (4 pi r)
+    freq, L, I = 1e9, 1e-3, 2.0
+    omega = 2 * np.pi * freq
+    e = eval_E_theta(freq, L, I, np.pi / 2, r_val=3.0)
+    assert e == pytest.approx(1j * omega * mu0 * I * L * np.exp(-1j * omega / c0 * 3.0)
+                              / (4 * np.pi * 3.0), rel=1e-12)
+    # the array factor sin(u)/u at an oblique angle, and zero on the axis
+    th = 0.7
+    u = omega / c0 * 0.4 / 2 * np.cos(th)
+    assert abs(eval_E_theta(freq, 0.4, 1.0, th)) == pytest.approx(
+        omega * mu0 * 0.4 / (4 * np.pi) * np.sin(th) * abs(np.sin(u) / u), rel=1e-12)
+    assert eval_E_theta(freq, 0.4, 1.0, 0.0) == 0
