@@ -35,10 +35,12 @@
 //     stage's "empty" barrier (the producers' permission to refill it);
 //     after a tile's last chunk it commits to the accumulator's "acc_full"
 //     barrier;
-//   warps 0-3 (epilogue): wait for "acc_full", read their 32 TMEM lanes
-//     (tile rows) of both accumulators 16 columns at a time, turn them
-//     through shared memory so that a warp's accesses to C cover two rows of
-//     16 consecutive columns, apply C -= D and arrive on "acc_empty".
+//   warps 0-3 (epilogue): request the tile's first 16 columns of C, wait
+//     for "acc_full", read their 32 TMEM lanes (tile rows) of both
+//     accumulators 16 columns at a time (each block's C requested before its
+//     TMEM reads), turn them through shared memory so that a warp's accesses
+//     to C cover two rows of 16 consecutive columns, apply C -= D and arrive
+//     on "acc_empty".
 // Two accumulators (all 512 TMEM columns) let the epilogue of one tile run
 // under the main loop of the next.  Every wait is bounded: on a timeout the
 // kernel raises *err, every role stops, and all meet at the final barrier.
