@@ -1,8 +1,8 @@
 """Convert the reference's own test fixtures into small .npz golden files.
 
-Run in a container where the reference tree is mounted (it reads it from
-/root/reference); the GPU machine never needs the reference, only the .npz files
-written here.  Sources:
+Run where the reference tree is available (it reads it from
+/root/reference, or the path given as the first argument); the tests need
+only the .npz files written here.  Sources:
 
 * sucemfem/ProblemConfigurations/tests/LHS_matrix.npy and RHS_vector.pickle
   (test_EMDrivenProblem.py:64-82): InscribedTet, order 1, f=1e8 Hz, ABC,
