@@ -1,7 +1,7 @@
 """Exact (rational) N1curl reference element for the oracle.
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the product imports this module; it
-is the checker that the GPU path is compared against.
+is part of the oracle the GPU path is compared against.
 
 Restates the Nedelec first-kind H(curl) element that the reference obtains
 from FIAT through ``dolfin.FunctionSpace(mesh, "Nedelec 1st kind H(curl)",
