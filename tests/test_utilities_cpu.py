@@ -135,3 +135,21 @@ def test_paths_and_filament_far_field(tmp_path):
     assert abs(eval_E_theta(freq, 0.4, 1.0, th)) == pytest.approx(
         omega * mu0 * 0.4 / (4 * np.pi) * np.sin(th) * abs(np.sin(u) / u), rel=1e-12)
     assert eval_E_theta(freq, 0.4, 1.0, 0.0) == 0
+
+
+def test_voltage_along_line_reference_cases():
+    """sucemfem/Sources/tests/test_postprocessing.py:31-76 with the field
+    given analytically: E = (0, 0, 2z) + j (0, 0, -z^2) between the test's
+    end points gives 1 - j/3, its negative on the reversed paths, and 0
+    along a line in the plane z = 1."""
+    from sucemfem.Sources.PostProcess import VoltageAlongLine
+    re = VoltageAlongLine(lambda x, y, z: np.array([0.0, 0.0, 2 * z]))
+    im = VoltageAlongLine(lambda x, y, z: np.array([0.0, 0.0, -z * z]))
+    cases = [((np.array([0.5, 0.35, 0]), np.array([0.5, 0.5, 1])), 1 - 1j / 3),
+             ((np.array([0, 0, 0.0]), np.array([1, 1, 1.0])), 1 - 1j / 3),
+             ((np.array([0.25, 0.5, 1 - 3e-16]), np.array([0.5, 0.75, 3e-16])), -(1 - 1j / 3)),
+             ((np.array([1, 1, 1.0]), np.array([0, 0, 0.0])), -(1 - 1j / 3)),
+             ((np.array([0, 0, 1.0]), np.array([1, 1, 1.0])), 0.0)]
+    for (a, b), want in cases:
+        got = re.calculate_voltage(a, b) + 1j * im.calculate_voltage(a, b)
+        assert abs(got - want) < 1e-7, (a, b, got, want)
