@@ -254,3 +254,27 @@ def test_complex_voltage_along_line():
         ref = (VoltageAlongLine(oracle_E(0)).calculate_voltage(start, end)
                + 1j * VoltageAlongLine(oracle_E(1)).calculate_voltage(start, end))
     assert abs(got - ref) <= 1e-9 * abs(ref), (got, ref)
+
+
+def test_em_functional_symmetry():
+    """sucemfem/PostProcessing/tests/test_Postprocessing.py:31-52: the
+    functional is symmetric in E and g (UnitCube(2,2,2), order 1, random
+    complex DOFs, random k0); here to round-off, the two sums being taken in
+    different orders."""
+    from sucemfem.mesh import UnitCube
+    from sucemfem.space import FunctionSpace
+    from sucemfem.PostProcessing import CalcEMFunctional
+    V = FunctionSpace(UnitCube(2, 2, 2), order=1)
+    rng = np.random.default_rng(11)
+    E = rng.random(V.n) + 1j * rng.random(V.n)
+    g = rng.random(V.n) + 1j * rng.random(V.n)
+    k0 = rng.random() * 10
+    f = CalcEMFunctional(V)
+    f.set_k0(k0)
+    f.set_g_dofs(g)
+    f.set_E_dofs(E)
+    v1 = f.calc_functional()
+    f.set_g_dofs(E)
+    f.set_E_dofs(g)
+    v2 = f.calc_functional()
+    assert abs(v1 - v2) <= 1e-13 * abs(v1)

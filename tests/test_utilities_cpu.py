@@ -87,6 +87,16 @@ def test_matrix_io_round_trip(tmp_path):
     assert sps.isspmatrix_csr(B) and abs(B - A).max() == 0
     assert np.array_equal(load_scipy_matrix_from_mat(path, "D"), D)
     assert load_scipy_matrix_from_mat(path, "missing") is None
+    # test_MatrixIO.py:52-76: complex sparse and a column vector
+    C = sps.csr_matrix(np.random.default_rng(2).random((30, 20))
+                       + 1j * np.random.default_rng(3).random((30, 20)))
+    save_scipy_matrix_as_mat(path, "C", C)
+    Cl = load_scipy_matrix_from_mat(path, "C")
+    assert np.array_equal(Cl.data, C.data) and np.array_equal(Cl.indices, C.indices)
+    assert np.array_equal(Cl.indptr, C.indptr)
+    col = np.random.default_rng(4).random((50, 1))
+    save_scipy_matrix_as_mat(path, "col", col)
+    assert np.array_equal(load_scipy_matrix_from_mat(path, "col"), col)
 
 
 def test_romberg_against_quadrature():
