@@ -348,10 +348,12 @@ def basis_at(coords, cells, order, c, p):
     return Nh @ Jinv[0]          # rows: J^-T N_hat  == N_hat^T J^-1
 
 
-def point_source_contrib(coords, cells, order, topo, dm, p, value, choose=min):
+def point_source_contrib(coords, cells, order, topo, dm, p, value, choose=min, cands=None):
     """point_source.py:49-94: (dofnos, N_i(p).value) for the cell chosen by
-    ``choose`` among the cells that contain p."""
-    cands = locate_cells(coords, cells, p)[0]
+    ``choose`` among the cells that contain p (``cands``: those cells, when
+    already located)."""
+    if cands is None:
+        cands = locate_cells(coords, cells, p)[0]
     if len(cands) == 0:
         raise ValueError("source point outside the mesh")
     c = int(choose(cands))
@@ -371,8 +373,9 @@ def fillament_contrib(coords, cells, order, topo, dm, endpoints, I, npts, choose
         pts = start + delta * np.linspace(0, 1, npts)[:, None]
     mag = vec * L / npts
     contribs = {}
-    for p in pts:
-        d, v = point_source_contrib(coords, cells, order, topo, dm, p, mag, choose)
+    located = locate_cells(coords, cells, np.atleast_2d(pts))   # one geometry pass
+    for p, cands in zip(pts, located):
+        d, v = point_source_contrib(coords, cells, order, topo, dm, p, mag, choose, cands)
         for dn, vv in zip(d, v):
             contribs[int(dn)] = contribs.get(int(dn), 0.0) + vv
     dn = np.array(sorted(contribs))

@@ -299,6 +299,7 @@ def reference_tensors(order):
     return {"mass": mass, "curl": cc, "face": np.array(faces)}
 
 
+@lru_cache(maxsize=None)
 def basis_lambdas(order):
     """numpy-callable reference basis values and curls: f(x,y,z) -> list."""
     B = basis(order)
