@@ -3,7 +3,9 @@
 // sparsity pass: sucemfem/ProblemConfigurations/EMProblem.py:100-105,
 // sucemfem/SystemMatrices.py:54).
 //
-// Numbering rules (kept identical to DOLFIN so DOF numbers are bit-exact):
+// Numbering rules (DOLFIN's, so the DOF numbers of orders 1 and 2 are
+// bit-exact with the reference's; orders 3 and 4 keep the same entity-major
+// layout, their per-entity order being the element's DOF order):
 //  * each cell's vertices are sorted by global index (mesh ordering);
 //  * edges and faces are numbered by first encounter while walking the cells
 //    in order and each cell's local entities in UFC order;
