@@ -321,6 +321,14 @@ int sucem_lu_perturbed(sucem_lu* lu);
  * counterpart (measurement hook). */
 int sucem_lu_kernel_stats(sucem_lu* lu, double* out);
 
+/* Self-test of the device-side failure detection: one thread of a one-block
+ * kernel waits, with the tensor-core kernel's bounded mbarrier wait limited
+ * to `polls` polls, for a barrier phase nothing completes; *gave_up = 1
+ * when the wait ran out and the kernel returned (the expected outcome; the
+ * CUDA context stays usable).  Synchronous on the default stream.  No
+ * reference counterpart (the reference has no device code). */
+int sucem_selftest_bounded_wait(int polls, int* gave_up);
+
 #ifdef __cplusplus
 }
 #endif

@@ -137,6 +137,13 @@ int sucem_lu_solve(sucem_lu* lu, int io_dtype, const void* b, void* x, void* str
 
 int sucem_lu_perturbed(sucem_lu* lu) { return lu ? sucem::mf_perturbed(*lu->h) : 0; }
 
+int sucem_selftest_bounded_wait(int polls, int* gave_up) {
+  if (!gave_up || polls < 1) return fail("gave_up must be non-null and polls >= 1", SUCEM_ERR_ARG);
+  cudaError_t e = sucem::mf_wait_selftest(polls, gave_up);
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_selftest_bounded_wait");
+  return SUCEM_OK;
+}
+
 int sucem_lu_kernel_stats(sucem_lu* lu, double* out) {
   if (!lu || !out) return fail("null argument", SUCEM_ERR_ARG);
   sucem::mf_tc_stats(*lu->h, out);

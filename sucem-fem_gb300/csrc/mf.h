@@ -72,4 +72,7 @@ int mf_perturbed(MFHandle& h);
 // out[1] their summed event-timed duration (ms), out[2] algorithmic flops
 void mf_tc_stats(MFHandle& h, double* out);
 void mf_free(MFHandle& h);
+// self-test of the bounded mbarrier wait of the tensor-core kernel:
+// *gave_up = 1 when a wait nothing arrives at ran out after `polls` polls
+cudaError_t mf_wait_selftest(int polls, int* gave_up);
 }  // namespace sucem

@@ -170,6 +170,18 @@ struct DNode {
 
 #include "mf_tc.cuh"
 
+// Self-test of the bounded mbarrier wait the tensor-core kernel relies on:
+// one thread initialises a barrier that nothing will arrive at and waits
+// for its first phase with the kernel's own wait, limited to `polls`; the
+// wait must give up (status 1) and the kernel must return normally.
+__global__ void wait_selftest_kernel(int polls, int* __restrict__ status) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc::smem_u32(&bar)));
+  const bool done = tc::wait_parity(tc::smem_u32(&bar), 0, false, polls);
+  *status = done ? 0 : 1;
+}
+
 // ---- factor kernels ----
 template <typename S>
 __global__ void scatter_kernel(int64_t m, const int32_t* __restrict__ src,
@@ -1549,5 +1561,24 @@ void mf_delete(MFHandle* h) {
   delete h;
 }
 MFSymbolic& mf_sym(MFHandle* h) { return h->sym; }
+
+// the bounded-wait self-test (wait_selftest_kernel): *gave_up = 1 when the
+// wait ran out as it must
+cudaError_t mf_wait_selftest(int polls, int* gave_up) {
+  int* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(int));
+  if (e != cudaSuccess) return e;
+  int h = -1;
+  e = cudaMemcpy(d, &h, sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    wait_selftest_kernel<<<1, 32>>>(polls, d);
+    count_launch(1);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  *gave_up = h;
+  return e;
+}
 
 }  // namespace sucem

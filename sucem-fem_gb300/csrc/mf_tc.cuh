@@ -103,10 +103,12 @@ __device__ __forceinline__ void arrive(uint32_t bar) {
 }
 
 // bounded wait for the phase with the given parity; with backoff, a failed
-// poll sleeps briefly (for waiters that are not on the critical path)
-__device__ __forceinline__ bool wait_parity(uint32_t bar, uint32_t parity, bool backoff = false) {
+// poll sleeps briefly (for waiters that are not on the critical path);
+// false after `limit` failed polls
+__device__ __forceinline__ bool wait_parity(uint32_t bar, uint32_t parity, bool backoff = false,
+                                            int limit = kWaitLimit) {
   uint32_t done = 0;
-  for (int it = 0; it < kWaitLimit; ++it) {
+  for (int it = 0; it < limit; ++it) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}\n"

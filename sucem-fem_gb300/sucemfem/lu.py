@@ -16,6 +16,8 @@ _native.declare("sucem_lu_destroy", None, [c_vp])
 _native.declare("sucem_lu_info", ctypes.c_int, [c_vp, c_vp])
 _native.declare("sucem_lu_copy_perm", ctypes.c_int, [c_vp, c_vp])
 _native.declare("sucem_lu_fronts", ctypes.c_int, [c_vp, c_vp])
+_native.declare("sucem_selftest_bounded_wait", ctypes.c_int,
+                [ctypes.c_int, ctypes.POINTER(ctypes.c_int)])
 _native.declare("sucem_lu_factor", ctypes.c_int, [c_vp, ctypes.c_int, c_vp, ctypes.c_double, c_vp])
 _native.declare("sucem_lu_solve", ctypes.c_int, [c_vp, ctypes.c_int, c_vp, c_vp, c_vp])
 _native.declare("sucem_lu_perturbed", ctypes.c_int, [c_vp])
@@ -84,6 +86,15 @@ class SparseLU:
              stream if stream is not None else _device.stream_ptr())
         self.dtype = dtype
         return self
+
+    @staticmethod
+    def selftest_bounded_wait(polls=2000):
+        """True when a device wait that nothing completes gives up after
+        ``polls`` polls and its kernel returns (the failure detection of the
+        tensor-core update)."""
+        out = ctypes.c_int(-1)
+        call("sucem_selftest_bounded_wait", int(polls), ctypes.byref(out))
+        return out.value == 1
 
     def perturbed(self):
         """Number of replaced (perturbed) pivots of the last factorisation."""

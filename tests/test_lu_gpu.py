@@ -84,3 +84,13 @@ def test_lu_real_indefinite(dtype):
     x = lu.solve(torch.as_tensor(b, device=_device.device())).cpu().numpy()
     res = np.linalg.norm(M @ x - b) / np.linalg.norm(b)
     assert res < (1e-3 if dtype == "f32" else 1e-11), res
+
+
+def test_bounded_wait_gives_up_and_the_context_stays_usable():
+    """Failure detection without a fault: a device wait on a barrier phase
+    that nothing completes (the tensor-core kernel's own bounded wait, here
+    limited to 2000 polls) gives up and its kernel returns; afterwards the
+    same process factorises and solves as usual."""
+    from sucemfem.lu import SparseLU
+    assert SparseLU.selftest_bounded_wait(2000)
+    test_lu_driven(2, "c64", "cells")
