@@ -165,7 +165,10 @@ int sucem_compact_fill(const sucem_space* sp, int dtype, const void* vals,
  * rows; larger matrices get SUCEM_ERR_ARG with a message.  The first call on
  * a device looks up the array's device address (make that first call before
  * any stream capture).  Every call shares the one array: calls that overlap
- * on the GPU (other streams, other threads) race and must be serialised. */
+ * on the GPU (other streams, other threads) race and must be serialised.
+ * The device address looked up on the first call is cached for the life of
+ * the process; it is not refreshed after cudaDeviceReset, so do not call
+ * this entry point on a device that the process has reset. */
 int sucem_compact_count_noalloc(const sucem_space* sp, int dtype, const void* vals,
                                 int32_t* out_indptr, void* stream);
 
@@ -315,6 +318,18 @@ int sucem_lu_fronts(const sucem_lu* lu, int64_t* out);
 int sucem_lu_factor(sucem_lu* lu, int dtype, const void* vals, double pivot_tol, void* stream);
 int sucem_lu_solve(sucem_lu* lu, int io_dtype, const void* b, void* x, void* stream);
 int sucem_lu_perturbed(sucem_lu* lu);
+/* Waits for the last factorisation and reports whether it can be used:
+ * SUCEM_OK, or SUCEM_ERR_STATE when it was not factored or when a bounded
+ * wait of its tensor-core update gave up (the factor is then invalid, and
+ * sucem_lu_solve refuses it with the same error).  No reference counterpart:
+ * dolfin.LUSolver / UMFPACK report no such device-side failure
+ * (EMVectorWaveEigenproblem.py:76-79, LinalgSolvers.py:262-277). */
+int sucem_lu_status(sucem_lu* lu);
+/* Test hook, no reference counterpart: marks the last factorisation as if a
+ * bounded wait of its tensor-core update had given up (a host write of the
+ * device flag; no kernel is made to fail), so that tests can check that
+ * sucem_lu_status and sucem_lu_solve refuse the factor. */
+int sucem_lu_inject_timeout(sucem_lu* lu);
 /* Tensor-core Schur-update launches of the last complex64 factorisation
  * (waits for them): out[3] = {launches, summed event-timed duration in ms,
  * algorithmic flops (8 per complex multiply-add)}.  No reference

@@ -571,20 +571,22 @@ int sucem_compact_count(const sucem_space* sp, int dtype, const void* vals, int3
   const sucem::DeviceSpace* d = dev_of(sp);
   if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
   if (!vals || !out_indptr || !work) return fail("null argument", SUCEM_ERR_ARG);
+  if (dtype != SUCEM_C64 && dtype != SUCEM_C128)
+    return fail("compaction needs a complex dtype", SUCEM_ERR_ARG);
   cudaStream_t s = (cudaStream_t)stream;
   const int threads = 256;
   const unsigned blocks = (unsigned)((d->n * 32 + threads - 1) / threads);
-  if (dtype == SUCEM_C64)
+  // no rows: no count launch (a zero-block grid is a launch error); the
+  // scan still writes out_indptr[0] = 0
+  if (d->n > 0 && dtype == SUCEM_C64)
     sucem::count_nonzero_kernel<float><<<blocks, threads, 0, s>>>(d->n, d->indptr,
                                                                   (const float*)vals, work);
-  else if (dtype == SUCEM_C128)
+  else if (d->n > 0)
     sucem::count_nonzero_kernel<double><<<blocks, threads, 0, s>>>(d->n, d->indptr,
                                                                    (const double*)vals, work);
-  else
-    return fail("compaction needs a complex dtype", SUCEM_ERR_ARG);
   sucem::scan_kernel<<<1, 1024, 0, s>>>(d->n, work, out_indptr);
   cudaError_t e = cudaGetLastError();
-  sucem::count_launch(2);
+  sucem::count_launch(d->n > 0 ? 2 : 1);
   return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_compact_count");
 }
 
@@ -593,6 +595,7 @@ int sucem_compact_fill(const sucem_space* sp, int dtype, const void* vals,
                        void* stream) {
   const sucem::DeviceSpace* d = dev_of(sp);
   if (!d) return fail("space is not on a device", SUCEM_ERR_STATE);
+  if (d->n == 0) return SUCEM_OK;  // nothing to fill
   cudaStream_t s = (cudaStream_t)stream;
   const int threads = 256;
   const unsigned blocks = (unsigned)((d->n * 32 + threads - 1) / threads);
@@ -634,6 +637,8 @@ std::mutex g_noalloc_mutex;
 // Device address of the array for the current device.  In host code the
 // array's name is only a host-side stand-in, so the address must come from
 // cudaGetSymbolAddress, looked up once per device with that device current.
+// The cached address is not refreshed after cudaDeviceReset: a process that
+// resets a device must not call the allocation-free entry point on it again.
 int noalloc_scratch(int32_t** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -674,14 +679,16 @@ extern "C" int sucem_compact_count_noalloc(const sucem_space* sp, int dtype, con
   cudaStream_t s = (cudaStream_t)stream;
   const int threads = 256;
   const unsigned blocks = (unsigned)((d->n * 32 + threads - 1) / threads);
-  if (dtype == SUCEM_C64)
+  // no rows: skip the count launch (a zero-block grid is a launch error);
+  // the scan still writes out_indptr[0] = 0
+  if (d->n > 0 && dtype == SUCEM_C64)
     sucem::count_nonzero_kernel<float><<<blocks, threads, 0, s>>>(d->n, d->indptr,
                                                                   (const float*)vals, counts);
-  else
+  else if (d->n > 0)
     sucem::count_nonzero_kernel<double><<<blocks, threads, 0, s>>>(d->n, d->indptr,
                                                                    (const double*)vals, counts);
   sucem::scan_kernel<<<1, 1024, 0, s>>>(d->n, counts, out_indptr);
   cudaError_t e = cudaGetLastError();
-  sucem::count_launch(2);
+  sucem::count_launch(d->n > 0 ? 2 : 1);
   return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_compact_count_noalloc");
 }

@@ -127,6 +127,11 @@ int sucem_lu_factor(sucem_lu* lu, int dtype, const void* vals, double pivot_tol,
 
 int sucem_lu_solve(sucem_lu* lu, int io_dtype, const void* b, void* x, void* stream) {
   if (!lu || !b || !x) return fail("null argument", SUCEM_ERR_ARG);
+  // the first solve after a factorisation waits for it and refuses a factor
+  // whose tensor-core update gave up waiting (its flag is device-side)
+  if (sucem::mf_factor_status(*lu->h) == -1)
+    return fail("the factorisation is invalid: a bounded wait of its tensor-core update gave up",
+                SUCEM_ERR_STATE);
   cudaError_t e = sucem::mf_solve(*lu->h, io_dtype, b, x, (cudaStream_t)stream);
   if (e == cudaErrorNotReady) return fail("factor before solving", SUCEM_ERR_STATE);
   if (e == cudaErrorInvalidValue)
@@ -136,6 +141,24 @@ int sucem_lu_solve(sucem_lu* lu, int io_dtype, const void* b, void* x, void* str
 }
 
 int sucem_lu_perturbed(sucem_lu* lu) { return lu ? sucem::mf_perturbed(*lu->h) : 0; }
+
+int sucem_lu_status(sucem_lu* lu) {
+  if (!lu) return fail("null argument", SUCEM_ERR_ARG);
+  const int st = sucem::mf_factor_status(*lu->h);
+  if (st == -2) return fail("not factored (or the factorisation failed)", SUCEM_ERR_STATE);
+  if (st == -1)
+    return fail("the factorisation is invalid: a bounded wait of its tensor-core update gave up",
+                SUCEM_ERR_STATE);
+  return SUCEM_OK;
+}
+
+int sucem_lu_inject_timeout(sucem_lu* lu) {
+  if (!lu) return fail("null argument", SUCEM_ERR_ARG);
+  cudaError_t e = sucem::mf_mark_timed_out(*lu->h);
+  if (e == cudaErrorNotReady) return fail("factor before injecting", SUCEM_ERR_STATE);
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_lu_inject_timeout");
+  return SUCEM_OK;
+}
 
 int sucem_selftest_bounded_wait(int polls, int* gave_up) {
   if (!gave_up || polls < 1) return fail("gave_up must be non-null and polls >= 1", SUCEM_ERR_ARG);

@@ -68,6 +68,13 @@ struct MFHandle;
 cudaError_t mf_factor(MFHandle& h, int dtype, const void* vals, double tau, cudaStream_t st);
 cudaError_t mf_solve(MFHandle& h, int io_dtype, const void* b, void* x, cudaStream_t st);
 int mf_perturbed(MFHandle& h);
+// 0: the last factorisation is usable; -1: a bounded wait of its
+// tensor-core update gave up (invalid factor); -2: not factored or a CUDA
+// error.  Waits for the factorisation the first time it is asked.
+int mf_factor_status(MFHandle& h);
+// host-side failure injection for tests: marks the last factorisation as if
+// a bounded wait of its tensor-core update had given up
+cudaError_t mf_mark_timed_out(MFHandle& h);
 // tensor-core update launches of the last factorisation: out[0] launches,
 // out[1] their summed event-timed duration (ms), out[2] algorithmic flops
 void mf_tc_stats(MFHandle& h, double* out);

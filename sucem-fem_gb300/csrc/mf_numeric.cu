@@ -945,6 +945,12 @@ struct MFDevice {
   std::vector<MFLevel> levels;
   bool factored = false;
   int perturbed = 0;
+  // end of the last factorisation on its stream; the first solve after it
+  // waits for it and reads d_flag once (a factor whose tensor-core wait gave
+  // up is refused)
+  cudaEvent_t factor_ev = nullptr;
+  bool checked = false;
+  bool valid = true;
   // cuBLAS handle for the single-precision Schur updates of the top levels
   cublasHandle_t blas = nullptr;
   cublasComputeType_t blas_compute = CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
@@ -993,6 +999,7 @@ void free_dev(MFDevice& d) {
   if (d.solve_exec) cudaGraphExecDestroy(d.solve_exec);
   for (cudaEvent_t ev : d.tc_ev) cudaEventDestroy(ev);
   if (d.cap_stream) cudaStreamDestroy(d.cap_stream);
+  if (d.factor_ev) cudaEventDestroy(d.factor_ev);
   d = MFDevice();
 }
 
@@ -1514,7 +1521,40 @@ cudaError_t mf_factor(MFHandle& h, int dtype, const void* vals, double tau, cuda
     case SUCEM_C128: e = factor_t<double2>(h, vals, tau, st); break;
     default: return cudaErrorInvalidValue;
   }
-  h.dev.factored = e == cudaSuccess;
+  MFDevice& d = h.dev;
+  if (e == cudaSuccess && !d.factor_ev) e = cudaEventCreateWithFlags(&d.factor_ev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventRecord(d.factor_ev, st);
+  d.factored = e == cudaSuccess;
+  d.checked = false;
+  d.valid = true;
+  return e;
+}
+
+// waits for the last factorisation (once per factorisation) and reads its
+// flags: 0 = usable, -1 = a bounded wait of its tensor-core update gave up
+// (the factor is invalid), -2 = not factored / CUDA error
+int mf_factor_status(MFHandle& h) {
+  MFDevice& d = h.dev;
+  if (!d.factored || !d.d_flag) return -2;
+  if (!d.checked) {
+    int v[2] = {0, 0};
+    if (cudaEventSynchronize(d.factor_ev) != cudaSuccess ||
+        cudaMemcpy(v, d.d_flag, sizeof(v), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return -2;
+    d.perturbed = v[0];
+    d.valid = v[1] == 0;
+    d.checked = true;
+  }
+  return d.valid ? 0 : -1;
+}
+
+cudaError_t mf_mark_timed_out(MFHandle& h) {
+  MFDevice& d = h.dev;
+  if (!d.factored || !d.d_flag) return cudaErrorNotReady;
+  const int one = 1;
+  cudaError_t e = cudaEventSynchronize(d.factor_ev);
+  if (e == cudaSuccess) e = cudaMemcpy(d.d_flag + 1, &one, sizeof(int), cudaMemcpyHostToDevice);
+  d.checked = false;
   return e;
 }
 
@@ -1532,10 +1572,10 @@ cudaError_t mf_solve(MFHandle& h, int io_dtype, const void* b, void* x, cudaStre
 }
 
 int mf_perturbed(MFHandle& h) {
-  int v[2] = {0, 0};
-  if (h.dev.d_flag) cudaMemcpy(v, h.dev.d_flag, sizeof(v), cudaMemcpyDeviceToHost);
+  const int st = mf_factor_status(h);
+  if (st == -2) return 0;
   // d_flag[1]: a bounded wait of the tensor-core update gave up
-  return v[1] ? -1 : v[0];
+  return st < 0 ? -1 : h.dev.perturbed;
 }
 
 void mf_tc_stats(MFHandle& h, double* out) {

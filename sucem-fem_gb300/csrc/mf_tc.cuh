@@ -183,7 +183,8 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
   uint64_t* empty = full + STAGES;
   uint64_t* acc_full = empty + STAGES;
   uint64_t* acc_empty = acc_full + 2;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+  uint64_t* drain = acc_empty + 2;  // give-up path: completion of issued MMAs
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
   volatile int* fail = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -197,6 +198,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_full[b])));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(smem_u32(&acc_empty[b])));
     }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(drain)));
     *fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
@@ -331,6 +333,13 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
         if (!ok) break;
         commit(smem_u32(&acc_full[b]));
         if (*fail) ok = false;
+      }
+      if (!ok) {
+        // giving up: MMAs already issued may still be writing TMEM, which is
+        // freed after the final barrier; track them all with one more commit
+        // and wait (bounded) until they have completed
+        commit(smem_u32(drain));
+        wait_parity(smem_u32(drain), 0);
       }
     }
     __syncwarp();

@@ -262,10 +262,15 @@ class UMFPACKSolver(SystemSolverBase):
 
 
 class PyAMGSolver(SystemSolverBase):
+    """The reference's optional algebraic-multigrid solver runs pyamg on the
+    host.  This library solves on the GPU only, so it refuses instead of
+    falling back to a CPU solve; use UMFPACKSolver (GPU LU) or the Krylov
+    solvers."""
+
     def _call_solver(self):
-        import pyamg  # optional, as in the reference
-        x = pyamg.solve(self._A, self._b, verb=True, tol=1e-8, maxiter=800)
-        return x, 0
+        raise NotImplementedError(
+            "PyAMGSolver is a CPU (pyamg) solver and this build has no CPU fallback; "
+            "use UMFPACKSolver, BiCGStabSolver or GMRESSolver")
 
 
 def calculate_residual(A, x, b):

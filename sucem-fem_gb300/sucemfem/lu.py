@@ -22,6 +22,8 @@ _native.declare("sucem_lu_factor", ctypes.c_int, [c_vp, ctypes.c_int, c_vp, ctyp
 _native.declare("sucem_lu_solve", ctypes.c_int, [c_vp, ctypes.c_int, c_vp, c_vp, c_vp])
 _native.declare("sucem_lu_perturbed", ctypes.c_int, [c_vp])
 _native.declare("sucem_lu_kernel_stats", ctypes.c_int, [c_vp, c_vp])
+_native.declare("sucem_lu_status", ctypes.c_int, [c_vp])
+_native.declare("sucem_lu_inject_timeout", ctypes.c_int, [c_vp])
 
 DTYPES = {"f32": _native.F32, "f64": _native.F64, "c64": _native.C64, "c128": _native.C128}
 
@@ -95,6 +97,17 @@ class SparseLU:
         out = ctypes.c_int(-1)
         call("sucem_selftest_bounded_wait", int(polls), ctypes.byref(out))
         return out.value == 1
+
+    def check(self):
+        """Wait for the last factorisation and raise RuntimeError when it
+        cannot be used (a bounded wait of its tensor-core update gave up)."""
+        call("sucem_lu_status", self._h)
+        return self
+
+    def _inject_timeout(self):
+        """Test hook: mark the last factorisation as if its tensor-core
+        update had given up waiting (host write of the device flag)."""
+        call("sucem_lu_inject_timeout", self._h)
 
     def perturbed(self):
         """Number of replaced (perturbed) pivots of the last factorisation."""

@@ -1,8 +1,7 @@
 """Convert the reference's own test fixtures into small .npz golden files.
 
-Run where the reference tree is available (it reads it from
-/root/reference, or the path given as the first argument); the tests need
-only the .npz files written here.  Sources:
+Run where the reference tree is available, with its path as the only
+argument; the tests need only the .npz files written here.  Sources:
 
 * sucemfem/ProblemConfigurations/tests/LHS_matrix.npy and RHS_vector.pickle
   (test_EMDrivenProblem.py:64-82): InscribedTet, order 1, f=1e8 Hz, ABC,
@@ -34,7 +33,9 @@ import sys
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python make_golden.py <path of the reference checkout>")
+REF = sys.argv[1]
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 

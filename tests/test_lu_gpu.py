@@ -94,3 +94,30 @@ def test_bounded_wait_gives_up_and_the_context_stays_usable():
     from sucemfem.lu import SparseLU
     assert SparseLU.selftest_bounded_wait(2000)
     test_lu_driven(2, "c64", "cells")
+
+
+def test_timed_out_factor_is_refused_until_refactored():
+    """A factorisation whose tensor-core update gave up waiting must not be
+    used: the failure is injected on the host (the device flag is written,
+    no kernel is made to fail); the status check and every later solve then
+    raise, and a fresh factorisation clears it."""
+    import torch
+    from sucemfem import _device
+    from sucemfem.lu import SparseLU
+    coords, cells, L, _ = _problem(1)
+    V = _space(coords, cells, 1)
+    vals = torch.as_tensor(_values_on_pattern(V, L), device=_device.device()).to(torch.complex64)
+    lu = SparseLU(V.indptr, V.indices, leaf_size=32, cells=(V.cell_dofs, coords[V.cells].mean(1)))
+    b = torch.ones(V.n, dtype=torch.complex128, device=_device.device())
+    lu.factor(vals, "c64").check()
+    lu._inject_timeout()
+    with pytest.raises(RuntimeError, match="gave up"):
+        lu.check()
+    with pytest.raises(RuntimeError, match="gave up"):
+        lu.solve(b)
+    with pytest.raises(RuntimeError, match="gave up"):
+        lu.perturbed()
+    lu.factor(vals, "c64")
+    x = lu.solve(b).cpu().numpy()
+    res = np.linalg.norm(L @ x - b.cpu().numpy()) / np.linalg.norm(b.cpu().numpy())
+    assert res < 1e-4

@@ -87,10 +87,14 @@ def test_femmesh_reader_rejects_bad_files(tmp_path, bad):
         FemmeshReader(str(p)).read_meshfile()
 
 
-SANDBOX = "/root/reference/sandbox/solvers/meshes/sphere-r1m-4.femmesh"
+# the reference checkout is optional test data: point SUCEM_REFERENCE_ROOT
+# at it to run this case
+_REF = os.environ.get("SUCEM_REFERENCE_ROOT", "")
+SANDBOX = os.path.join(_REF, "sandbox/solvers/meshes/sphere-r1m-4.femmesh") if _REF else ""
 
 
-@pytest.mark.skipif(not os.path.exists(SANDBOX), reason="reference sandbox meshes not present")
+@pytest.mark.skipif(not SANDBOX or not os.path.exists(SANDBOX),
+                    reason="SUCEM_REFERENCE_ROOT not set or its sandbox meshes not present")
 def test_reference_sandbox_sphere_mesh():
     """One of the reference's own sphere meshes (read in place, not copied):
     block counts as declared (242 nodes, 659 tetrahedra), nodes on or inside
