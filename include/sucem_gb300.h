@@ -81,7 +81,16 @@ int sucem_space_sizes(const sucem_space* sp, int64_t* out);
                                        centroid) */
 #define SUCEM_COPY_BOUNDARY_DUAL 11 /* double[n_boundary_dofs*6] dual functional of each boundary
                                        DOF: point, tangent (DOF(u) = u(point).tangent) */
+#define SUCEM_COPY_TASK_ENT 12     /* int32[n_tasks*32] assembly schedule: entity of each lane */
+#define SUCEM_COPY_TASK_META 13    /* int32[n_tasks*4] first step block, steps per local entity
+                                      index (8 bytes), flags (bit 0: faces) */
+#define SUCEM_COPY_STEP_WORDS 14   /* uint32[n_step_blocks*(1+slot_planes)*32] step blocks */
 int sucem_space_copy(const sucem_space* sp, int what, void* host_dst);
+
+/* Sizes of the order-1/2 assembly schedule (the kernel's work plan; no
+ * reference counterpart, exposed so that tests can check it on the host):
+ * out[4] = {n_tasks, n_tasks_interior, n_step_blocks, slot_planes}. */
+int sucem_space_schedule_sizes(const sucem_space* sp, int64_t* out);
 
 /* Copies the space to CUDA device `device` (idempotent). */
 int sucem_space_upload(sucem_space* sp, int device);

@@ -17,7 +17,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 
 CU = ["abi.cu", "assemble.cu", "linalg.cu"]
-CPP = ["space.cpp", "mf_symbolic.cpp"]
+CPP = ["space.cpp", "schedule.cpp", "mf_symbolic.cpp"]
 
 
 def _sources():
@@ -37,8 +37,9 @@ def build(verbose=False, force=False):
     os.makedirs(BUILD, exist_ok=True)
     tables = os.path.join(CSRC, "n1curl_tables.h")
     tables_hi = os.path.join(CSRC, "n1curl_tables_hi.h")
-    if not os.path.exists(tables) or not os.path.exists(tables_hi):
-        _run([sys.executable, os.path.join(CSRC, "gen_tables.py"), tables, tables_hi])
+    contract = os.path.join(CSRC, "n1curl_contract.h")
+    if not all(os.path.exists(p) for p in (tables, tables_hi, contract)):
+        _run([sys.executable, os.path.join(CSRC, "gen_tables.py"), tables, tables_hi, contract])
     srcs = _sources()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
     headers.append(os.path.join(ROOT, "include", "sucem_gb300.h"))

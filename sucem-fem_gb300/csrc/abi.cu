@@ -62,7 +62,8 @@ void free_device_space(DeviceSpace* d) {
                   d->cell_dofs, d->boundary_dofs, d->kc_f, d->km_f, d->kt_f,
                   d->kc_d,    d->km_d,    d->kt_d, d->bidx, d->g_f, d->g_d, d->h_f, d->h_d,
                   d->kab_f, d->kab_d, d->ext_facets, d->ntff_pts, d->bdof_pt,
-                  d->bin_ptr, d->bin_cells, d->cell_pos};
+                  d->bin_ptr, d->bin_cells, d->cell_pos, d->task_ent, d->task_meta,
+                  d->step_words};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   cudaSetDevice(prev);
@@ -149,9 +150,6 @@ std::string upload_space(Space& s, int device) {
   UP(xyz_lo, lo.data(), (size_t)s.nv);
   UP(xyz, s.coords.data(), (size_t)s.nv * 3);
   UP(ext_mask, s.ext_mask.data(), (size_t)s.nt);
-  UP(ent_ptr, s.ent_ptr.data(), s.ent_ptr.size());
-  UP(inc_cell, s.inc_cell.data(), s.inc_cell.size());
-  UP(inc_rec, s.inc_rec.data(), s.inc_rec.size());
   UP(indptr, indptr32.data(), indptr32.size());
   UP(indices, s.indices.data(), s.indices.size());
   UP(cell_dofs, s.cell_dofs.data(), s.cell_dofs.size());
@@ -166,6 +164,12 @@ std::string upload_space(Space& s, int device) {
   UP(kab_d, kab.data(), kab.size());
   UP(bidx, bidx.data(), bidx.size());
   UP(cell_pos, s.cell_pos.data(), s.cell_pos.size());
+  UP(task_ent, s.task_ent.data(), s.task_ent.size());
+  UP(task_meta, reinterpret_cast<const int4*>(s.task_meta.data()), s.task_meta.size() / 4);
+  UP(step_words, s.step_words.data(), s.step_words.size());
+  d->n_tasks = s.n_tasks;
+  d->n_tasks_interior = s.n_tasks_interior;
+  d->slot_planes = s.slot_planes;
   d->nb = nb;
 #undef UP
   d->n_boundary = (int64_t)s.boundary_dofs.size();
@@ -229,6 +233,16 @@ int sucem_space_sizes(const sucem_space* sp, int64_t* out) {
   return SUCEM_OK;
 }
 
+int sucem_space_schedule_sizes(const sucem_space* sp, int64_t* out) {
+  if (!sp || !out) return fail("null argument", SUCEM_ERR_ARG);
+  const sucem::Space& s = sp->s;
+  out[0] = s.n_tasks;
+  out[1] = s.n_tasks_interior;
+  out[2] = s.slot_planes ? (int64_t)s.step_words.size() / ((1 + s.slot_planes) * 32) : 0;
+  out[3] = s.slot_planes;
+  return SUCEM_OK;
+}
+
 int sucem_space_copy(const sucem_space* sp, int what, void* dst) {
   if (!sp || !dst) return fail("null argument", SUCEM_ERR_ARG);
   const sucem::Space& s = sp->s;
@@ -248,6 +262,9 @@ int sucem_space_copy(const sucem_space* sp, int what, void* dst) {
     case SUCEM_COPY_CELL_EDGES: return cp(s.cell_edges.data(), s.cell_edges.size() * 4);
     case SUCEM_COPY_CELL_FACES: return cp(s.cell_faces.data(), s.cell_faces.size() * 4);
     case SUCEM_COPY_DOF_XYZ: return cp(s.dof_xyz.data(), s.dof_xyz.size() * 8);
+    case SUCEM_COPY_TASK_ENT: return cp(s.task_ent.data(), s.task_ent.size() * 4);
+    case SUCEM_COPY_TASK_META: return cp(s.task_meta.data(), s.task_meta.size() * 4);
+    case SUCEM_COPY_STEP_WORDS: return cp(s.step_words.data(), s.step_words.size() * 4);
     case SUCEM_COPY_BOUNDARY_DUAL: {
       if (s.order > 2) return fail("boundary dual functionals: basis orders 1 and 2 only", SUCEM_ERR_ARG);
       std::vector<double> pt;

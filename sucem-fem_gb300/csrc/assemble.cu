@@ -1,22 +1,21 @@
-// Row-gather assembly of the N1curl curl-curl (S), mass (T) and first-order
-// ABC (B) matrices, the GPU replacement of dolfin.assemble for the forms of
+// Assembly of the N1curl curl-curl (S), mass (T) and first-order ABC (B)
+// matrices, the GPU replacement of dolfin.assemble for the forms of
 // sucemfem/Forms.py:71-85 and sucemfem/BoundaryConditions/ABC.py:56-57.
 // Orders 3 and 4 (45 and 84 DOFs per cell) use assemble_cells_kernel below
-// instead of the row kernel.
+// instead of the entity kernel.
 //
 // Two kernels (orders 1-2):
 //  1. cell_geometry_kernel (one thread per cell) writes the cell's 12 metric
-//     coefficients (6 for S, 6 for T, already scaled by 1/mu_r, eps_r) and,
-//     for cells with exterior facets, 3 tangential coefficients per facet.
-//  2. assemble_rows_kernel: one warp owns one mesh entity (an edge, or for
-//     order 2 also a face) and therefore the dofs_per_entity CSR rows that
-//     share its column list.  Lanes map to the columns of the incident
-//     cells (order 2: one cell per step; order 1: five), contract the cell
-//     coefficients with the reference tensors held in shared memory for
-//     the entity's rows, and add the values into shared-memory row
-//     accumulators at the precomputed column slots.  Each CSR value is then
-//     written exactly once with coalesced stores: no zero-fill pass, no
-//     atomics and a fixed summation order (bit-reproducible run to run).
+//     coefficients (6 for S, 6 for T, already scaled by 1/mu_r, eps_r, and
+//     for the fused complex matrix the T part by -k0^2) and, for cells with
+//     exterior facets, 3 tangential coefficients per facet (scaled by k0 for
+//     the fused matrix).
+//  2. assemble_entities_kernel: one lane owns one mesh entity (an edge, or
+//     for order 2 also a face) and therefore the dofs_per_entity CSR rows
+//     that share its column list; a warp takes 32 of them (see the kernel).
+//     Each CSR value is written exactly once with coalesced stores: no
+//     zero-fill pass, no atomics and a fixed summation order
+//     (bit-reproducible run to run).
 //
 // Element formulas (affine tet, J = [x1-x0 | x2-x0 | x3-x0], covariant
 // Piola N = J^-T N_hat):
@@ -34,13 +33,12 @@
 #include <cstdio>
 
 #include "device.h"
+#include "n1curl_contract.h"
 
 namespace sucem {
 void count_launch(int k);
 
 namespace {
-
-constexpr int kWarps = 8;  // warps per block of the row kernel
 
 template <typename Real>
 struct Cplx;
@@ -97,7 +95,8 @@ __global__ void cell_geometry_kernel(int64_t nt, const int4* __restrict__ cells,
                                      const int32_t* __restrict__ bidx,
                                      const Real* __restrict__ eps_r,
                                      const Real* __restrict__ mu_inv, Real* __restrict__ g,
-                                     Real* __restrict__ h, bool with_b) {
+                                     Real* __restrict__ h, bool with_b, Real tscale,
+                                     Real hscale) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nt) return;
   const int4 v = __ldg(&cells[c]);
@@ -120,7 +119,7 @@ __global__ void cell_geometry_kernel(int64_t nt, const int4* __restrict__ cells,
   Ji[2][1] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]) * id;
   Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
   const Real sS = (mu_inv ? __ldg(mu_inv + c) : Real(1)) / adet;
-  const Real sT = (eps_r ? __ldg(eps_r + c) : Real(1)) * adet;
+  const Real sT = (eps_r ? __ldg(eps_r + c) : Real(1)) * adet * tscale;
   Real out[12];
 #pragma unroll
   for (int m = 0; m < 6; ++m) {
@@ -158,7 +157,7 @@ __global__ void cell_geometry_kernel(int64_t nt, const int4* __restrict__ cells,
       const Real cx = a[1] * b[2] - a[2] * b[1];
       const Real cy = a[2] * b[0] - a[0] * b[2];
       const Real cz = a[0] * b[1] - a[1] * b[0];
-      const Real ita = Real(1) / sqrt(cx * cx + cy * cy + cz * cz);
+      const Real ita = hscale / sqrt(cx * cx + cy * cy + cz * cz);
       c0 = (b[0] * b[0] + b[1] * b[1] + b[2] * b[2]) * ita;
       c1 = -(a[0] * b[0] + a[1] * b[1] + a[2] * b[2]) * ita;
       c2 = (a[0] * a[0] + a[1] * a[1] + a[2] * a[2]) * ita;
@@ -169,17 +168,6 @@ __global__ void cell_geometry_kernel(int64_t nt, const int4* __restrict__ cells,
   }
 }
 
-struct RowPtrs {
-  const int32_t* ent_ptr;
-  const int32_t* inc_cell;
-  const uint8_t* inc_rec;
-  const int32_t* indptr;
-  const int32_t* bidx;
-  const uint8_t* ext_mask;
-  int64_t n_ent;
-  int max_row;
-};
-
 template <typename Real>
 __device__ __forceinline__ void load12(const Real* p, Real out[12]);
 template <>
@@ -187,7 +175,7 @@ __device__ __forceinline__ void load12<float>(const float* p, float out[12]) {
   const float4* q = reinterpret_cast<const float4*>(p);
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    const float4 t = q[i];
+    const float4 t = __ldg(q + i);
     out[4 * i] = t.x;
     out[4 * i + 1] = t.y;
     out[4 * i + 2] = t.z;
@@ -199,139 +187,323 @@ __device__ __forceinline__ void load12<double>(const double* p, double out[12]) 
   const double2* q = reinterpret_cast<const double2*>(p);
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
-    const double2 t = q[i];
+    const double2 t = __ldg(q + i);
     out[2 * i] = t.x;
     out[2 * i + 1] = t.y;
   }
 }
 
-// ORDER: 1 or 2.  WITH_B: accumulate the ABC matrix.  MODE 0: separate
-// real outputs; MODE 1: fused complex A = S - k0^2 T + j k0 B.
+// ---- entity-per-lane assembly of orders 1-2 ----
 //
-// One warp per entity.  Its lanes take ICH = 32/ND incident cells at a time
-// (order 2: one cell, lane b = cell column b; order 1: five cells x six
-// columns).  Each lane contracts the cell's coefficients with the reference
-// tensors for the entity's rows and adds the result into its accumulator
-// copy (copy = which of the ICH cells of the step it handles).  Within a copy
-// the columns of one cell are distinct slots, so plain shared-memory
-// read-add-write is race free; copies are summed in a fixed order when the
-// rows are written, so results are bit-reproducible.
-template <int ORDER, typename Real, bool WITH_B, int MODE>
-__global__ void __launch_bounds__(kWarps * 32)
-    assemble_rows_kernel(RowPtrs p, const Real* __restrict__ gcell, const Real* __restrict__ hcell,
-                         const Real* __restrict__ kab, const Real* __restrict__ kt, Real* S,
-                         Real* T, Real* B, typename Cplx<Real>::T* A, Real k0) {
-  constexpr int ND = ORDER == 1 ? 6 : 20;
-  constexpr int DPE = ORDER == 1 ? 1 : 2;
-  constexpr int REC = ORDER == 1 ? 8 : 24;
-  constexpr int ICH = 32 / ND;                 // incident cells per sweep step
-  // accumulated matrices: mode 0 -> S, T (, B); mode 1 -> Re A, Im A
-  constexpr int NMAT = MODE == 1 ? 2 : (WITH_B ? 3 : 2);
-  constexpr int KSZ = ND * ND * 12;
+// One warp owns a task of 32 entities (edges, or faces of order 2), one per
+// lane; a lane's entity owns DPE consecutive CSR rows (DPE = order) that
+// share one column list of L slots.  The task's steps (see Space: local
+// entity index le major, trip[le] steps each) give every lane one incident
+// cell per step.  For step le the element-matrix rows of local entity le
+// are the same straight-line code on every lane (contract::Rows, reference
+// constants inlined), so the contraction needs no table loads; the lane
+// adds its DPE x ND values (and, in separate mode, S and T apart) to its
+// own accumulator row in shared memory at the column slots of the step
+// record.  A lane's accumulator is private: no atomics and a fixed
+// summation order (bit-reproducible).  The slots of one slot index of all
+// lanes sit in distinct banks (per-lane stride odd in units of the slot
+// vector).  At the end the warp writes each lane's rows in turn with
+// coalesced stores: every CSR value is written once and nothing is
+// zero-filled first.
+//
+// Boundary entities (on an exterior facet) are in tasks of their own that
+// also accumulate the ABC matrix B from the cells' tangential coefficients
+// h and the face tables KT (read through L1: the cells concerned are few).
+// Blocks hold either w_int interior tasks or fewer boundary tasks, so that
+// both fit the same shared memory.
+constexpr int kEntWarps = 4;
 
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  Real* sK = reinterpret_cast<Real*>(smem_raw);  // [a][b][12]: KC[0..5], KM[0..5]
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int R = p.max_row;
-  const int copy_len = DPE * NMAT * R;        // one copy: [DPE][NMAT][R]
-  const int acc_len = ICH * copy_len;
-  Real* acc = sK + KSZ + warp * acc_len;      // [ICH][DPE][NMAT][R]
+template <int V, typename Real>
+struct SlotVec;  // V values of one slot, moved with the widest shared access
+template <>
+struct SlotVec<1, float> {
+  static __device__ __forceinline__ void add(float* p, const float* v) { p[0] += v[0]; }
+};
+template <>
+struct SlotVec<2, float> {
+  static __device__ __forceinline__ void add(float* p, const float* v) {
+    float2 t = *reinterpret_cast<float2*>(p);
+    t.x += v[0];
+    t.y += v[1];
+    *reinterpret_cast<float2*>(p) = t;
+  }
+};
+template <>
+struct SlotVec<4, float> {
+  static __device__ __forceinline__ void add(float* p, const float* v) {
+    float4 t = *reinterpret_cast<float4*>(p);
+    t.x += v[0];
+    t.y += v[1];
+    t.z += v[2];
+    t.w += v[3];
+    *reinterpret_cast<float4*>(p) = t;
+  }
+};
+template <>
+struct SlotVec<1, double> {
+  static __device__ __forceinline__ void add(double* p, const double* v) { p[0] += v[0]; }
+};
+template <>
+struct SlotVec<2, double> {
+  static __device__ __forceinline__ void add(double* p, const double* v) {
+    double2 t = *reinterpret_cast<double2*>(p);
+    t.x += v[0];
+    t.y += v[1];
+    *reinterpret_cast<double2*>(p) = t;
+  }
+};
+template <>
+struct SlotVec<4, double> {
+  static __device__ __forceinline__ void add(double* p, const double* v) {
+    SlotVec<2, double>::add(p, v);
+    SlotVec<2, double>::add(p + 2, v + 2);
+  }
+};
 
-  for (int i = threadIdx.x; i < KSZ; i += blockDim.x) sK[i] = kab[i];
-  for (int i = lane; i < acc_len; i += 32) acc[i] = Real(0);
-  __syncthreads();
-  const Real k0sq = k0 * k0;
-  const int sub = lane / ND, b = lane - sub * ND;   // cell of the step, cell column
-  const bool lane_on = sub < ICH;
-  Real* my_copy = acc + (lane_on ? sub : 0) * copy_len;
+struct EntArgs {
+  const int32_t* task_ent;     // n_tasks*32
+  const int4* task_meta;       // n_tasks
+  const uint32_t* step_words;  // step blocks
+  const int32_t* indptr;       // n+1
+  const int32_t* bidx;         // nt
+  const uint8_t* ext_mask;     // nt
+  int64_t n_tasks;             // tasks handled by this launch
+  int64_t n_int_tasks;         // of which interior (the first ones)
+  int64_t n_int_blocks;        // blocks [0, n_int_blocks) take interior tasks
+  int w_int;                   // tasks per interior block (= warps per block)
+  int w_bnd;                   // tasks per boundary block
+  int P;                       // per-lane accumulator stride in slots (odd)
+};
 
-  const int64_t nwarps = (int64_t)gridDim.x * kWarps;
-  for (int64_t e = (int64_t)blockIdx.x * kWarps + warp; e < p.n_ent; e += nwarps) {
-    const int i0 = __ldg(&p.ent_ptr[e]), i1 = __ldg(&p.ent_ptr[e + 1]);
-    const int64_t r0 = (int64_t)DPE * e;
-    const int off = __ldg(&p.indptr[r0]);
-    const int L = __ldg(&p.indptr[r0 + 1]) - off;
-    for (int k0i = i0; k0i < i1; k0i += ICH) {
-      const int inc = k0i + sub;
-      if (lane_on && inc < i1) {
-        const int c = __ldg(&p.inc_cell[inc]);
-        const uint8_t* rec = p.inc_rec + (int64_t)inc * REC;
-        const int le = __ldg(rec);
-        const int slot = __ldg(rec + 1 + b);
-        Real g[12];
-        load12<Real>(gcell + (int64_t)c * 12, g);
-        int hb = -1, mask = 0;
-        if (WITH_B) {
-          hb = __ldg(&p.bidx[c]);
-          if (hb >= 0) mask = __ldg(&p.ext_mask[c]);
-        }
+template <int ORDER, typename Real, int MODE>
+struct EntCfg {
+  static constexpr int ND = ORDER == 1 ? 6 : 20;
+  static constexpr int DPE = ORDER;
+  static constexpr int PL = (ND + 3) / 4;              // slot planes of a step block
+  static constexpr int WPS = (1 + PL) * 32;            // words per step block
+  static constexpr int NMAT = MODE == 1 ? 1 : 2;       // fused A, or S and T
+  static constexpr int V = DPE * NMAT;                 // values per slot (main accumulator)
+  static constexpr int VB = DPE;                       // values per slot (B / Im accumulator)
+};
+
+struct StepRec {
+  int cell;
+  uint32_t sl[5];
+};
+
+template <int PL>
+__device__ __forceinline__ StepRec load_step(const uint32_t* blk, int lane) {
+  StepRec r;
+  r.cell = (int)__ldg(blk + lane);
 #pragma unroll
-        for (int j = 0; j < DPE; ++j) {
-          const int a = DPE * le + j;
-          Real kk[12];
-          load12<Real>(sK + (a * ND + b) * 12, kk);
-          Real s = 0, tm = 0;
+  for (int q = 0; q < PL; ++q) r.sl[q] = __ldg(blk + 32 * (1 + q) + lane);
+  return r;
+}
+
+template <typename Real>
+__device__ __forceinline__ void load_g(const Real* gcell, int c, Real g[12]) {
+  if (c >= 0) {
+    load12<Real>(gcell + (int64_t)c * 12, g);
+  } else {
 #pragma unroll
-          for (int m = 0; m < 6; ++m) {
-            s = fma(g[m], kk[m], s);
-            tm = fma(g[6 + m], kk[6 + m], tm);
-          }
-          Real* ar = my_copy + j * NMAT * R + slot;
-          if (MODE == 1) {
-            ar[0] += s - k0sq * tm;
-          } else {
-            ar[0] += s;
-            ar[R] += tm;
-          }
-          if (WITH_B && hb >= 0) {
-            const Real* hh = hcell + (int64_t)hb * 12;
-            Real bv = 0;
+    for (int m = 0; m < 12; ++m) g[m] = Real(0);
+  }
+}
+
+__device__ __forceinline__ int slot_of(const StepRec& r, int b) {
+  return (int)((r.sl[b >> 2] >> (8 * (b & 3))) & 0xffu);
+}
+
+// does exterior local face f of a cell contain the lane's entity (local
+// index LE, edge or face)?
+template <bool FACE, int LE>
+__device__ __forceinline__ bool face_holds(int f) {
+  if (FACE) return f == LE;
+  constexpr int ev0 = LE == 0 ? 2 : LE == 1 ? 1 : LE == 2 ? 1 : 0;
+  constexpr int ev1 = LE == 0 ? 3 : LE == 1 ? 3 : LE == 2 ? 2 : LE == 3 ? 3 : LE == 4 ? 2 : 1;
+  return f != ev0 && f != ev1;
+}
+
+// one step of local entity LE: contract, then add into the lane's rows
+template <int ORDER, typename Real, int MODE, bool FACE, int LE, bool BND>
+__device__ __forceinline__ void ent_step(const StepRec& r, const Real g[12], Real* acc, Real* bacc,
+                                         const EntArgs& p, const Real* __restrict__ hcell,
+                                         const Real* __restrict__ kt) {
+  using C = EntCfg<ORDER, Real, MODE>;
+  constexpr int ND = C::ND, DPE = C::DPE;
+  Real v[ND][C::V];
 #pragma unroll
-            for (int f = 0; f < 4; ++f) {
-              if (!(mask >> f & 1)) continue;
+  for (int b = 0; b < ND; ++b)
 #pragma unroll
-              for (int m = 0; m < 3; ++m)
-                bv = fma(__ldg(&hh[f * 3 + m]), __ldg(&kt[((f * 3 + m) * ND + a) * ND + b]), bv);
-            }
-            if (MODE == 1)
-              ar[R] += k0 * bv;
-            else
-              ar[2 * R] += bv;
-          }
-        }
-      }
-      __syncwarp();
-    }
-    // ---- write the entity's rows (sum of the copies), reset the copies ----
+    for (int q = 0; q < C::V; ++q) v[b][q] = Real(0);
+  if (MODE == 1) {
+    contract::Rows<ORDER, FACE, LE>::fused(g, [&](int j, int b, Real x) { v[b][j] = x; });
+  } else {
+    contract::Rows<ORDER, FACE, LE>::split(g, [&](int j, int b, Real sv, Real tv, bool) {
+      v[b][j] = sv;
+      v[b][DPE + j] = tv;
+    });
+  }
+  if (r.cell < 0) return;
+#pragma unroll
+  for (int b = 0; b < ND; ++b) SlotVec<C::V, Real>::add(acc + slot_of(r, b) * C::V, v[b]);
+  if (!BND) return;
+  const int hb = __ldg(&p.bidx[r.cell]);
+  if (hb < 0) return;
+  const int mask = __ldg(&p.ext_mask[r.cell]);
+  for (int f = 0; f < 4; ++f) {
+    if (!(mask >> f & 1) || !face_holds<FACE, LE>(f)) continue;
+    const Real h0 = __ldg(&hcell[(int64_t)hb * 12 + 3 * f]);
+    const Real h1 = __ldg(&hcell[(int64_t)hb * 12 + 3 * f + 1]);
+    const Real h2 = __ldg(&hcell[(int64_t)hb * 12 + 3 * f + 2]);
 #pragma unroll
     for (int j = 0; j < DPE; ++j) {
-      const int64_t base = (int64_t)off + (int64_t)j * L;
-      for (int col = lane; col < L; col += 32) {
-        Real v[NMAT];
-#pragma unroll
-        for (int q = 0; q < NMAT; ++q) v[q] = 0;
-#pragma unroll
-        for (int cc = 0; cc < ICH; ++cc) {
-          Real* ar = acc + cc * copy_len + j * NMAT * R + col;
-#pragma unroll
-          for (int q = 0; q < NMAT; ++q) {
-            v[q] += ar[q * R];
-            ar[q * R] = 0;
-          }
-        }
-        if (MODE == 0) {
-          if (S) S[base + col] = v[0];
-          if (T) T[base + col] = v[1];
-          if (WITH_B && B) B[base + col] = v[NMAT - 1];
-        } else {
-          typename Cplx<Real>::T z;
-          z.x = v[0];
-          z.y = v[1];
-          A[base + col] = z;
-        }
+      const int a = FACE ? 12 + 2 * LE + j : DPE * LE + j;
+      const Real* k0p = kt + ((int64_t)(f * 3 + 0) * ND + a) * ND;
+      const Real* k1p = kt + ((int64_t)(f * 3 + 1) * ND + a) * ND;
+      const Real* k2p = kt + ((int64_t)(f * 3 + 2) * ND + a) * ND;
+#pragma unroll 4
+      for (int b = 0; b < ND; ++b) {
+        const Real bv = fma(h2, __ldg(k2p + b), fma(h1, __ldg(k1p + b), h0 * __ldg(k0p + b)));
+        bacc[slot_of(r, b) * C::VB + j] += bv;
       }
     }
-    __syncwarp();
+  }
+}
+
+// the steps of local entities LE .. NLE-1; the next step's record and cell
+// coefficients and the record after it are loaded one step ahead
+template <int ORDER, typename Real, int MODE, bool FACE, int LE, int NLE, bool BND>
+__device__ __forceinline__ void ent_steps(const uint8_t* trip, int& s, int nsteps,
+                                          const uint32_t* blk0, int lane, StepRec& r0, Real* g0,
+                                          StepRec& r1, Real* acc, Real* bacc, const EntArgs& p,
+                                          const Real* __restrict__ gcell,
+                                          const Real* __restrict__ hcell,
+                                          const Real* __restrict__ kt) {
+  if constexpr (LE < NLE) {
+    using C = EntCfg<ORDER, Real, MODE>;
+    for (int t = 0; t < trip[LE]; ++t, ++s) {
+      Real g1[12];
+      load_g<Real>(gcell, s + 1 < nsteps ? r1.cell : -1, g1);
+      StepRec r2;
+      r2.cell = -1;
+      if (s + 2 < nsteps) r2 = load_step<C::PL>(blk0 + (int64_t)(s + 2) * C::WPS, lane);
+      ent_step<ORDER, Real, MODE, FACE, LE, BND>(r0, g0, acc, bacc, p, hcell, kt);
+      r0 = r1;
+#pragma unroll
+      for (int m = 0; m < 12; ++m) g0[m] = g1[m];
+      r1 = r2;
+    }
+    ent_steps<ORDER, Real, MODE, FACE, LE + 1, NLE, BND>(trip, s, nsteps, blk0, lane, r0, g0, r1,
+                                                        acc, bacc, p, gcell, hcell, kt);
+  }
+}
+
+template <int ORDER, typename Real, int MODE, bool BND>
+__device__ __forceinline__ void ent_task(int64_t task, int lane, Real* acc, Real* bacc,
+                                         const EntArgs& p, const Real* __restrict__ gcell,
+                                         const Real* __restrict__ hcell,
+                                         const Real* __restrict__ kt, Real* S, Real* T, Real* B,
+                                         typename Cplx<Real>::T* A) {
+  using C = EntCfg<ORDER, Real, MODE>;
+  constexpr int DPE = C::DPE;
+  const int P = p.P;
+  // clear the warp's accumulators (each lane's P slots)
+  {
+    Real* a0 = acc - (int64_t)lane * P * C::V;
+    const int words = 32 * P * C::V;
+    for (int i = lane; i < words; i += 32) a0[i] = Real(0);
+    if (BND) {
+      Real* b0 = bacc - (int64_t)lane * P * C::VB;
+      for (int i = lane; i < 32 * P * C::VB; i += 32) b0[i] = Real(0);
+    }
+  }
+  __syncwarp();
+  const int4 meta = p.task_meta[task];
+  uint8_t trip[8];
+  *reinterpret_cast<int*>(&trip[0]) = meta.y;
+  *reinterpret_cast<int*>(&trip[4]) = meta.z;
+  int nsteps = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) nsteps += trip[i];
+  const uint32_t* blk0 = p.step_words + (int64_t)meta.x * C::WPS;
+  StepRec r0, r1;
+  r0.cell = r1.cell = -1;
+  if (nsteps > 0) r0 = load_step<C::PL>(blk0, lane);
+  if (nsteps > 1) r1 = load_step<C::PL>(blk0 + C::WPS, lane);
+  Real g0[12];
+  load_g<Real>(gcell, r0.cell, g0);
+  int s = 0;
+  bool done = false;
+  if constexpr (ORDER == 2) {
+    if (meta.w & 1) {
+      ent_steps<ORDER, Real, MODE, true, 0, 4, BND>(trip, s, nsteps, blk0, lane, r0, g0, r1, acc,
+                                                    bacc, p, gcell, hcell, kt);
+      done = true;
+    }
+  }
+  if (!done)
+    ent_steps<ORDER, Real, MODE, false, 0, 6, BND>(trip, s, nsteps, blk0, lane, r0, g0, r1, acc,
+                                                   bacc, p, gcell, hcell, kt);
+  __syncwarp();
+  // write each lane's rows, one entity at a time, coalesced
+  const int my_ent = p.task_ent[task * 32 + lane];
+  const Real* acc0 = acc - (int64_t)lane * P * C::V;
+  const Real* bacc0 = BND ? bacc - (int64_t)lane * P * C::VB : nullptr;
+  for (int l = 0; l < 32; ++l) {
+    const int k = __shfl_sync(0xffffffffu, my_ent, l);
+    if (k < 0) continue;
+    const int off = __ldg(&p.indptr[(int64_t)DPE * k]);
+    const int L = __ldg(&p.indptr[(int64_t)DPE * k + 1]) - off;
+    const Real* al = acc0 + (int64_t)l * P * C::V;
+    const Real* bl = BND ? bacc0 + (int64_t)l * P * C::VB : nullptr;
+    for (int idx = lane; idx < DPE * L; idx += 32) {
+      const int j = DPE == 2 ? (idx >= L) : 0;
+      const int sl = idx - j * L;
+      const Real bval = BND ? bl[sl * C::VB + j] : Real(0);
+      if (MODE == 1) {
+        typename Cplx<Real>::T z;
+        z.x = al[sl * C::V + j];
+        z.y = bval;
+        A[(int64_t)off + idx] = z;
+      } else {
+        if (S) S[(int64_t)off + idx] = al[sl * C::V + j];
+        if (T) T[(int64_t)off + idx] = al[sl * C::V + DPE + j];
+        if (B) B[(int64_t)off + idx] = bval;
+      }
+    }
+  }
+}
+
+template <int ORDER, typename Real, int MODE, bool WITH_B>
+__global__ void __launch_bounds__(kEntWarps * 32)
+    assemble_entities_kernel(EntArgs p, const Real* __restrict__ gcell,
+                             const Real* __restrict__ hcell, const Real* __restrict__ kt, Real* S,
+                             Real* T, Real* B, typename Cplx<Real>::T* A) {
+  using C = EntCfg<ORDER, Real, MODE>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Real* sm = reinterpret_cast<Real*>(smem_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t main_words = (int64_t)32 * p.P * C::V;
+  if ((int64_t)blockIdx.x < p.n_int_blocks) {
+    const int64_t task = (int64_t)blockIdx.x * p.w_int + warp;
+    if (task >= p.n_int_tasks) return;
+    Real* acc = sm + warp * main_words + (int64_t)lane * p.P * C::V;
+    ent_task<ORDER, Real, MODE, false>(task, lane, acc, nullptr, p, gcell, hcell, kt, S, T, B, A);
+  } else if (WITH_B) {
+    if (warp >= p.w_bnd) return;
+    const int64_t task = p.n_int_tasks + ((int64_t)blockIdx.x - p.n_int_blocks) * p.w_bnd + warp;
+    if (task >= p.n_tasks) return;
+    const int64_t bwords = (int64_t)32 * p.P * C::VB;
+    Real* base = sm + warp * (main_words + bwords);
+    Real* acc = base + (int64_t)lane * p.P * C::V;
+    Real* bacc = base + main_words + (int64_t)lane * p.P * C::VB;
+    ent_task<ORDER, Real, MODE, WITH_B>(task, lane, acc, bacc, p, gcell, hcell, kt, S, T, B, A);
   }
 }
 
@@ -411,49 +583,53 @@ cudaError_t ensure_scratch(DeviceSpace& d, Real** g, Real** h) {
 
 template <int ORDER, typename Real, bool WITH_B, int MODE>
 cudaError_t launch_t(DeviceSpace& d, const AssembleArgs& a, cudaStream_t stream) {
-  constexpr int ND = ORDER == 1 ? 6 : 20;
-  constexpr int DPE = ORDER == 1 ? 1 : 2;
-  constexpr int NMAT = MODE == 1 ? 2 : (WITH_B ? 3 : 2);
-  constexpr int ICH = 32 / ND;
+  using C = EntCfg<ORDER, Real, MODE>;
+  if (!d.task_meta || d.n_tasks == 0) return cudaErrorInvalidValue;
   Real *g = nullptr, *h = nullptr;
   cudaError_t err = ensure_scratch<Real>(d, &g, &h);
   if (err != cudaSuccess) return err;
   {
     const int threads = 256;
     const int64_t blocks = (d.nt + threads - 1) / threads;
+    const Real tscale = MODE == 1 ? Real(-a.k0 * a.k0) : Real(1);
+    const Real hscale = MODE == 1 ? Real(a.k0) : Real(1);
     cell_geometry_kernel<Real><<<(unsigned)blocks, threads, 0, stream>>>(
         d.nt, d.cells, d.xyz_hi, d.xyz_lo, d.xyz, d.ext_mask, d.bidx, (const Real*)a.eps_r,
-        (const Real*)a.mu_r_inv, g, h, WITH_B);
+        (const Real*)a.mu_r_inv, g, h, WITH_B, tscale, hscale);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
   }
-  RowPtrs p;
-  p.ent_ptr = d.ent_ptr;
-  p.inc_cell = d.inc_cell;
-  p.inc_rec = d.inc_rec;
+  EntArgs p;
+  p.task_ent = d.task_ent;
+  p.task_meta = d.task_meta;
+  p.step_words = d.step_words;
   p.indptr = d.indptr;
   p.bidx = d.bidx;
   p.ext_mask = d.ext_mask;
-  p.n_ent = d.n_ent;
-  p.max_row = d.max_row;
-  const size_t smem =
-      sizeof(Real) * ((size_t)ND * ND * 12 + (size_t)kWarps * ICH * DPE * NMAT * d.max_row);
-  auto kern = assemble_rows_kernel<ORDER, Real, WITH_B, MODE>;
+  p.P = d.max_row | 1;
+  p.n_tasks = d.n_tasks;
+  // without B every task is an interior one (no B or Im accumulator)
+  p.n_int_tasks = WITH_B ? d.n_tasks_interior : d.n_tasks;
+  const int64_t main_bytes = (int64_t)32 * p.P * C::V * sizeof(Real);
+  const int64_t bnd_bytes = main_bytes + (int64_t)32 * p.P * C::VB * sizeof(Real);
+  // up to kEntWarps tasks per block within ~80 KB, so that two or more
+  // blocks share an SM
+  p.w_int = (int)std::max<int64_t>(1, std::min<int64_t>(kEntWarps, (80 << 10) / main_bytes));
+  p.n_int_blocks = (p.n_int_tasks + p.w_int - 1) / p.w_int;
+  int64_t smem = p.w_int * main_bytes;
+  p.w_bnd = (int)std::max<int64_t>(1, std::min<int64_t>(p.w_int, smem / bnd_bytes));
+  smem = std::max<int64_t>(smem, p.w_bnd * bnd_bytes);
+  const int64_t n_bnd_tasks = p.n_tasks - p.n_int_tasks;
+  const int64_t n_bnd_blocks = WITH_B ? (n_bnd_tasks + p.w_bnd - 1) / p.w_bnd : 0;
+  const int64_t grid = p.n_int_blocks + n_bnd_blocks;
+  if (grid < 1) return cudaSuccess;
+  if (smem > (227 << 10)) return cudaErrorInvalidConfiguration;  // rows too long
+  auto kern = assemble_entities_kernel<ORDER, Real, MODE, WITH_B>;
   err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
-  int dev = 0, nsm = 0, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarps * 32, smem);
-  if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  int64_t want = (d.n_ent + kWarps - 1) / kWarps;
-  int64_t grid = std::min<int64_t>(want, (int64_t)nsm * per_sm);
-  if (grid < 1) grid = 1;
-  const Real* kab = sizeof(Real) == 4 ? (const Real*)d.kab_f : (const Real*)d.kab_d;
   const Real* kt = sizeof(Real) == 4 ? (const Real*)d.kt_f : (const Real*)d.kt_d;
-  kern<<<(unsigned)grid, kWarps * 32, smem, stream>>>(p, g, h, kab, kt, (Real*)a.S, (Real*)a.T,
-                                                      (Real*)a.B, (typename Cplx<Real>::T*)a.A,
-                                                      (Real)a.k0);
+  kern<<<(unsigned)grid, p.w_int * 32, (size_t)smem, stream>>>(
+      p, g, h, kt, (Real*)a.S, (Real*)a.T, (Real*)a.B, (typename Cplx<Real>::T*)a.A);
   count_launch(2);
   return cudaGetLastError();
 }
@@ -468,7 +644,7 @@ cudaError_t launch_cells_t(DeviceSpace& d, const AssembleArgs& a, cudaStream_t s
     const int64_t blocks = (d.nt + threads - 1) / threads;
     cell_geometry_kernel<Real><<<(unsigned)blocks, threads, 0, stream>>>(
         d.nt, d.cells, d.xyz_hi, d.xyz_lo, d.xyz, d.ext_mask, d.bidx, (const Real*)a.eps_r,
-        (const Real*)a.mu_r_inv, g, h, WITH_B);
+        (const Real*)a.mu_r_inv, g, h, WITH_B, Real(1), Real(1));
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
   }

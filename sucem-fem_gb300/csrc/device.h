@@ -47,7 +47,13 @@ struct DeviceSpace {
   double* g_d = nullptr;
   float* h_f = nullptr;           // nb*12
   double* h_d = nullptr;
-  // reference tensors in the row kernel's layout [a][b][12] (KC m=0..5, KM m=0..5)
+  // entity-per-lane assembly schedule (orders 1-2, see Space)
+  int64_t n_tasks = 0, n_tasks_interior = 0;
+  int slot_planes = 0;
+  int32_t* task_ent = nullptr;    // n_tasks*32
+  int4* task_meta = nullptr;      // n_tasks
+  uint32_t* step_words = nullptr; // step blocks
+  // reference tensors in the cell kernel's layout [a][b][12] (KC m=0..5, KM m=0..5)
   float* kab_f = nullptr;
   double* kab_d = nullptr;
   // reference tensors [6][nd][nd] (curl, mass), [4][3][nd][nd] (face tangential)

@@ -348,6 +348,68 @@ def tables_moments(order):
     return sym6(PC), sym6(PN), KT
 
 
+def _chain(terms):
+    """Straight-line FMA chain for sum(coef * g[m]) over the nonzero terms
+    (constants rounded to the kernel's type R at compile time)."""
+    expr = None
+    for m, c in terms:
+        k = "R(%r)" % float(c)
+        expr = "g[%d] * %s" % (m, k) if expr is None else "fma(g[%d], %s, %s)" % (m, k, expr)
+    return expr
+
+
+def contract_code():
+    """Device code for the element-matrix rows of one local entity of an
+    order-1 or order-2 cell, with the reference constants inlined (zero
+    constants dropped):
+
+      Rows<ORDER, FACE, LE>::fused(g, fn)  calls fn(j, b, v) with
+          v = sum_m g[m] KC[m][a][b] + g[6 + m] KM[m][a][b]
+      Rows<ORDER, FACE, LE>::split(g, fn)  calls fn(j, b, s, t, has_s) with
+          s = sum_m g[m] KC[m][a][b], t = sum_m g[6 + m] KM[m][a][b]
+          (has_s false when every KC constant of the entry is zero, s = 0)
+
+    for every column b of the cell and the entity's local DOFs a (j-th):
+    edge LE of order k -> a = k*LE + j, face LE of order 2 -> a = 12 + 2*LE + j.
+    The entity-per-lane assembly kernel calls them with the cell's metric
+    coefficients g (12 values, S then T)."""
+    out = ["// Generated by gen_tables.py: N1curl element-matrix rows of one local",
+           "// entity with the reference constants inlined.  Do not edit; rerun the",
+           "// generator.  See contract_code() in gen_tables.py for the contract.",
+           "#pragma once", "", "namespace sucem {", "namespace contract {", "",
+           "template <int ORDER, bool FACE, int LE>", "struct Rows;", ""]
+    for order in (1, 2):
+        KC, KM, _, _ = tables(order)
+        n = len(KC[0])
+        kinds = [(False, 6)] + ([(True, 4)] if order == 2 else [])
+        for face, nle in kinds:
+            for le in range(nle):
+                rows = ([12 + 2 * le, 13 + 2 * le] if face else
+                        [order * le + j for j in range(order)])
+                fused, split = [], []
+                for j, a in enumerate(rows):
+                    for b in range(n):
+                        ts = [(m, KC[m][a][b]) for m in range(6) if KC[m][a][b] != 0]
+                        tt = [(6 + m, KM[m][a][b]) for m in range(6) if KM[m][a][b] != 0]
+                        if ts or tt:
+                            fused.append("    fn(%d, %d, %s);" % (j, b, _chain(ts + tt)))
+                        sv = _chain(ts) if ts else "R(0)"
+                        tv = _chain(tt) if tt else "R(0)"
+                        split.append("    fn(%d, %d, %s, %s, %s);" % (j, b, sv, tv,
+                                                                   "true" if ts else "false"))
+                out += ["template <>",
+                        "struct Rows<%d, %s, %d> {" % (order, "true" if face else "false", le),
+                        "  template <class R, class Fn>",
+                        "  static __device__ __forceinline__ void fused(const R* g, Fn&& fn) {"]
+                out += fused
+                out += ["  }", "  template <class R, class Fn>",
+                        "  static __device__ __forceinline__ void split(const R* g, Fn&& fn) {"]
+                out += split
+                out += ["  }", "};", ""]
+    out += ["}  // namespace contract", "}  // namespace sucem", ""]
+    return "\n".join(out)
+
+
 def _fmt(x, depth):
     if isinstance(x, list):
         inner = ",".join(_fmt(y, depth + 1) for y in x)
@@ -355,7 +417,7 @@ def _fmt(x, depth):
     return "0" if x == 0 else repr(float(x))
 
 
-def main(path, path_hi):
+def main(path, path_hi, path_contract=None):
     lines = ["// Generated by gen_tables.py: N1curl reference-element constants.",
              "// Do not edit; rerun the generator.", "#pragma once", ""]
     for order in (1, 2):
@@ -382,9 +444,13 @@ def main(path, path_hi):
         lines.append("")
     with open(path_hi, "w") as f:
         f.write("\n".join(lines))
+    if path_contract:
+        with open(path_contract, "w") as f:
+            f.write(contract_code())
 
 
 if __name__ == "__main__":
     here = os.path.dirname(os.path.abspath(__file__))
     main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(here, "n1curl_tables.h"),
-         sys.argv[2] if len(sys.argv) > 2 else os.path.join(here, "n1curl_tables_hi.h"))
+         sys.argv[2] if len(sys.argv) > 2 else os.path.join(here, "n1curl_tables_hi.h"),
+         sys.argv[3] if len(sys.argv) > 3 else os.path.join(here, "n1curl_contract.h"))

@@ -313,6 +313,7 @@ std::string build_space(Space& s, const double* coords, int64_t nv, const int64_
     for (int64_t r = 0; r < s.n; ++r)
       if (mark[r]) s.boundary_dofs.push_back(int32_t(r));
   }
+  build_row_schedule(s);
   return "";
 }
 

@@ -53,6 +53,26 @@ struct Space {
   // cell_pos[(c * ndof_cell + a) * ndof_cell + b] = index of (dof a, dof b)
   std::vector<int32_t> cell_pos;
 
+  // Entity-per-lane assembly schedule (orders 1-2).  Entities are grouped
+  // into warp tasks of 32 (one entity per lane) that share the entity kind
+  // (edge / face) and the boundary class (on an exterior facet or not), in
+  // an order that puts entities with the same incidence structure side by
+  // side.  A task walks its lanes' incidences local-entity-major: for each
+  // local index le (edges 0..5, faces 0..3) trip[le] steps, step t giving
+  // every lane its t-th incident cell with the entity at local index le
+  // (cell order within le, so the summation order is fixed).  One step is a
+  // block of 32 records laid out as planes of 32 words: the cells (-1: the
+  // lane has no incidence in this step), then ceil(ndof_cell / 4) words of
+  // column slots (byte b = slot of the cell's local DOF b in the entity's
+  // column list).
+  int64_t n_tasks = 0;                 // warp tasks
+  int64_t n_tasks_interior = 0;        // tasks [0, n_tasks_interior) have no boundary entity
+  std::vector<int32_t> task_ent;       // n_tasks*32: entity per lane (-1: none)
+  std::vector<int32_t> task_meta;      // n_tasks*4: first step block, trips le 0-3 (bytes),
+                                       //   trips le 4-7 (bytes), flags (bit 0: faces)
+  std::vector<uint32_t> step_words;    // step blocks, (1 + slot_planes) * 32 words each
+  int slot_planes = 0;                 // ceil(ndof_cell / 4)
+
   std::vector<int32_t> boundary_dofs;  // closure of the exterior facets, sorted
   std::vector<double> dof_xyz;         // n*3: edge midpoint / face centroid of each DOF
 
@@ -62,5 +82,9 @@ struct Space {
 // Builds everything above; returns an empty string or an error message.
 std::string build_space(Space& s, const double* coords, int64_t nv, const int64_t* cells,
                         int64_t nt, int order);
+
+// The entity-per-lane assembly schedule of an order-1/2 space (called by
+// build_space once the incidence tables exist).
+void build_row_schedule(Space& s);
 
 }  // namespace sucem

@@ -13,7 +13,8 @@ SUCEM_OK = 0
 ERR_ARG, ERR_MEMORY, ERR_CUDA, ERR_STATE, ERR_NOCONV, ERR_BREAKDOWN = -1, -2, -3, -4, -5, -6
 
 COPY = dict(indptr=0, indices=1, cell_dofs=2, boundary_dofs=3, edges=4, faces=5, cells=6, ext_mask=7,
-            cell_edges=8, cell_faces=9, dof_xyz=10, boundary_dual=11)
+            cell_edges=8, cell_faces=9, dof_xyz=10, boundary_dual=11, task_ent=12, task_meta=13,
+            step_words=14)
 DEV = dict(indptr=0, indices=1, cell_dofs=2, boundary_dofs=3)
 
 _lib = None
@@ -40,6 +41,7 @@ _SIGS = [
     ("sucem_space_destroy", None, [c_vp]),
     ("sucem_space_sizes", ctypes.c_int, [c_vp, c_i64p]),
     ("sucem_space_copy", ctypes.c_int, [c_vp, ctypes.c_int, c_vp]),
+    ("sucem_space_schedule_sizes", ctypes.c_int, [c_vp, c_i64p]),
     ("sucem_space_upload", ctypes.c_int, [c_vp, ctypes.c_int]),
     ("sucem_space_device_ptr", ctypes.c_int, [c_vp, ctypes.c_int, ctypes.POINTER(c_vp)]),
     ("sucem_assemble", ctypes.c_int,

@@ -110,6 +110,19 @@ class FunctionSpace:
     def cell_faces(self):
         return self._copy("cell_faces", (self.nt, 4), np.int32)
 
+    def assembly_schedule(self):
+        """The order-1/2 assembly kernel's work plan (host copy): per warp
+        task the entity of each lane, (first step block, steps per local
+        entity index, flags), and the step blocks (cells, then column-slot
+        words, 32 lanes each)."""
+        sz = np.zeros(4, dtype=np.int64)
+        call("sucem_space_schedule_sizes", self._h, sz.ctypes.data_as(_native.c_i64p))
+        nt_, nint, nblk, planes = [int(x) for x in sz]
+        ent = self._copy("task_ent", (nt_, 32), np.int32)
+        meta = self._copy("task_meta", (nt_, 4), np.int32)
+        words = self._copy("step_words", (nblk, 1 + planes, 32), np.uint32)
+        return dict(n_tasks_interior=nint, task_ent=ent, task_meta=meta, step_words=words)
+
     def facet_closure_dofs(self, faces):
         """DOFs on the closure of the given facets (facet ids = face ids)."""
         faces = np.asarray(faces, dtype=np.int64)
