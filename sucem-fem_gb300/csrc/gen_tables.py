@@ -358,6 +358,30 @@ def _chain(terms):
     return expr
 
 
+def _f32(x):
+    """Nearest float32 of a Fraction (round half to even), as a Fraction."""
+    import struct
+    f = float(x)
+    r = struct.unpack("f", struct.pack("f", f))[0]
+    # struct rounds the double; fix double rounding by checking neighbours
+    cands = [r]
+    for d in (-1, 1):
+        b = struct.unpack("I", struct.pack("f", r))[0] + (d if r >= 0 else -d)
+        cands.append(struct.unpack("f", struct.pack("I", b & 0xFFFFFFFF))[0])
+    return min((F(c) for c in cands), key=lambda c: (abs(c - x), c))
+
+
+def _dot2(terms):
+    """Compensated sum of coef * g[m] (Dot2): the float kernels get each
+    constant as float hi + lo and add the products with error-free
+    transformations, the double kernels a plain FMA chain."""
+    parts = []
+    for m, c in terms:
+        hi = _f32(c)
+        parts.append("t.add(g[%d], %r, %rf, %rf)" % (m, float(c), float(hi), float(_f32(c - hi))))
+    return "Dot2<R> t; " + "; ".join(parts) + ";"
+
+
 def contract_code():
     """Device code for the element-matrix rows of one local entity of an
     order-1 or order-2 cell, with the reference constants inlined (zero
@@ -367,7 +391,11 @@ def contract_code():
           v = sum_m g[m] KC[m][a][b] + g[6 + m] KM[m][a][b]
       Rows<ORDER, FACE, LE>::split(g, fn)  calls fn(j, b, s, t, has_s) with
           s = sum_m g[m] KC[m][a][b], t = sum_m g[6 + m] KM[m][a][b]
-          (has_s false when every KC constant of the entry is zero, s = 0)
+          (has_s false when every KC constant of the entry is zero, s = 0);
+          t is a compensated dot product (Dot2): in single precision the
+          mass-matrix terms of an element entry can cancel to a few percent
+          of their size, and a plain FMA chain then loses the 1e-6 relative
+          accuracy the separate matrices are held to
 
     for every column b of the cell and the entity's local DOFs a (j-th):
     edge LE of order k -> a = k*LE + j, face LE of order 2 -> a = 12 + 2*LE + j.
@@ -377,6 +405,43 @@ def contract_code():
            "// entity with the reference constants inlined.  Do not edit; rerun the",
            "// generator.  See contract_code() in gen_tables.py for the contract.",
            "#pragma once", "", "namespace sucem {", "namespace contract {", "",
+           "#ifdef __CUDA_ARCH__",
+           "#define SUCEM_FMUL(a, b) __fmul_rn(a, b)",
+           "#define SUCEM_FADD(a, b) __fadd_rn(a, b)",
+           "#define SUCEM_FSUB(a, b) __fsub_rn(a, b)",
+           "#else  // host builds of this header (tests) compile with -ffp-contract=off",
+           "#define SUCEM_FMUL(a, b) ((a) * (b))",
+           "#define SUCEM_FADD(a, b) ((a) + (b))",
+           "#define SUCEM_FSUB(a, b) ((a) - (b))",
+           "#endif",
+           "",
+           "// sum of g * k over the added terms: float keeps s + c with every",
+           "// product split exactly (p + e) and every sum step exactly (TwoSum),",
+           "// k given as float hi + lo (hi the nearest float of k); the",
+           "// intrinsics are never fused into FMAs.  double: a plain FMA chain.",
+           "template <class R>",
+           "struct Dot2;",
+           "template <>",
+           "struct Dot2<float> {",
+           "  float s = 0.f, c = 0.f;",
+           "  __device__ __forceinline__ void add(float g, double, float kh, float klo) {",
+           "    const float p = SUCEM_FMUL(g, kh);",
+           "    const float e = fmaf(g, kh, -p);",
+           "    const float t = SUCEM_FADD(s, p);",
+           "    const float z = SUCEM_FSUB(t, s);",
+           "    const float d = SUCEM_FADD(SUCEM_FSUB(s, SUCEM_FSUB(t, z)), SUCEM_FSUB(p, z));",
+           "    s = t;",
+           "    c = fmaf(g, klo, SUCEM_FADD(c, SUCEM_FADD(d, e)));",
+           "  }",
+           "  __device__ __forceinline__ float sum() const { return SUCEM_FADD(s, c); }",
+           "};",
+           "template <>",
+           "struct Dot2<double> {",
+           "  double s = 0.0;",
+           "  __device__ __forceinline__ void add(double g, double k, float, float) { s = fma(g, k, s); }",
+           "  __device__ __forceinline__ double sum() const { return s; }",
+           "};",
+           "",
            "template <int ORDER, bool FACE, int LE>", "struct Rows;", ""]
     for order in (1, 2):
         KC, KM, _, _ = tables(order)
@@ -394,9 +459,12 @@ def contract_code():
                         if ts or tt:
                             fused.append("    fn(%d, %d, %s);" % (j, b, _chain(ts + tt)))
                         sv = _chain(ts) if ts else "R(0)"
-                        tv = _chain(tt) if tt else "R(0)"
-                        split.append("    fn(%d, %d, %s, %s, %s);" % (j, b, sv, tv,
-                                                                   "true" if ts else "false"))
+                        if tt:
+                            split.append("    { %s fn(%d, %d, %s, t.sum(), %s); }" % (
+                                _dot2(tt), j, b, sv, "true" if ts else "false"))
+                        else:
+                            split.append("    fn(%d, %d, %s, R(0), %s);" % (
+                                j, b, sv, "true" if ts else "false"))
                 out += ["template <>",
                         "struct Rows<%d, %s, %d> {" % (order, "true" if face else "false", le),
                         "  template <class R, class Fn>",

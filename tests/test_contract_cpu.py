@@ -3,7 +3,9 @@
 and evaluated in double precision on random tetrahedra, against the
 oracle's element matrices (an independent, sympy-exact derivation of the
 same reference tensors).  Covers every (order, edge/face, local index) and
-both the fused (S + T part) and split (S, T apart) forms."""
+both the fused (S + T part) and split (S, T apart) forms; the split form is
+also run in single precision, whose compensated mass entries must stay
+within float rounding of their exact value where their terms cancel."""
 import os
 import shutil
 import subprocess
@@ -24,22 +26,30 @@ using std::fma;
 #define __forceinline__ inline
 #include "%s"
 using namespace sucem::contract;
+using std::fmaf;
 template <int O, bool F, int LE>
-void rows(const double* g) {
+void rows(const double* g, const float* gf) {
   Rows<O, F, LE>::fused(g, [&](int j, int b, double v) { std::printf("f %%d %%d %%d %%d %%d %%.17g\n", O, F, LE, j, b, v); });
   Rows<O, F, LE>::split(g, [&](int j, int b, double s, double t, bool) {
     std::printf("s %%d %%d %%d %%d %%d %%.17g %%.17g\n", O, F, LE, j, b, s, t);
   });
+  Rows<O, F, LE>::split(gf, [&](int j, int b, float s, float t, bool) {
+    std::printf("t %%d %%d %%d %%d %%d %%.9g %%.9g\n", O, F, LE, j, b, (double)s, (double)t);
+  });
 }
 int main() {
   double g[12];
-  for (int i = 0; i < 12; ++i)
+  float gf[12];
+  for (int i = 0; i < 12; ++i) {
     if (std::scanf("%%lf", &g[i]) != 1) return 1;
-  rows<1, false, 0>(g); rows<1, false, 1>(g); rows<1, false, 2>(g);
-  rows<1, false, 3>(g); rows<1, false, 4>(g); rows<1, false, 5>(g);
-  rows<2, false, 0>(g); rows<2, false, 1>(g); rows<2, false, 2>(g);
-  rows<2, false, 3>(g); rows<2, false, 4>(g); rows<2, false, 5>(g);
-  rows<2, true, 0>(g); rows<2, true, 1>(g); rows<2, true, 2>(g); rows<2, true, 3>(g);
+    gf[i] = (float)g[i];
+  }
+  rows<1, false, 0>(g, gf); rows<1, false, 1>(g, gf); rows<1, false, 2>(g, gf);
+  rows<1, false, 3>(g, gf); rows<1, false, 4>(g, gf); rows<1, false, 5>(g, gf);
+  rows<2, false, 0>(g, gf); rows<2, false, 1>(g, gf); rows<2, false, 2>(g, gf);
+  rows<2, false, 3>(g, gf); rows<2, false, 4>(g, gf); rows<2, false, 5>(g, gf);
+  rows<2, true, 0>(g, gf); rows<2, true, 1>(g, gf); rows<2, true, 2>(g, gf);
+  rows<2, true, 3>(g, gf);
   return 0;
 }
 """
@@ -54,7 +64,8 @@ def driver(tmp_path_factory):
     src = d / "drv.cpp"
     src.write_text(DRIVER % HEADER)
     exe = d / "drv"
-    subprocess.run([gxx, "-O1", "-std=c++17", "-o", str(exe), str(src)], check=True)
+    subprocess.run([gxx, "-O1", "-std=c++17", "-ffp-contract=off", "-o", str(exe), str(src)],
+                   check=True)
     return str(exe)
 
 
@@ -76,6 +87,15 @@ def test_generated_rows_match_oracle(driver, seed):
     out = subprocess.run([driver], input=" ".join("%.17g" % x for x in g), capture_output=True,
                          text=True, check=True).stdout.split("\n")
     ref = {o: fem.element_matrices(coords, cells, o, [1.0], [1.0]) for o in (1, 2)}
+    # the same element with the single-precision metric (what the float
+    # kernel is given): its exact mass rows and the size of their terms
+    from oracle import n1curl_exact
+    g32 = g.astype(np.float32).astype(np.float64)
+    exact32, termsum = {}, {}
+    for o in (1, 2):
+        Km = fem._sym6(n1curl_exact.reference_tensors(o)["mass"])
+        exact32[o] = np.einsum("m,mab->ab", g32[6:], Km)
+        termsum[o] = np.einsum("m,mab->ab", np.abs(g32[6:]), np.abs(Km))
     seen = 0
     for line in out:
         if not line:
@@ -87,9 +107,14 @@ def test_generated_rows_match_oracle(driver, seed):
         scale = max(np.abs(S).max(), np.abs(T).max())
         if kind == "f":
             assert abs(float(parts[6]) - (S[a, b] + T[a, b])) <= 1e-13 * scale
+        elif kind == "t":
+            # compensated single-precision mass entry: within a few units of
+            # float rounding of its exact value even where its terms cancel
+            e = exact32[o][a, b]
+            assert abs(float(parts[7]) - e) <= 1.2e-7 * abs(e) + 1e-12 * termsum[o][a, b]
         else:
             assert abs(float(parts[6]) - S[a, b]) <= 1e-13 * scale
             assert abs(float(parts[7]) - T[a, b]) <= 1e-13 * scale
         seen += 1
-    # split form: every entry of every local entity's rows
-    assert seen >= 6 * 6 + 10 * 2 * 20 + 6 * 6
+    # split forms (double and float): every entry of every local entity's rows
+    assert seen >= 2 * (6 * 6 + 10 * 2 * 20) + 6 * 6

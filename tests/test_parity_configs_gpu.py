@@ -1,0 +1,185 @@
+"""Per-entry parity of the GPU matrices with the FP64 oracle on the
+benchmark configurations, at the stated tolerances:
+
+  FP64 assembly: every entry within 1e-12 relative;
+  FP32 assembly: every entry within 1e-6 relative;
+  sparsity pattern and DOF numbering bit-exact.
+
+The one exception is stated and counted: an entry smaller than tol x its
+row's scale is a cancellation zero (its exact value is zero or cancels to
+below the tolerance; the FP64 oracle itself carries round-off there), and
+is held to an absolute error of tol x row scale instead.  The row scale is
+the row's largest |entry|, but at least 1e-3 of the matrix's largest: rows
+whose entries are all round-off (the ABC matrix B has them: rows of DOFs
+off the exterior facets of a boundary cell, which the oracle computes by
+cancellation through the facet normal) are then cancellation zeros too.
+
+Configurations:
+  * the driven ABC box of 20^3 cubes x 6 tets, order 2, eps_r ~ U[1,4)
+    seed 0 (the benchmark's matrix): S, T, B in FP64 and FP32, and the
+    fused complex matrix the FP32 solve factorises;
+  * the PEC cavity 1.0 x 0.5 x 0.75 m of 8 x 4 x 6 cubes, order 1, vacuum
+    (the eigen configuration): S and T in FP64 and FP32;
+  * the jittered 60^3 box, order 1 (1,296,000 tets): FP32 against FP64 on
+    the GPU for every entry, and 1,000 random rows against the oracle.
+Reference: sucemfem/ProblemConfigurations/tests/test_EMDrivenProblem.py:64-72
+(the reference's LHS parity test this extends to the benchmark sizes)."""
+import numpy as np
+import pytest
+
+from oracle import fem
+
+pytestmark = pytest.mark.gpu
+
+TOL = {8: 1e-12, 4: 1e-6}
+
+
+def per_entry(got, ref_data, indptr, tol):
+    """(max relative error over ordinary entries, max error / row scale over
+    cancellation zeros, number of cancellation zeros); asserts the bar."""
+    a = np.abs(ref_data)
+    rows = np.repeat(np.arange(len(indptr) - 1), np.diff(indptr))
+    rowmax = np.maximum.reduceat(a, indptr[:-1].astype(np.int64))
+    scale = np.maximum(rowmax, 1e-3 * a.max())[rows]
+    err = np.abs(np.asarray(got) - ref_data)
+    zero = a <= tol * scale
+    rel = err[~zero] / a[~zero]
+    zerr = err[zero] / scale[zero]
+    worst = float(rel.max()) if rel.size else 0.0
+    worst_zero = float(zerr.max()) if zerr.size else 0.0
+    assert worst <= tol, (worst, int((rel > tol).sum()))
+    assert worst_zero <= tol, worst_zero
+    return worst, worst_zero, int(zero.sum())
+
+
+def _assemble_split(V, rb, eps, with_b=True):
+    import torch
+    from sucemfem import _device
+    from sucemfem._native import call, ptr
+    dev = _device.device()
+    dt = torch.float32 if rb == 4 else torch.float64
+    out = {k: torch.empty(V.nnz, dtype=dt, device=dev) for k in ("STB" if with_b else "ST")}
+    de = None if eps is None else torch.as_tensor(eps, dtype=dt, device=dev)
+    call("sucem_assemble", V.upload(), rb, ptr(de), None, ptr(out["S"]), ptr(out["T"]),
+         ptr(out.get("B")), _device.stream_ptr())
+    torch.cuda.synchronize()
+    return {k: v.double().cpu().numpy() for k, v in out.items()}
+
+
+@pytest.fixture(scope="module")
+def config2():
+    """The benchmark's driven matrix (20^3 order 2) and its oracle."""
+    from sucemfem.mesh import BoxMesh
+    from sucemfem.space import FunctionSpace
+    n = 20
+    mesh = BoxMesh(1.0, 1.0, 1.0, n, n, n)
+    eps = np.random.default_rng(0).uniform(1.0, 4.0, mesh.num_cells())
+    ref = fem.assemble(mesh.coordinates(), mesh.cells(), 2, eps_r=eps)
+    V = FunctionSpace(mesh, order=2)
+    return V, eps, ref
+
+
+def test_config2_pattern_bit_exact(config2):
+    V, _, ref = config2
+    assert V.n == 316120 and V.nnz == 13419440
+    assert np.array_equal(V.indptr, ref.indptr)
+    assert np.array_equal(V.indices, ref.indices)
+
+
+@pytest.mark.parametrize("rb", [8, 4])
+def test_config2_matrices_per_entry(config2, rb):
+    V, eps, ref = config2
+    got = _assemble_split(V, rb, eps)
+    report = {}
+    for k, R in (("S", ref.S), ("T", ref.T), ("B", ref.B)):
+        report[k] = per_entry(got[k], R.data, ref.indptr, TOL[rb])
+    print("config 2, %s: (max rel, max zero err/scale, cancellation zeros) %s"
+          % ("FP64" if rb == 8 else "FP32", report))
+
+
+def test_config2_fused_complex_matrix(config2):
+    """The FP32 solve factorises A = S - k0^2 T + j k0 B assembled in one
+    pass (complex64).  S and k0^2 T cancel in part (the box is several
+    wavelengths across), so A is held to the FP32 bar relative to the size
+    of its two parts: |A32 - A| <= 1e-6 (|S| + k0^2 |T| + k0 |B|) per entry."""
+    import torch
+    from sucemfem import _device
+    from sucemfem._native import call, ptr
+    V, eps, ref = config2
+    k0 = 2 * np.pi / 0.4
+    dev = _device.device()
+    A = torch.empty(V.nnz, dtype=torch.complex64, device=dev)
+    call("sucem_assemble_helmholtz", V.upload(), 4,
+         ptr(torch.as_tensor(eps, dtype=torch.float32, device=dev)), None, float(k0), ptr(A),
+         _device.stream_ptr())
+    torch.cuda.synchronize()
+    a = A.cpu().numpy().astype(np.complex128)
+    aref = ref.S.data - k0 ** 2 * ref.T.data + 1j * k0 * ref.B.data
+    size = np.abs(ref.S.data) + k0 ** 2 * np.abs(ref.T.data) + k0 * np.abs(ref.B.data)
+    rows = np.repeat(np.arange(V.n), np.diff(ref.indptr))
+    rowmax = np.maximum.reduceat(size, ref.indptr[:-1].astype(np.int64))[rows]
+    err = np.abs(a - aref) / np.maximum(size, 1e-6 * rowmax)
+    assert err.max() <= 1e-6, err.max()
+
+
+def test_config1_cavity_per_entry():
+    from sucemfem.mesh import Mesh
+    from sucemfem.space import FunctionSpace
+    coords, cells = fem.box_mesh(1.0, 0.5, 0.75, 8, 4, 6)
+    ref = fem.assemble(coords, cells, 1, with_abc=False)
+    V = FunctionSpace(Mesh(coords, cells), order=1)
+    assert V.n == 1674
+    assert np.array_equal(V.indptr, ref.indptr) and np.array_equal(V.indices, ref.indices)
+    for rb in (8, 4):
+        got = _assemble_split(V, rb, None, with_b=False)
+        for k, R in (("S", ref.S), ("T", ref.T)):
+            per_entry(got[k], R.data, ref.indptr, TOL[rb])
+
+
+def _jittered60():
+    from sucemfem.mesh import BoxMesh, Mesh
+    n = 60
+    m = BoxMesh(1.0, 1.0, 1.0, n, n, n)
+    x = m.coordinates().copy()
+    interior = np.all((x > 1e-12) & (x < 1 - 1e-12), axis=1)
+    d = np.random.default_rng(0).uniform(-0.2 / n, 0.2 / n, size=x.shape)
+    x[interior] += d[interior]
+    return Mesh(x, m.cells())
+
+
+def test_jittered_60_order1_fp32_vs_fp64_and_oracle_rows():
+    from sucemfem.space import FunctionSpace
+    mesh = _jittered60()
+    eps = np.random.default_rng(1).uniform(1.0, 4.0, mesh.num_cells())
+    V = FunctionSpace(mesh, order=1)
+    assert V.nt == 1296000 and V.n == 1544580
+    g64 = _assemble_split(V, 8, eps)
+    g32 = _assemble_split(V, 4, eps)
+    for k in "STB":
+        per_entry(g32[k], g64[k], V.indptr, 1e-6)
+    # 1,000 random rows against the oracle: element matrices of the cells
+    # that hold those rows' DOFs, added up in FP64 on the space's numbering
+    rng = np.random.default_rng(2)
+    rows = np.sort(rng.choice(V.n, 1000, replace=False))
+    cd = V.cell_dofs
+    sel = np.nonzero(np.isin(cd, rows).any(axis=1))[0]
+    coords, cells = mesh.coordinates(), V.cells
+    Se, Te = fem.element_matrices(coords, cells[sel], 1, eps[sel], np.ones(len(sel)))
+    want = {k: {} for k in "ST"}
+    pick = np.zeros(V.n, dtype=bool)
+    pick[rows] = True
+    for i, c in enumerate(sel):
+        d = cd[c]
+        for a in range(6):
+            if not pick[d[a]]:
+                continue
+            for b in range(6):
+                want["S"][(d[a], d[b])] = want["S"].get((d[a], d[b]), 0.0) + Se[i, a, b]
+                want["T"][(d[a], d[b])] = want["T"].get((d[a], d[b]), 0.0) + Te[i, a, b]
+    ip, ix = V.indptr, V.indices
+    for k in "ST":
+        for r in rows:
+            cols = ix[ip[r]:ip[r + 1]]
+            ref_row = np.array([want[k].get((r, c), 0.0) for c in cols])
+            per_entry(g32[k][ip[r]:ip[r + 1]], ref_row, np.array([0, len(cols)]), 1e-6)
+            per_entry(g64[k][ip[r]:ip[r + 1]], ref_row, np.array([0, len(cols)]), 1e-12)
