@@ -60,7 +60,7 @@ void free_device_space(DeviceSpace* d) {
   void* ptrs[] = {d->cells,   d->xyz_hi,  d->xyz_lo,    d->xyz,           d->ext_mask,
                   d->ent_ptr, d->inc_cell, d->inc_rec,  d->indptr,        d->indices,
                   d->cell_dofs, d->boundary_dofs, d->kc_f, d->km_f, d->kt_f,
-                  d->kc_d,    d->km_d,    d->kt_d, d->bidx, d->g_f, d->g_d, d->h_f, d->h_d,
+                  d->kc_d,    d->km_d,    d->kt_d, d->bidx, d->g_f, d->g_d, d->g2_f, d->h_f, d->h_d,
                   d->kab_f, d->kab_d, d->ext_facets, d->ntff_pts, d->bdof_pt,
                   d->bin_ptr, d->bin_cells, d->cell_pos, d->task_ent, d->task_meta,
                   d->step_words};

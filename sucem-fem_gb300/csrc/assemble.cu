@@ -87,15 +87,19 @@ __device__ __forceinline__ int sym_p(int m) { return m < 3 ? m : (m == 5 ? 1 : 0
 __device__ __forceinline__ int sym_q(int m) { return m < 3 ? m : (m == 3 ? 1 : 2); }
 
 // ---- kernel 1: per-cell coefficients ----
-template <typename Real>
+// Computed in Real, written as Out (the assembly's precision).  HILO (Real
+// double, Out float): each coefficient is written as float hi + lo, the 12
+// hi values then the 12 rests (24 per cell), for the compensated
+// single-precision contraction.
+template <typename Real, typename Out, bool HILO>
 __global__ void cell_geometry_kernel(int64_t nt, const int4* __restrict__ cells,
                                      const float4* __restrict__ hi, const float4* __restrict__ lo,
                                      const double* __restrict__ xyz,
                                      const uint8_t* __restrict__ ext_mask,
                                      const int32_t* __restrict__ bidx,
-                                     const Real* __restrict__ eps_r,
-                                     const Real* __restrict__ mu_inv, Real* __restrict__ g,
-                                     Real* __restrict__ h, bool with_b, Real tscale,
+                                     const Out* __restrict__ eps_r,
+                                     const Out* __restrict__ mu_inv, Out* __restrict__ g,
+                                     Out* __restrict__ h, bool with_b, Real tscale,
                                      Real hscale) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nt) return;
@@ -118,8 +122,8 @@ __global__ void cell_geometry_kernel(int64_t nt, const int4* __restrict__ cells,
   Ji[2][0] = m02 * id;
   Ji[2][1] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]) * id;
   Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-  const Real sS = (mu_inv ? __ldg(mu_inv + c) : Real(1)) / adet;
-  const Real sT = (eps_r ? __ldg(eps_r + c) : Real(1)) * adet * tscale;
+  const Real sS = (mu_inv ? Real(__ldg(mu_inv + c)) : Real(1)) / adet;
+  const Real sT = (eps_r ? Real(__ldg(eps_r + c)) : Real(1)) * adet * tscale;
   Real out[12];
 #pragma unroll
   for (int m = 0; m < 6; ++m) {
@@ -127,8 +131,17 @@ __global__ void cell_geometry_kernel(int64_t nt, const int4* __restrict__ cells,
     out[m] = (J[0][pp] * J[0][qq] + J[1][pp] * J[1][qq] + J[2][pp] * J[2][qq]) * sS;
     out[6 + m] = (Ji[pp][0] * Ji[qq][0] + Ji[pp][1] * Ji[qq][1] + Ji[pp][2] * Ji[qq][2]) * sT;
   }
+  if (HILO) {
 #pragma unroll
-  for (int m = 0; m < 12; ++m) g[c * 12 + m] = out[m];
+    for (int m = 0; m < 12; ++m) {
+      const Out gh = Out(out[m]);
+      g[c * 24 + m] = gh;
+      g[c * 24 + 12 + m] = Out(out[m] - Real(gh));
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < 12; ++m) g[c * 12 + m] = Out(out[m]);
+  }
   if (!with_b) return;
   const int hb = __ldg(&bidx[c]);
   if (hb < 0) return;
@@ -162,9 +175,9 @@ __global__ void cell_geometry_kernel(int64_t nt, const int4* __restrict__ cells,
       c1 = -(a[0] * b[0] + a[1] * b[1] + a[2] * b[2]) * ita;
       c2 = (a[0] * a[0] + a[1] * a[1] + a[2] * a[2]) * ita;
     }
-    h[(int64_t)hb * 12 + f * 3 + 0] = c0;
-    h[(int64_t)hb * 12 + f * 3 + 1] = c1;
-    h[(int64_t)hb * 12 + f * 3 + 2] = c2;
+    h[(int64_t)hb * 12 + f * 3 + 0] = Out(c0);
+    h[(int64_t)hb * 12 + f * 3 + 1] = Out(c1);
+    h[(int64_t)hb * 12 + f * 3 + 2] = Out(c2);
   }
 }
 
@@ -289,6 +302,9 @@ struct EntCfg {
   static constexpr int NMAT = MODE == 1 ? 1 : 2;       // fused A, or S and T
   static constexpr int V = DPE * NMAT;                 // values per slot (main accumulator)
   static constexpr int VB = DPE;                       // values per slot (B / Im accumulator)
+  // cell coefficients per cell: 12, or 24 (float hi + lo) for the
+  // compensated single-precision separate matrices
+  static constexpr int NG = (MODE == 0 && sizeof(Real) == 4) ? 24 : 12;
 };
 
 struct StepRec {
@@ -305,13 +321,14 @@ __device__ __forceinline__ StepRec load_step(const uint32_t* blk, int lane) {
   return r;
 }
 
-template <typename Real>
-__device__ __forceinline__ void load_g(const Real* gcell, int c, Real g[12]) {
+template <typename Real, int NG>
+__device__ __forceinline__ void load_g(const Real* gcell, int c, Real* g) {
   if (c >= 0) {
-    load12<Real>(gcell + (int64_t)c * 12, g);
+#pragma unroll
+    for (int q = 0; q < NG / 12; ++q) load12<Real>(gcell + (int64_t)c * NG + 12 * q, g + 12 * q);
   } else {
 #pragma unroll
-    for (int m = 0; m < 12; ++m) g[m] = Real(0);
+    for (int m = 0; m < NG; ++m) g[m] = Real(0);
   }
 }
 
@@ -331,7 +348,7 @@ __device__ __forceinline__ bool face_holds(int f) {
 
 // one step of local entity LE: contract, then add into the lane's rows
 template <int ORDER, typename Real, int MODE, bool FACE, int LE, bool BND>
-__device__ __forceinline__ void ent_step(const StepRec& r, const Real g[12], Real* acc, Real* bacc,
+__device__ __forceinline__ void ent_step(const StepRec& r, const Real* g, Real* acc, Real* bacc,
                                          const EntArgs& p, const Real* __restrict__ hcell,
                                          const Real* __restrict__ kt) {
   using C = EntCfg<ORDER, Real, MODE>;
@@ -388,15 +405,15 @@ __device__ __forceinline__ void ent_steps(const uint8_t* trip, int& s, int nstep
   if constexpr (LE < NLE) {
     using C = EntCfg<ORDER, Real, MODE>;
     for (int t = 0; t < trip[LE]; ++t, ++s) {
-      Real g1[12];
-      load_g<Real>(gcell, s + 1 < nsteps ? r1.cell : -1, g1);
+      Real g1[C::NG];
+      load_g<Real, C::NG>(gcell, s + 1 < nsteps ? r1.cell : -1, g1);
       StepRec r2;
       r2.cell = -1;
       if (s + 2 < nsteps) r2 = load_step<C::PL>(blk0 + (int64_t)(s + 2) * C::WPS, lane);
       ent_step<ORDER, Real, MODE, FACE, LE, BND>(r0, g0, acc, bacc, p, hcell, kt);
       r0 = r1;
 #pragma unroll
-      for (int m = 0; m < 12; ++m) g0[m] = g1[m];
+      for (int m = 0; m < C::NG; ++m) g0[m] = g1[m];
       r1 = r2;
     }
     ent_steps<ORDER, Real, MODE, FACE, LE + 1, NLE, BND>(trip, s, nsteps, blk0, lane, r0, g0, r1,
@@ -413,18 +430,28 @@ __device__ __forceinline__ void ent_task(int64_t task, int lane, Real* acc, Real
   using C = EntCfg<ORDER, Real, MODE>;
   constexpr int DPE = C::DPE;
   const int P = p.P;
-  // clear the warp's accumulators (each lane's P slots)
+  // the lane's entity and its rows' CSR offset and length: loaded first so
+  // that their latency hides under the steps (the write phase needs them)
+  const int my_ent = __ldg(&p.task_ent[task * 32 + lane]);
+  int my_off = 0, my_len = 0;
+  if (my_ent >= 0) {
+    my_off = __ldg(&p.indptr[(int64_t)DPE * my_ent]);
+    my_len = __ldg(&p.indptr[(int64_t)DPE * my_ent + 1]) - my_off;
+  }
+  const int4 meta = __ldg(&p.task_meta[task]);
+  // clear the warp's accumulators (each lane's P slots; 16-byte stores, the
+  // regions start 16-byte aligned and hold a multiple of 16 bytes)
   {
-    Real* a0 = acc - (int64_t)lane * P * C::V;
-    const int words = 32 * P * C::V;
-    for (int i = lane; i < words; i += 32) a0[i] = Real(0);
+    float4* a0 = reinterpret_cast<float4*>(acc - (int64_t)lane * P * C::V);
+    const int n4 = 32 * P * C::V * (int)sizeof(Real) / 16;
+    for (int i = lane; i < n4; i += 32) a0[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (BND) {
-      Real* b0 = bacc - (int64_t)lane * P * C::VB;
-      for (int i = lane; i < 32 * P * C::VB; i += 32) b0[i] = Real(0);
+      float4* b0 = reinterpret_cast<float4*>(bacc - (int64_t)lane * P * C::VB);
+      const int m4 = 32 * P * C::VB * (int)sizeof(Real) / 16;
+      for (int i = lane; i < m4; i += 32) b0[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
   }
   __syncwarp();
-  const int4 meta = p.task_meta[task];
   uint8_t trip[8];
   *reinterpret_cast<int*>(&trip[0]) = meta.y;
   *reinterpret_cast<int*>(&trip[4]) = meta.z;
@@ -436,8 +463,8 @@ __device__ __forceinline__ void ent_task(int64_t task, int lane, Real* acc, Real
   r0.cell = r1.cell = -1;
   if (nsteps > 0) r0 = load_step<C::PL>(blk0, lane);
   if (nsteps > 1) r1 = load_step<C::PL>(blk0 + C::WPS, lane);
-  Real g0[12];
-  load_g<Real>(gcell, r0.cell, g0);
+  Real g0[C::NG];
+  load_g<Real, C::NG>(gcell, r0.cell, g0);
   int s = 0;
   bool done = false;
   if constexpr (ORDER == 2) {
@@ -452,14 +479,13 @@ __device__ __forceinline__ void ent_task(int64_t task, int lane, Real* acc, Real
                                                    bacc, p, gcell, hcell, kt);
   __syncwarp();
   // write each lane's rows, one entity at a time, coalesced
-  const int my_ent = p.task_ent[task * 32 + lane];
   const Real* acc0 = acc - (int64_t)lane * P * C::V;
   const Real* bacc0 = BND ? bacc - (int64_t)lane * P * C::VB : nullptr;
   for (int l = 0; l < 32; ++l) {
     const int k = __shfl_sync(0xffffffffu, my_ent, l);
+    const int off = __shfl_sync(0xffffffffu, my_off, l);
+    const int L = __shfl_sync(0xffffffffu, my_len, l);
     if (k < 0) continue;
-    const int off = __ldg(&p.indptr[(int64_t)DPE * k]);
-    const int L = __ldg(&p.indptr[(int64_t)DPE * k + 1]) - off;
     const Real* al = acc0 + (int64_t)l * P * C::V;
     const Real* bl = BND ? bacc0 + (int64_t)l * P * C::VB : nullptr;
     for (int idx = lane; idx < DPE * L; idx += 32) {
@@ -591,11 +617,24 @@ cudaError_t launch_t(DeviceSpace& d, const AssembleArgs& a, cudaStream_t stream)
   {
     const int threads = 256;
     const int64_t blocks = (d.nt + threads - 1) / threads;
-    const Real tscale = MODE == 1 ? Real(-a.k0 * a.k0) : Real(1);
-    const Real hscale = MODE == 1 ? Real(a.k0) : Real(1);
-    cell_geometry_kernel<Real><<<(unsigned)blocks, threads, 0, stream>>>(
-        d.nt, d.cells, d.xyz_hi, d.xyz_lo, d.xyz, d.ext_mask, d.bidx, (const Real*)a.eps_r,
-        (const Real*)a.mu_r_inv, g, h, WITH_B, tscale, hscale);
+    if constexpr (C::NG == 24) {
+      // separate single-precision matrices: coefficients from FP64
+      // geometry as float hi + lo (see contract::Dot2)
+      if (!d.g2_f) {
+        err = cudaMalloc((void**)&d.g2_f, sizeof(float) * 24 * std::max<int64_t>(d.nt, 1));
+        if (err != cudaSuccess) return err;
+      }
+      g = reinterpret_cast<Real*>(d.g2_f);
+      cell_geometry_kernel<double, float, true><<<(unsigned)blocks, threads, 0, stream>>>(
+          d.nt, d.cells, d.xyz_hi, d.xyz_lo, d.xyz, d.ext_mask, d.bidx, (const float*)a.eps_r,
+          (const float*)a.mu_r_inv, (float*)g, (float*)h, WITH_B, 1.0, 1.0);
+    } else {
+      const Real tscale = MODE == 1 ? Real(-a.k0 * a.k0) : Real(1);
+      const Real hscale = MODE == 1 ? Real(a.k0) : Real(1);
+      cell_geometry_kernel<Real, Real, false><<<(unsigned)blocks, threads, 0, stream>>>(
+          d.nt, d.cells, d.xyz_hi, d.xyz_lo, d.xyz, d.ext_mask, d.bidx, (const Real*)a.eps_r,
+          (const Real*)a.mu_r_inv, g, h, WITH_B, tscale, hscale);
+    }
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
   }
@@ -642,7 +681,7 @@ cudaError_t launch_cells_t(DeviceSpace& d, const AssembleArgs& a, cudaStream_t s
   {
     const int threads = 256;
     const int64_t blocks = (d.nt + threads - 1) / threads;
-    cell_geometry_kernel<Real><<<(unsigned)blocks, threads, 0, stream>>>(
+    cell_geometry_kernel<Real, Real, false><<<(unsigned)blocks, threads, 0, stream>>>(
         d.nt, d.cells, d.xyz_hi, d.xyz_lo, d.xyz, d.ext_mask, d.bidx, (const Real*)a.eps_r,
         (const Real*)a.mu_r_inv, g, h, WITH_B, Real(1), Real(1));
     err = cudaGetLastError();

@@ -45,6 +45,7 @@ struct DeviceSpace {
   // per-cell coefficient scratch of the assembly (allocated on first use)
   float* g_f = nullptr;           // nt*12
   double* g_d = nullptr;
+  float* g2_f = nullptr;          // nt*24: float hi + lo coefficients (separate FP32 matrices)
   float* h_f = nullptr;           // nb*12
   double* h_d = nullptr;
   // entity-per-lane assembly schedule (orders 1-2, see Space)

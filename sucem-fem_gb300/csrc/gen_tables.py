@@ -378,7 +378,7 @@ def _dot2(terms):
     parts = []
     for m, c in terms:
         hi = _f32(c)
-        parts.append("t.add(g[%d], %r, %rf, %rf)" % (m, float(c), float(hi), float(_f32(c - hi))))
+        parts.append("t.add(g, %d, %r, %rf, %rf)" % (m, float(c), float(hi), float(_f32(c - hi))))
     return "Dot2<R> t; " + "; ".join(parts) + ";"
 
 
@@ -394,8 +394,10 @@ def contract_code():
           (has_s false when every KC constant of the entry is zero, s = 0);
           t is a compensated dot product (Dot2): in single precision the
           mass-matrix terms of an element entry can cancel to a few percent
-          of their size, and a plain FMA chain then loses the 1e-6 relative
-          accuracy the separate matrices are held to
+          of their size, and a plain FMA chain (or coefficients rounded to
+          float) then loses the 1e-6 relative accuracy the separate matrices
+          are held to; the single-precision split form therefore takes g as
+          24 values, the 12 coefficients rounded to float and their rests
 
     for every column b of the cell and the entity's local DOFs a (j-th):
     edge LE of order k -> a = k*LE + j, face LE of order 2 -> a = 12 + 2*LE + j.
@@ -415,30 +417,35 @@ def contract_code():
            "#define SUCEM_FSUB(a, b) ((a) - (b))",
            "#endif",
            "",
-           "// sum of g * k over the added terms: float keeps s + c with every",
-           "// product split exactly (p + e) and every sum step exactly (TwoSum),",
-           "// k given as float hi + lo (hi the nearest float of k); the",
-           "// intrinsics are never fused into FMAs.  double: a plain FMA chain.",
+           "// sum of g[m] * k over the added terms.  float: the coefficients come",
+           "// as hi + lo pairs (g[m] + g[m + 12]) and so do the constants (kh the",
+           "// nearest float of k, klo the rest); s + c is kept with every product",
+           "// hi * kh split exactly (p + e) and every sum step exact (TwoSum), and",
+           "// the small cross terms added to c; the intrinsics are never fused",
+           "// into FMAs.  double: a plain FMA chain.",
            "template <class R>",
            "struct Dot2;",
            "template <>",
            "struct Dot2<float> {",
            "  float s = 0.f, c = 0.f;",
-           "  __device__ __forceinline__ void add(float g, double, float kh, float klo) {",
-           "    const float p = SUCEM_FMUL(g, kh);",
-           "    const float e = fmaf(g, kh, -p);",
+           "  __device__ __forceinline__ void add(const float* g, int m, double, float kh, float klo) {",
+           "    const float gh = g[m], gl = g[m + 12];",
+           "    const float p = SUCEM_FMUL(gh, kh);",
+           "    const float e = fmaf(gh, kh, -p);",
            "    const float t = SUCEM_FADD(s, p);",
            "    const float z = SUCEM_FSUB(t, s);",
            "    const float d = SUCEM_FADD(SUCEM_FSUB(s, SUCEM_FSUB(t, z)), SUCEM_FSUB(p, z));",
            "    s = t;",
-           "    c = fmaf(g, klo, SUCEM_FADD(c, SUCEM_FADD(d, e)));",
+           "    c = fmaf(gh, klo, fmaf(gl, kh, SUCEM_FADD(c, SUCEM_FADD(d, e))));",
            "  }",
            "  __device__ __forceinline__ float sum() const { return SUCEM_FADD(s, c); }",
            "};",
            "template <>",
            "struct Dot2<double> {",
            "  double s = 0.0;",
-           "  __device__ __forceinline__ void add(double g, double k, float, float) { s = fma(g, k, s); }",
+           "  __device__ __forceinline__ void add(const double* g, int m, double k, float, float) {",
+           "    s = fma(g[m], k, s);",
+           "  }",
            "  __device__ __forceinline__ double sum() const { return s; }",
            "};",
            "",

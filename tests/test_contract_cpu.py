@@ -39,10 +39,11 @@ void rows(const double* g, const float* gf) {
 }
 int main() {
   double g[12];
-  float gf[12];
+  float gf[24];  // single precision: the coefficients as float hi + lo
   for (int i = 0; i < 12; ++i) {
     if (std::scanf("%%lf", &g[i]) != 1) return 1;
     gf[i] = (float)g[i];
+    gf[i + 12] = (float)(g[i] - (double)gf[i]);
   }
   rows<1, false, 0>(g, gf); rows<1, false, 1>(g, gf); rows<1, false, 2>(g, gf);
   rows<1, false, 3>(g, gf); rows<1, false, 4>(g, gf); rows<1, false, 5>(g, gf);
@@ -87,15 +88,13 @@ def test_generated_rows_match_oracle(driver, seed):
     out = subprocess.run([driver], input=" ".join("%.17g" % x for x in g), capture_output=True,
                          text=True, check=True).stdout.split("\n")
     ref = {o: fem.element_matrices(coords, cells, o, [1.0], [1.0]) for o in (1, 2)}
-    # the same element with the single-precision metric (what the float
-    # kernel is given): its exact mass rows and the size of their terms
+    # exact mass rows of the element and the size of their terms
     from oracle import n1curl_exact
-    g32 = g.astype(np.float32).astype(np.float64)
     exact32, termsum = {}, {}
     for o in (1, 2):
         Km = fem._sym6(n1curl_exact.reference_tensors(o)["mass"])
-        exact32[o] = np.einsum("m,mab->ab", g32[6:], Km)
-        termsum[o] = np.einsum("m,mab->ab", np.abs(g32[6:]), np.abs(Km))
+        exact32[o] = np.einsum("m,mab->ab", g[6:], Km)
+        termsum[o] = np.einsum("m,mab->ab", np.abs(g[6:]), np.abs(Km))
     seen = 0
     for line in out:
         if not line:
@@ -108,8 +107,9 @@ def test_generated_rows_match_oracle(driver, seed):
         if kind == "f":
             assert abs(float(parts[6]) - (S[a, b] + T[a, b])) <= 1e-13 * scale
         elif kind == "t":
-            # compensated single-precision mass entry: within a few units of
-            # float rounding of its exact value even where its terms cancel
+            # compensated single-precision mass entry (coefficients as float
+            # hi + lo): within float rounding of its exact value even where
+            # its terms cancel
             e = exact32[o][a, b]
             assert abs(float(parts[7]) - e) <= 1.2e-7 * abs(e) + 1e-12 * termsum[o][a, b]
         else:

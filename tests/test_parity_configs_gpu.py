@@ -99,9 +99,11 @@ def test_config2_matrices_per_entry(config2, rb):
 
 def test_config2_fused_complex_matrix(config2):
     """The FP32 solve factorises A = S - k0^2 T + j k0 B assembled in one
-    pass (complex64).  S and k0^2 T cancel in part (the box is several
-    wavelengths across), so A is held to the FP32 bar relative to the size
-    of its two parts: |A32 - A| <= 1e-6 (|S| + k0^2 |T| + k0 |B|) per entry."""
+    pass (complex64, plain FP32 arithmetic: it is the input of the
+    single-precision factorisation, whose error the FP64 refinement removes,
+    not one of the reference's matrices).  Inside an element the S and
+    -k0^2 T terms of an entry can cancel, so A is held to the FP32 bar
+    relative to its row: |A32 - A| <= 1e-6 max_row(|S| + k0^2 |T| + k0 |B|)."""
     import torch
     from sucemfem import _device
     from sucemfem._native import call, ptr
@@ -118,7 +120,8 @@ def test_config2_fused_complex_matrix(config2):
     size = np.abs(ref.S.data) + k0 ** 2 * np.abs(ref.T.data) + k0 * np.abs(ref.B.data)
     rows = np.repeat(np.arange(V.n), np.diff(ref.indptr))
     rowmax = np.maximum.reduceat(size, ref.indptr[:-1].astype(np.int64))[rows]
-    err = np.abs(a - aref) / np.maximum(size, 1e-6 * rowmax)
+    err = np.abs(a - aref) / rowmax
+    print("config 2, fused complex64: max |A32 - A| / row scale %.2e" % err.max())
     assert err.max() <= 1e-6, err.max()
 
 
