@@ -83,7 +83,8 @@ int sucem_space_sizes(const sucem_space* sp, int64_t* out);
                                        DOF: point, tangent (DOF(u) = u(point).tangent) */
 #define SUCEM_COPY_TASK_ENT 12     /* int32[n_tasks*32] assembly schedule: entity of each lane */
 #define SUCEM_COPY_TASK_META 13    /* int32[n_tasks*4] first step block, steps per local entity
-                                      index (8 bytes), flags (bit 0: faces) */
+                                      index (8 bytes), flags (bit 0: faces; bits 8-23: the
+                                      task's longest row, made odd) */
 #define SUCEM_COPY_STEP_WORDS 14   /* uint32[n_step_blocks*(1+slot_planes)*32] step blocks */
 int sucem_space_copy(const sucem_space* sp, int what, void* host_dst);
 

@@ -60,12 +60,14 @@ void free_device_space(DeviceSpace* d) {
   void* ptrs[] = {d->cells,   d->xyz_hi,  d->xyz_lo,    d->xyz,           d->ext_mask,
                   d->ent_ptr, d->inc_cell, d->inc_rec,  d->indptr,        d->indices,
                   d->cell_dofs, d->boundary_dofs, d->kc_f, d->km_f, d->kt_f,
-                  d->kc_d,    d->km_d,    d->kt_d, d->bidx, d->g_f, d->g_d, d->g2_f, d->h_f, d->h_d,
+                  d->kc_d,    d->km_d,    d->kt_d, d->bidx, d->g_f, d->g_d, d->g2_f, d->h2_f, d->kt_lo_f, d->h_f, d->h_d,
                   d->kab_f, d->kab_d, d->ext_facets, d->ntff_pts, d->bdof_pt,
                   d->bin_ptr, d->bin_cells, d->cell_pos, d->task_ent, d->task_meta,
                   d->step_words};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (auto& kv : d->task_blocks)
+    if (kv.second.first) cudaFree(kv.second.first);
   cudaSetDevice(prev);
   delete d;
 }
@@ -157,6 +159,9 @@ std::string upload_space(Space& s, int device) {
   UP(kc_f, kcf.data(), kcf.size());
   UP(km_f, kmf.data(), kmf.size());
   UP(kt_f, kff.data(), kff.size());
+  std::vector<float> kfl(kf.size());
+  for (size_t i = 0; i < kf.size(); ++i) kfl[i] = (float)(kf[i] - (double)kff[i]);
+  UP(kt_lo_f, kfl.data(), kfl.size());
   UP(kc_d, kc.data(), kc.size());
   UP(km_d, km.data(), km.size());
   UP(kt_d, kf.data(), kf.size());
@@ -167,6 +172,8 @@ std::string upload_space(Space& s, int device) {
   UP(task_ent, s.task_ent.data(), s.task_ent.size());
   UP(task_meta, reinterpret_cast<const int4*>(s.task_meta.data()), s.task_meta.size() / 4);
   UP(step_words, s.step_words.data(), s.step_words.size());
+  d->task_P.resize(s.n_tasks);
+  for (int64_t t = 0; t < s.n_tasks; ++t) d->task_P[t] = (uint16_t)((s.task_meta[t * 4 + 3] >> 8) & 0xffff);
   d->n_tasks = s.n_tasks;
   d->n_tasks_interior = s.n_tasks_interior;
   d->slot_planes = s.slot_planes;

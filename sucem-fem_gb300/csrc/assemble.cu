@@ -89,8 +89,9 @@ __device__ __forceinline__ int sym_q(int m) { return m < 3 ? m : (m == 3 ? 1 : 2
 // ---- kernel 1: per-cell coefficients ----
 // Computed in Real, written as Out (the assembly's precision).  HILO (Real
 // double, Out float): each coefficient is written as float hi + lo, the 12
-// hi values then the 12 rests (24 per cell), for the compensated
-// single-precision contraction.
+// hi values then the 12 rests (24 per cell, and likewise the 12 tangential
+// coefficients of a boundary cell), for the compensated single-precision
+// contraction.
 template <typename Real, typename Out, bool HILO>
 __global__ void cell_geometry_kernel(int64_t nt, const int4* __restrict__ cells,
                                      const float4* __restrict__ hi, const float4* __restrict__ lo,
@@ -175,9 +176,17 @@ __global__ void cell_geometry_kernel(int64_t nt, const int4* __restrict__ cells,
       c1 = -(a[0] * b[0] + a[1] * b[1] + a[2] * b[2]) * ita;
       c2 = (a[0] * a[0] + a[1] * a[1] + a[2] * a[2]) * ita;
     }
-    h[(int64_t)hb * 12 + f * 3 + 0] = Out(c0);
-    h[(int64_t)hb * 12 + f * 3 + 1] = Out(c1);
-    h[(int64_t)hb * 12 + f * 3 + 2] = Out(c2);
+    const Real cc[3] = {c0, c1, c2};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const Out hv = Out(cc[q]);
+      if (HILO) {
+        h[(int64_t)hb * 24 + f * 3 + q] = hv;
+        h[(int64_t)hb * 24 + 12 + f * 3 + q] = Out(cc[q] - Real(hv));
+      } else {
+        h[(int64_t)hb * 12 + f * 3 + q] = hv;
+      }
+    }
   }
 }
 
@@ -227,9 +236,9 @@ __device__ __forceinline__ void load12<double>(const double* p, double out[12]) 
 // Boundary entities (on an exterior facet) are in tasks of their own that
 // also accumulate the ABC matrix B from the cells' tangential coefficients
 // h and the face tables KT (read through L1: the cells concerned are few).
-// Blocks hold either w_int interior tasks or fewer boundary tasks, so that
-// both fit the same shared memory.
-constexpr int kEntWarps = 4;
+// The host packs consecutive tasks into blocks (up to a per-variant number)
+// within a shared-memory budget: a task's accumulators take 32 x P slot
+// vectors, P its longest row, so blocks of short rows hold more tasks.
 
 template <int V, typename Real>
 struct SlotVec;  // V values of one slot, moved with the widest shared access
@@ -285,13 +294,17 @@ struct EntArgs {
   const int32_t* indptr;       // n+1
   const int32_t* bidx;         // nt
   const uint8_t* ext_mask;     // nt
-  int64_t n_tasks;             // tasks handled by this launch
-  int64_t n_int_tasks;         // of which interior (the first ones)
+  const int32_t* blocks;       // first task of each block (+ end)
   int64_t n_int_blocks;        // blocks [0, n_int_blocks) take interior tasks
-  int w_int;                   // tasks per interior block (= warps per block)
-  int w_bnd;                   // tasks per boundary block
-  int P;                       // per-lane accumulator stride in slots (odd)
 };
+
+// Block shape per kernel variant (EntCfg::BLOCK_WARPS / BLOCK_BYTES): the
+// fused single-precision kernel (< 85 registers) takes blocks of 8 warps
+// within 68 KB, so three blocks share an SM's shared memory and registers,
+// i.e. 24 warps where the rows are short enough (order-2 faces: 8 tasks of
+// 33 slots) and fewer for the longest rows (3 tasks of 75 slots); the
+// register-heavy variants (double precision, compensated separate
+// matrices) take blocks of 2 warps within 40 KB.
 
 template <int ORDER, typename Real, int MODE>
 struct EntCfg {
@@ -300,12 +313,28 @@ struct EntCfg {
   static constexpr int PL = (ND + 3) / 4;              // slot planes of a step block
   static constexpr int WPS = (1 + PL) * 32;            // words per step block
   static constexpr int NMAT = MODE == 1 ? 1 : 2;       // fused A, or S and T
-  static constexpr int V = DPE * NMAT;                 // values per slot (main accumulator)
-  static constexpr int VB = DPE;                       // values per slot (B / Im accumulator)
-  // cell coefficients per cell: 12, or 24 (float hi + lo) for the
-  // compensated single-precision separate matrices
-  static constexpr int NG = (MODE == 0 && sizeof(Real) == 4) ? 24 : 12;
+  // separate single-precision matrices: compensated throughout (element
+  // sums by contract::Dot2, accumulation in double-float hi + lo slots)
+  static constexpr bool DD = MODE == 0 && sizeof(Real) == 4;
+  // values per slot of the main accumulator: [S0 S1 T0 T1] / [A0 A1]; DD:
+  // per row j [S hi, S lo, T hi, T lo]
+  static constexpr int V = DD ? 4 * DPE : DPE * NMAT;
+  static constexpr int VB = DD ? 2 * DPE : DPE;        // B / Im accumulator (DD: hi, lo per row)
+  // cell coefficients per cell: 12, or 24 (float hi + lo) when DD
+  static constexpr int NG = DD ? 24 : 12;
+  static constexpr bool LIGHT = MODE == 1 && sizeof(Real) == 4;
+  static constexpr int BLOCK_WARPS = LIGHT ? 8 : 2;          // most tasks per block
+  static constexpr int BLOCK_BYTES = (LIGHT ? 68 : 40) << 10;  // shared memory budget
 };
+
+// (hi, lo) += (xh, xl): TwoSum of the leading parts, rests added to lo
+__device__ __forceinline__ void dd_add(float& hi, float& lo, float xh, float xl) {
+  const float s = __fadd_rn(hi, xh);
+  const float z = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, z)), __fsub_rn(xh, z));
+  hi = s;
+  lo = __fadd_rn(lo, __fadd_rn(xl, e));
+}
 
 struct StepRec {
   int cell;
@@ -350,44 +379,70 @@ __device__ __forceinline__ bool face_holds(int f) {
 template <int ORDER, typename Real, int MODE, bool FACE, int LE, bool BND>
 __device__ __forceinline__ void ent_step(const StepRec& r, const Real* g, Real* acc, Real* bacc,
                                          const EntArgs& p, const Real* __restrict__ hcell,
-                                         const Real* __restrict__ kt) {
+                                         const Real* __restrict__ kt,
+                                         const float* __restrict__ kt_lo) {
   using C = EntCfg<ORDER, Real, MODE>;
   constexpr int ND = C::ND, DPE = C::DPE;
-  Real v[ND][C::V];
-#pragma unroll
-  for (int b = 0; b < ND; ++b)
-#pragma unroll
-    for (int q = 0; q < C::V; ++q) v[b][q] = Real(0);
-  if (MODE == 1) {
-    contract::Rows<ORDER, FACE, LE>::fused(g, [&](int j, int b, Real x) { v[b][j] = x; });
+  if constexpr (C::DD) {
+    // compensated: each element sum (unrounded s + c) straight into its
+    // double-float slot
+    if (r.cell >= 0)
+      contract::Rows<ORDER, FACE, LE>::split(
+          g, [&](int j, int b, const contract::Dot2<float>& sd, const contract::Dot2<float>& td) {
+            float4* q = reinterpret_cast<float4*>(acc + (slot_of(r, b) * DPE + j) * 4);
+            float4 t = *q;
+            dd_add(t.x, t.y, sd.s, sd.c);
+            dd_add(t.z, t.w, td.s, td.c);
+            *q = t;
+          });
   } else {
-    contract::Rows<ORDER, FACE, LE>::split(g, [&](int j, int b, Real sv, Real tv, bool) {
-      v[b][j] = sv;
-      v[b][DPE + j] = tv;
-    });
-  }
-  if (r.cell < 0) return;
+    Real v[ND][C::V];
 #pragma unroll
-  for (int b = 0; b < ND; ++b) SlotVec<C::V, Real>::add(acc + slot_of(r, b) * C::V, v[b]);
-  if (!BND) return;
+    for (int b = 0; b < ND; ++b)
+#pragma unroll
+      for (int q = 0; q < C::V; ++q) v[b][q] = Real(0);
+    if constexpr (MODE == 1) {
+      contract::Rows<ORDER, FACE, LE>::fused(g, [&](int j, int b, Real x) { v[b][j] = x; });
+    } else {
+      contract::Rows<ORDER, FACE, LE>::split(
+          g, [&](int j, int b, const contract::Dot2<Real>& sd, const contract::Dot2<Real>& td) {
+            v[b][j] = sd.s;
+            v[b][DPE + j] = td.s;
+          });
+    }
+    if (r.cell < 0) return;
+#pragma unroll
+    for (int b = 0; b < ND; ++b) SlotVec<C::V, Real>::add(acc + slot_of(r, b) * C::V, v[b]);
+  }
+  if (!BND || r.cell < 0) return;
   const int hb = __ldg(&p.bidx[r.cell]);
   if (hb < 0) return;
   const int mask = __ldg(&p.ext_mask[r.cell]);
+  const Real* hh = hcell + (int64_t)hb * (C::DD ? 24 : 12);
   for (int f = 0; f < 4; ++f) {
     if (!(mask >> f & 1) || !face_holds<FACE, LE>(f)) continue;
-    const Real h0 = __ldg(&hcell[(int64_t)hb * 12 + 3 * f]);
-    const Real h1 = __ldg(&hcell[(int64_t)hb * 12 + 3 * f + 1]);
-    const Real h2 = __ldg(&hcell[(int64_t)hb * 12 + 3 * f + 2]);
 #pragma unroll
     for (int j = 0; j < DPE; ++j) {
       const int a = FACE ? 12 + 2 * LE + j : DPE * LE + j;
-      const Real* k0p = kt + ((int64_t)(f * 3 + 0) * ND + a) * ND;
-      const Real* k1p = kt + ((int64_t)(f * 3 + 1) * ND + a) * ND;
-      const Real* k2p = kt + ((int64_t)(f * 3 + 2) * ND + a) * ND;
+      const int64_t k0i = ((int64_t)(f * 3 + 0) * ND + a) * ND;
+      const int64_t k1i = ((int64_t)(f * 3 + 1) * ND + a) * ND;
+      const int64_t k2i = ((int64_t)(f * 3 + 2) * ND + a) * ND;
 #pragma unroll 4
       for (int b = 0; b < ND; ++b) {
-        const Real bv = fma(h2, __ldg(k2p + b), fma(h1, __ldg(k1p + b), h0 * __ldg(k0p + b)));
-        bacc[slot_of(r, b) * C::VB + j] += bv;
+        if constexpr (C::DD) {
+          // h as hi + lo pairs (stride 12), KT as float hi + lo
+          contract::Dot2<float> bd;
+          bd.add(hh, 3 * f, 0.0, __ldg(kt + k0i + b), __ldg(kt_lo + k0i + b));
+          bd.add(hh, 3 * f + 1, 0.0, __ldg(kt + k1i + b), __ldg(kt_lo + k1i + b));
+          bd.add(hh, 3 * f + 2, 0.0, __ldg(kt + k2i + b), __ldg(kt_lo + k2i + b));
+          float* q = bacc + (slot_of(r, b) * DPE + j) * 2;
+          dd_add(q[0], q[1], bd.s, bd.c);
+        } else {
+          const Real bv = fma(__ldg(hh + 3 * f + 2), __ldg(kt + k2i + b),
+                              fma(__ldg(hh + 3 * f + 1), __ldg(kt + k1i + b),
+                                  __ldg(hh + 3 * f) * __ldg(kt + k0i + b)));
+          bacc[slot_of(r, b) * C::VB + j] += bv;
+        }
       }
     }
   }
@@ -401,7 +456,8 @@ __device__ __forceinline__ void ent_steps(const uint8_t* trip, int& s, int nstep
                                           StepRec& r1, Real* acc, Real* bacc, const EntArgs& p,
                                           const Real* __restrict__ gcell,
                                           const Real* __restrict__ hcell,
-                                          const Real* __restrict__ kt) {
+                                          const Real* __restrict__ kt,
+                                          const float* __restrict__ kt_lo) {
   if constexpr (LE < NLE) {
     using C = EntCfg<ORDER, Real, MODE>;
     for (int t = 0; t < trip[LE]; ++t, ++s) {
@@ -410,26 +466,27 @@ __device__ __forceinline__ void ent_steps(const uint8_t* trip, int& s, int nstep
       StepRec r2;
       r2.cell = -1;
       if (s + 2 < nsteps) r2 = load_step<C::PL>(blk0 + (int64_t)(s + 2) * C::WPS, lane);
-      ent_step<ORDER, Real, MODE, FACE, LE, BND>(r0, g0, acc, bacc, p, hcell, kt);
+      ent_step<ORDER, Real, MODE, FACE, LE, BND>(r0, g0, acc, bacc, p, hcell, kt, kt_lo);
       r0 = r1;
 #pragma unroll
       for (int m = 0; m < C::NG; ++m) g0[m] = g1[m];
       r1 = r2;
     }
     ent_steps<ORDER, Real, MODE, FACE, LE + 1, NLE, BND>(trip, s, nsteps, blk0, lane, r0, g0, r1,
-                                                        acc, bacc, p, gcell, hcell, kt);
+                                                        acc, bacc, p, gcell, hcell, kt, kt_lo);
   }
 }
 
 template <int ORDER, typename Real, int MODE, bool BND>
-__device__ __forceinline__ void ent_task(int64_t task, int lane, Real* acc, Real* bacc,
-                                         const EntArgs& p, const Real* __restrict__ gcell,
+__device__ __forceinline__ void ent_task(int64_t task, const int4 meta, int P, int lane,
+                                         Real* acc, Real* bacc, const EntArgs& p,
+                                         const Real* __restrict__ gcell,
                                          const Real* __restrict__ hcell,
-                                         const Real* __restrict__ kt, Real* S, Real* T, Real* B,
-                                         typename Cplx<Real>::T* A) {
+                                         const Real* __restrict__ kt,
+                                         const float* __restrict__ kt_lo, Real* S, Real* T,
+                                         Real* B, typename Cplx<Real>::T* A) {
   using C = EntCfg<ORDER, Real, MODE>;
   constexpr int DPE = C::DPE;
-  const int P = p.P;
   // the lane's entity and its rows' CSR offset and length: loaded first so
   // that their latency hides under the steps (the write phase needs them)
   const int my_ent = __ldg(&p.task_ent[task * 32 + lane]);
@@ -438,7 +495,6 @@ __device__ __forceinline__ void ent_task(int64_t task, int lane, Real* acc, Real
     my_off = __ldg(&p.indptr[(int64_t)DPE * my_ent]);
     my_len = __ldg(&p.indptr[(int64_t)DPE * my_ent + 1]) - my_off;
   }
-  const int4 meta = __ldg(&p.task_meta[task]);
   // clear the warp's accumulators (each lane's P slots; 16-byte stores, the
   // regions start 16-byte aligned and hold a multiple of 16 bytes)
   {
@@ -470,13 +526,13 @@ __device__ __forceinline__ void ent_task(int64_t task, int lane, Real* acc, Real
   if constexpr (ORDER == 2) {
     if (meta.w & 1) {
       ent_steps<ORDER, Real, MODE, true, 0, 4, BND>(trip, s, nsteps, blk0, lane, r0, g0, r1, acc,
-                                                    bacc, p, gcell, hcell, kt);
+                                                    bacc, p, gcell, hcell, kt, kt_lo);
       done = true;
     }
   }
   if (!done)
     ent_steps<ORDER, Real, MODE, false, 0, 6, BND>(trip, s, nsteps, blk0, lane, r0, g0, r1, acc,
-                                                   bacc, p, gcell, hcell, kt);
+                                                   bacc, p, gcell, hcell, kt, kt_lo);
   __syncwarp();
   // write each lane's rows, one entity at a time, coalesced
   const Real* acc0 = acc - (int64_t)lane * P * C::V;
@@ -488,49 +544,65 @@ __device__ __forceinline__ void ent_task(int64_t task, int lane, Real* acc, Real
     if (k < 0) continue;
     const Real* al = acc0 + (int64_t)l * P * C::V;
     const Real* bl = BND ? bacc0 + (int64_t)l * P * C::VB : nullptr;
-    for (int idx = lane; idx < DPE * L; idx += 32) {
-      const int j = DPE == 2 ? (idx >= L) : 0;
-      const int sl = idx - j * L;
-      const Real bval = BND ? bl[sl * C::VB + j] : Real(0);
-      if (MODE == 1) {
-        typename Cplx<Real>::T z;
-        z.x = al[sl * C::V + j];
-        z.y = bval;
-        A[(int64_t)off + idx] = z;
+    // lanes over the slots, both rows of a slot per lane: row j of the
+    // entity starts at off + j * L
+    for (int sl = lane; sl < L; sl += 32)
+#pragma unroll
+    for (int j = 0; j < DPE; ++j) {
+      const int idx = j * L + sl;
+      if constexpr (C::DD) {
+        const float* q = al + (sl * DPE + j) * 4;
+        if (S) S[(int64_t)off + idx] = __fadd_rn(q[0], q[1]);
+        if (T) T[(int64_t)off + idx] = __fadd_rn(q[2], q[3]);
+        if (B) B[(int64_t)off + idx] = BND ? __fadd_rn(bl[(sl * DPE + j) * 2], bl[(sl * DPE + j) * 2 + 1]) : 0.f;
       } else {
-        if (S) S[(int64_t)off + idx] = al[sl * C::V + j];
-        if (T) T[(int64_t)off + idx] = al[sl * C::V + DPE + j];
-        if (B) B[(int64_t)off + idx] = bval;
+        const Real bval = BND ? bl[sl * C::VB + j] : Real(0);
+        if (MODE == 1) {
+          typename Cplx<Real>::T z;
+          z.x = al[sl * C::V + j];
+          z.y = bval;
+          A[(int64_t)off + idx] = z;
+        } else {
+          if (S) S[(int64_t)off + idx] = al[sl * C::V + j];
+          if (T) T[(int64_t)off + idx] = al[sl * C::V + DPE + j];
+          if (B) B[(int64_t)off + idx] = bval;
+        }
       }
     }
   }
 }
 
 template <int ORDER, typename Real, int MODE, bool WITH_B>
-__global__ void __launch_bounds__(kEntWarps * 32)
+__global__ void __launch_bounds__(EntCfg<ORDER, Real, MODE>::BLOCK_WARPS * 32)
     assemble_entities_kernel(EntArgs p, const Real* __restrict__ gcell,
-                             const Real* __restrict__ hcell, const Real* __restrict__ kt, Real* S,
-                             Real* T, Real* B, typename Cplx<Real>::T* A) {
+                             const Real* __restrict__ hcell, const Real* __restrict__ kt,
+                             const float* __restrict__ kt_lo, Real* S, Real* T, Real* B,
+                             typename Cplx<Real>::T* A) {
   using C = EntCfg<ORDER, Real, MODE>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Real* sm = reinterpret_cast<Real*>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t main_words = (int64_t)32 * p.P * C::V;
-  if ((int64_t)blockIdx.x < p.n_int_blocks) {
-    const int64_t task = (int64_t)blockIdx.x * p.w_int + warp;
-    if (task >= p.n_int_tasks) return;
-    Real* acc = sm + warp * main_words + (int64_t)lane * p.P * C::V;
-    ent_task<ORDER, Real, MODE, false>(task, lane, acc, nullptr, p, gcell, hcell, kt, S, T, B, A);
-  } else if (WITH_B) {
-    if (warp >= p.w_bnd) return;
-    const int64_t task = p.n_int_tasks + ((int64_t)blockIdx.x - p.n_int_blocks) * p.w_bnd + warp;
-    if (task >= p.n_tasks) return;
-    const int64_t bwords = (int64_t)32 * p.P * C::VB;
-    Real* base = sm + warp * (main_words + bwords);
-    Real* acc = base + (int64_t)lane * p.P * C::V;
-    Real* bacc = base + main_words + (int64_t)lane * p.P * C::VB;
-    ent_task<ORDER, Real, MODE, WITH_B>(task, lane, acc, bacc, p, gcell, hcell, kt, S, T, B, A);
+  const int64_t t0 = __ldg(&p.blocks[blockIdx.x]), t1 = __ldg(&p.blocks[blockIdx.x + 1]);
+  const int64_t task = t0 + warp;
+  if (task >= t1) return;
+  const bool bnd = WITH_B && (int64_t)blockIdx.x >= p.n_int_blocks;
+  const int words = bnd ? C::V + C::VB : C::V;  // per slot and lane
+  // this warp's accumulators follow those of the block's earlier tasks
+  int64_t off = 0;
+  for (int i = 0; i < warp; ++i) off += 32LL * ((__ldg(&p.task_meta[t0 + i].w) >> 8) & 0xffff) * words;
+  const int4 meta = __ldg(&p.task_meta[task]);
+  const int P = (meta.w >> 8) & 0xffff;
+  Real* base = sm + off;
+  if constexpr (WITH_B) {
+    if (bnd) {
+      ent_task<ORDER, Real, MODE, true>(task, meta, P, lane, base + (int64_t)lane * P * C::V,
+                                        base + 32LL * P * C::V + (int64_t)lane * P * C::VB, p,
+                                        gcell, hcell, kt, kt_lo, S, T, B, A);
+      return;
+    }
   }
+  ent_task<ORDER, Real, MODE, false>(task, meta, P, lane, base + (int64_t)lane * P * C::V,
+                                     nullptr, p, gcell, hcell, kt, kt_lo, S, T, B, A);
 }
 
 // Orders 3-4: one block per cell (grid-stride over the cells), a thread per
@@ -607,6 +679,55 @@ cudaError_t ensure_scratch(DeviceSpace& d, Real** g, Real** h) {
   return cudaSuccess;
 }
 
+// Blocks of the entity kernel for a slot size (bytes per accumulator slot
+// and lane: interior tasks, boundary tasks): consecutive tasks share a block
+// while their accumulators fit `budget` bytes and at most `warps` tasks;
+// interior tasks first, then (with B) boundary tasks.  Built once per layout
+// and kept with the space.
+cudaError_t task_blocks(DeviceSpace& d, int slot_int, int slot_bnd, bool with_b, int warps,
+                        int budget, const DeviceSpace::TaskBlocks** out) {
+  const int key = slot_int | (slot_bnd << 8) | ((with_b ? 1 : 0) << 16) | (warps << 17) |
+                  ((budget >> 10) << 21);
+  auto it = d.task_blocks.find(key);
+  if (it != d.task_blocks.end()) {
+    *out = &it->second;
+    return cudaSuccess;
+  }
+  DeviceSpace::TaskBlocks tb;
+  std::vector<int32_t> first;
+  const int64_t n_int = with_b ? d.n_tasks_interior : d.n_tasks;
+  auto pack = [&](int64_t lo, int64_t hi, int slot) {
+    int64_t t = lo;
+    while (t < hi) {
+      first.push_back((int32_t)t);
+      int64_t used = 0;
+      int n = 0;
+      while (t < hi && n < warps) {
+        const int64_t need = 32LL * d.task_P[t] * slot;
+        if (n > 0 && used + need > budget) break;
+        used += need;
+        ++n;
+        ++t;
+      }
+      tb.smem = std::max(tb.smem, used);
+    }
+  };
+  pack(0, n_int, slot_int);
+  tb.n_int = (int64_t)first.size();
+  if (with_b) pack(n_int, d.n_tasks, slot_bnd);
+  tb.n_bnd = (int64_t)first.size() - tb.n_int;
+  first.push_back((int32_t)d.n_tasks);
+  cudaError_t e = cudaMalloc((void**)&tb.first, first.size() * sizeof(int32_t));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(tb.first, first.data(), first.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    if (tb.first) cudaFree(tb.first);
+    return e;
+  }
+  *out = &(d.task_blocks[key] = tb);
+  return cudaSuccess;
+}
+
 template <int ORDER, typename Real, bool WITH_B, int MODE>
 cudaError_t launch_t(DeviceSpace& d, const AssembleArgs& a, cudaStream_t stream) {
   using C = EntCfg<ORDER, Real, MODE>;
@@ -624,7 +745,12 @@ cudaError_t launch_t(DeviceSpace& d, const AssembleArgs& a, cudaStream_t stream)
         err = cudaMalloc((void**)&d.g2_f, sizeof(float) * 24 * std::max<int64_t>(d.nt, 1));
         if (err != cudaSuccess) return err;
       }
+      if (!d.h2_f) {
+        err = cudaMalloc((void**)&d.h2_f, sizeof(float) * 24 * std::max<int64_t>(d.nb, 1));
+        if (err != cudaSuccess) return err;
+      }
       g = reinterpret_cast<Real*>(d.g2_f);
+      h = reinterpret_cast<Real*>(d.h2_f);
       cell_geometry_kernel<double, float, true><<<(unsigned)blocks, threads, 0, stream>>>(
           d.nt, d.cells, d.xyz_hi, d.xyz_lo, d.xyz, d.ext_mask, d.bidx, (const float*)a.eps_r,
           (const float*)a.mu_r_inv, (float*)g, (float*)h, WITH_B, 1.0, 1.0);
@@ -638,6 +764,10 @@ cudaError_t launch_t(DeviceSpace& d, const AssembleArgs& a, cudaStream_t stream)
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
   }
+  const DeviceSpace::TaskBlocks* tb = nullptr;
+  err = task_blocks(d, (int)(C::V * sizeof(Real)), (int)((C::V + C::VB) * sizeof(Real)), WITH_B,
+                    C::BLOCK_WARPS, C::BLOCK_BYTES, &tb);
+  if (err != cudaSuccess) return err;
   EntArgs p;
   p.task_ent = d.task_ent;
   p.task_meta = d.task_meta;
@@ -645,30 +775,17 @@ cudaError_t launch_t(DeviceSpace& d, const AssembleArgs& a, cudaStream_t stream)
   p.indptr = d.indptr;
   p.bidx = d.bidx;
   p.ext_mask = d.ext_mask;
-  p.P = d.max_row | 1;
-  p.n_tasks = d.n_tasks;
-  // without B every task is an interior one (no B or Im accumulator)
-  p.n_int_tasks = WITH_B ? d.n_tasks_interior : d.n_tasks;
-  const int64_t main_bytes = (int64_t)32 * p.P * C::V * sizeof(Real);
-  const int64_t bnd_bytes = main_bytes + (int64_t)32 * p.P * C::VB * sizeof(Real);
-  // up to kEntWarps tasks per block within ~80 KB, so that two or more
-  // blocks share an SM
-  p.w_int = (int)std::max<int64_t>(1, std::min<int64_t>(kEntWarps, (80 << 10) / main_bytes));
-  p.n_int_blocks = (p.n_int_tasks + p.w_int - 1) / p.w_int;
-  int64_t smem = p.w_int * main_bytes;
-  p.w_bnd = (int)std::max<int64_t>(1, std::min<int64_t>(p.w_int, smem / bnd_bytes));
-  smem = std::max<int64_t>(smem, p.w_bnd * bnd_bytes);
-  const int64_t n_bnd_tasks = p.n_tasks - p.n_int_tasks;
-  const int64_t n_bnd_blocks = WITH_B ? (n_bnd_tasks + p.w_bnd - 1) / p.w_bnd : 0;
-  const int64_t grid = p.n_int_blocks + n_bnd_blocks;
+  p.blocks = tb->first;
+  p.n_int_blocks = tb->n_int;
+  const int64_t grid = tb->n_int + tb->n_bnd;
   if (grid < 1) return cudaSuccess;
-  if (smem > (227 << 10)) return cudaErrorInvalidConfiguration;  // rows too long
+  if (tb->smem > (227 << 10)) return cudaErrorInvalidConfiguration;  // rows too long
   auto kern = assemble_entities_kernel<ORDER, Real, MODE, WITH_B>;
-  err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb->smem);
   if (err != cudaSuccess) return err;
   const Real* kt = sizeof(Real) == 4 ? (const Real*)d.kt_f : (const Real*)d.kt_d;
-  kern<<<(unsigned)grid, p.w_int * 32, (size_t)smem, stream>>>(
-      p, g, h, kt, (Real*)a.S, (Real*)a.T, (Real*)a.B, (typename Cplx<Real>::T*)a.A);
+  kern<<<(unsigned)grid, C::BLOCK_WARPS * 32, (size_t)tb->smem, stream>>>(
+      p, g, h, kt, d.kt_lo_f, (Real*)a.S, (Real*)a.T, (Real*)a.B, (typename Cplx<Real>::T*)a.A);
   count_launch(2);
   return cudaGetLastError();
 }

@@ -3,7 +3,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <string>
+#include <vector>
 
 #include "space.h"
 
@@ -46,6 +48,7 @@ struct DeviceSpace {
   float* g_f = nullptr;           // nt*12
   double* g_d = nullptr;
   float* g2_f = nullptr;          // nt*24: float hi + lo coefficients (separate FP32 matrices)
+  float* h2_f = nullptr;          // nb*24: float hi + lo tangential coefficients
   float* h_f = nullptr;           // nb*12
   double* h_d = nullptr;
   // entity-per-lane assembly schedule (orders 1-2, see Space)
@@ -54,6 +57,15 @@ struct DeviceSpace {
   int32_t* task_ent = nullptr;    // n_tasks*32
   int4* task_meta = nullptr;      // n_tasks
   uint32_t* step_words = nullptr; // step blocks
+  std::vector<uint16_t> task_P;   // host copy of every task's accumulator stride
+  // tasks of each block of the assembly kernel, packed per shared-memory
+  // need (key: bytes per accumulator slot and boundary layout; built once)
+  struct TaskBlocks {
+    int32_t* first = nullptr;     // device: first task of each block (+ end)
+    int64_t n_int = 0, n_bnd = 0; // interior blocks, then boundary blocks
+    int64_t smem = 0;             // largest block's shared memory
+  };
+  std::map<int, TaskBlocks> task_blocks;
   // reference tensors in the cell kernel's layout [a][b][12] (KC m=0..5, KM m=0..5)
   float* kab_f = nullptr;
   double* kab_d = nullptr;
@@ -61,6 +73,7 @@ struct DeviceSpace {
   float* kc_f = nullptr;
   float* km_f = nullptr;
   float* kt_f = nullptr;
+  float* kt_lo_f = nullptr;       // kt_d - kt_f rounded to float (compensated FP32 ABC terms)
   double* kc_d = nullptr;
   double* km_d = nullptr;
   double* kt_d = nullptr;

@@ -364,22 +364,27 @@ def _f32(x):
     f = float(x)
     r = struct.unpack("f", struct.pack("f", f))[0]
     # struct rounds the double; fix double rounding by checking neighbours
+    if r == 0.0:
+        return F(0)
     cands = [r]
     for d in (-1, 1):
-        b = struct.unpack("I", struct.pack("f", r))[0] + (d if r >= 0 else -d)
-        cands.append(struct.unpack("f", struct.pack("I", b & 0xFFFFFFFF))[0])
+        b = struct.unpack("I", struct.pack("f", r))[0] + d
+        c = struct.unpack("f", struct.pack("I", b & 0xFFFFFFFF))[0]
+        if c == c and abs(c) != float("inf"):
+            cands.append(c)
     return min((F(c) for c in cands), key=lambda c: (abs(c - x), c))
 
 
-def _dot2(terms):
-    """Compensated sum of coef * g[m] (Dot2): the float kernels get each
-    constant as float hi + lo and add the products with error-free
+def _dot2(name, terms):
+    """Compensated sum of coef * g[m] into Dot2 `name`: the float kernels
+    get each constant as float hi + lo and add the products with error-free
     transformations, the double kernels a plain FMA chain."""
-    parts = []
+    parts = ["Dot2<R> %s;" % name]
     for m, c in terms:
         hi = _f32(c)
-        parts.append("t.add(g, %d, %r, %rf, %rf)" % (m, float(c), float(hi), float(_f32(c - hi))))
-    return "Dot2<R> t; " + "; ".join(parts) + ";"
+        parts.append("%s.add(g, %d, %r, %rf, %rf);" % (name, m, float(c), float(hi),
+                                                       float(_f32(c - hi))))
+    return " ".join(parts)
 
 
 def contract_code():
@@ -389,15 +394,16 @@ def contract_code():
 
       Rows<ORDER, FACE, LE>::fused(g, fn)  calls fn(j, b, v) with
           v = sum_m g[m] KC[m][a][b] + g[6 + m] KM[m][a][b]
-      Rows<ORDER, FACE, LE>::split(g, fn)  calls fn(j, b, s, t, has_s) with
-          s = sum_m g[m] KC[m][a][b], t = sum_m g[6 + m] KM[m][a][b]
-          (has_s false when every KC constant of the entry is zero, s = 0);
-          t is a compensated dot product (Dot2): in single precision the
-          mass-matrix terms of an element entry can cancel to a few percent
-          of their size, and a plain FMA chain (or coefficients rounded to
-          float) then loses the 1e-6 relative accuracy the separate matrices
-          are held to; the single-precision split form therefore takes g as
-          24 values, the 12 coefficients rounded to float and their rests
+      Rows<ORDER, FACE, LE>::split(g, fn)  calls fn(j, b, s, t) with the
+          Dot2 sums s = sum_m g[m] KC[m][a][b], t = sum_m g[6 + m] KM[m][a][b]:
+          compensated dot products.  In single precision the terms of an
+          element entry can cancel (to a few percent of their size on
+          regular meshes, to far less on jittered ones), and a plain FMA
+          chain, or coefficients rounded to float, then loses the 1e-6
+          relative accuracy the separate matrices are held to; the
+          single-precision split form therefore takes g as 24 values (the 12
+          coefficients rounded to float, then their rests) and hands each
+          sum on unrounded (s.s + s.c) for a double-float accumulation
 
     for every column b of the cell and the entity's local DOFs a (j-th):
     edge LE of order k -> a = k*LE + j, face LE of order 2 -> a = 12 + 2*LE + j.
@@ -465,13 +471,8 @@ def contract_code():
                         tt = [(6 + m, KM[m][a][b]) for m in range(6) if KM[m][a][b] != 0]
                         if ts or tt:
                             fused.append("    fn(%d, %d, %s);" % (j, b, _chain(ts + tt)))
-                        sv = _chain(ts) if ts else "R(0)"
-                        if tt:
-                            split.append("    { %s fn(%d, %d, %s, t.sum(), %s); }" % (
-                                _dot2(tt), j, b, sv, "true" if ts else "false"))
-                        else:
-                            split.append("    fn(%d, %d, %s, R(0), %s);" % (
-                                j, b, sv, "true" if ts else "false"))
+                        split.append("    { %s %s fn(%d, %d, sd, td); }" % (
+                            _dot2("sd", ts), _dot2("td", tt), j, b))
                 out += ["template <>",
                         "struct Rows<%d, %s, %d> {" % (order, "true" if face else "false", le),
                         "  template <class R, class Fn>",

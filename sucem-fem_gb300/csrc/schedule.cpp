@@ -118,9 +118,16 @@ void build_row_schedule(Space& s) {
     step_base[t + 1] = step_base[t] + steps;
     const int64_t k0 = ord[task_first[t]];
     if (!on_bnd[k0]) s.n_tasks_interior = t + 1;
+    // the task's accumulator stride: its longest row, made odd (slot
+    // vectors of the 32 lanes then fall in distinct banks)
+    int64_t lmax = 1;
+    for (int64_t i = task_first[t]; i < task_first[t + 1]; ++i) {
+      const int64_t r = (int64_t)s.dofs_per_entity * ord[i];
+      lmax = std::max<int64_t>(lmax, s.indptr[r + 1] - s.indptr[r]);
+    }
     int32_t* meta = &s.task_meta[t * 4];
     std::memcpy(&meta[1], trip, 8);
-    meta[3] = k0 >= ne ? 1 : 0;
+    meta[3] = (k0 >= ne ? 1 : 0) | (int32_t)((lmax | 1) << 8);
   }
   const int64_t words_per_step = (int64_t)(1 + planes) * 32;
   s.step_words.assign(step_base[nt_] * words_per_step, 0);

@@ -69,7 +69,9 @@ struct Space {
   int64_t n_tasks_interior = 0;        // tasks [0, n_tasks_interior) have no boundary entity
   std::vector<int32_t> task_ent;       // n_tasks*32: entity per lane (-1: none)
   std::vector<int32_t> task_meta;      // n_tasks*4: first step block, trips le 0-3 (bytes),
-                                       //   trips le 4-7 (bytes), flags (bit 0: faces)
+                                       //   trips le 4-7 (bytes), flags (bit 0: faces;
+                                       //   bits 8-23: accumulator stride P, the task's
+                                       //   longest row made odd)
   std::vector<uint32_t> step_words;    // step blocks, (1 + slot_planes) * 32 words each
   int slot_planes = 0;                 // ceil(ndof_cell / 4)
 

@@ -4,8 +4,8 @@ and evaluated in double precision on random tetrahedra, against the
 oracle's element matrices (an independent, sympy-exact derivation of the
 same reference tensors).  Covers every (order, edge/face, local index) and
 both the fused (S + T part) and split (S, T apart) forms; the split form is
-also run in single precision, whose compensated mass entries must stay
-within float rounding of their exact value where their terms cancel."""
+also run in single precision, whose compensated sums must stay exact to
+~1e-13 of the size of their terms where those terms cancel."""
 import os
 import shutil
 import subprocess
@@ -30,11 +30,13 @@ using std::fmaf;
 template <int O, bool F, int LE>
 void rows(const double* g, const float* gf) {
   Rows<O, F, LE>::fused(g, [&](int j, int b, double v) { std::printf("f %%d %%d %%d %%d %%d %%.17g\n", O, F, LE, j, b, v); });
-  Rows<O, F, LE>::split(g, [&](int j, int b, double s, double t, bool) {
-    std::printf("s %%d %%d %%d %%d %%d %%.17g %%.17g\n", O, F, LE, j, b, s, t);
+  Rows<O, F, LE>::split(g, [&](int j, int b, const Dot2<double>& s, const Dot2<double>& t) {
+    std::printf("s %%d %%d %%d %%d %%d %%.17g %%.17g\n", O, F, LE, j, b, s.s, t.s);
   });
-  Rows<O, F, LE>::split(gf, [&](int j, int b, float s, float t, bool) {
-    std::printf("t %%d %%d %%d %%d %%d %%.9g %%.9g\n", O, F, LE, j, b, (double)s, (double)t);
+  // single precision: the unrounded double-float sums s + c
+  Rows<O, F, LE>::split(gf, [&](int j, int b, const Dot2<float>& s, const Dot2<float>& t) {
+    std::printf("t %%d %%d %%d %%d %%d %%.17g %%.17g\n", O, F, LE, j, b, (double)s.s + (double)s.c,
+                (double)t.s + (double)t.c);
   });
 }
 int main() {
@@ -88,13 +90,15 @@ def test_generated_rows_match_oracle(driver, seed):
     out = subprocess.run([driver], input=" ".join("%.17g" % x for x in g), capture_output=True,
                          text=True, check=True).stdout.split("\n")
     ref = {o: fem.element_matrices(coords, cells, o, [1.0], [1.0]) for o in (1, 2)}
-    # exact mass rows of the element and the size of their terms
+    # exact element rows and the size of their terms
     from oracle import n1curl_exact
-    exact32, termsum = {}, {}
+    exact, termsum = {}, {}
     for o in (1, 2):
-        Km = fem._sym6(n1curl_exact.reference_tensors(o)["mass"])
-        exact32[o] = np.einsum("m,mab->ab", g[6:], Km)
-        termsum[o] = np.einsum("m,mab->ab", np.abs(g[6:]), np.abs(Km))
+        R = n1curl_exact.reference_tensors(o)
+        Kc, Km = fem._sym6(R["curl"]), fem._sym6(R["mass"])
+        exact[o] = (np.einsum("m,mab->ab", g[:6], Kc), np.einsum("m,mab->ab", g[6:], Km))
+        termsum[o] = (np.einsum("m,mab->ab", np.abs(g[:6]), np.abs(Kc)),
+                      np.einsum("m,mab->ab", np.abs(g[6:]), np.abs(Km)))
     seen = 0
     for line in out:
         if not line:
@@ -107,11 +111,12 @@ def test_generated_rows_match_oracle(driver, seed):
         if kind == "f":
             assert abs(float(parts[6]) - (S[a, b] + T[a, b])) <= 1e-13 * scale
         elif kind == "t":
-            # compensated single-precision mass entry (coefficients as float
-            # hi + lo): within float rounding of its exact value even where
-            # its terms cancel
-            e = exact32[o][a, b]
-            assert abs(float(parts[7]) - e) <= 1.2e-7 * abs(e) + 1e-12 * termsum[o][a, b]
+            # compensated single-precision sums (coefficients and constants
+            # as float hi + lo, result kept as s + c): exact to ~1e-13 of the
+            # size of their terms, even where the terms cancel
+            for q in (0, 1):
+                e = exact[o][q][a, b]
+                assert abs(float(parts[6 + q]) - e) <= 1e-12 * termsum[o][q][a, b] + 1e-15 * scale
         else:
             assert abs(float(parts[6]) - S[a, b]) <= 1e-13 * scale
             assert abs(float(parts[7]) - T[a, b]) <= 1e-13 * scale

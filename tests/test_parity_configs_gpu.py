@@ -151,15 +151,24 @@ def _jittered60():
 
 
 def test_jittered_60_order1_fp32_vs_fp64_and_oracle_rows():
+    """Both assemblies take the same eps_r values (rounded to float, the
+    FP32 entry point's input type): on a jittered mesh the contributions of
+    neighbouring cells to an entry can cancel 1e4-fold, and the rounding of
+    a float eps_r would then show in the entry without any arithmetic
+    error.  Against the oracle, the FP64 rows are held to 1e-12 relative or,
+    for entries that cancel that far, to the FP64 rounding bound
+    2e-16 x (sum of |cell contributions|), counted."""
     from sucemfem.space import FunctionSpace
     mesh = _jittered60()
     eps = np.random.default_rng(1).uniform(1.0, 4.0, mesh.num_cells())
+    eps = eps.astype(np.float32).astype(np.float64)
     V = FunctionSpace(mesh, order=1)
     assert V.nt == 1296000 and V.n == 1544580
     g64 = _assemble_split(V, 8, eps)
     g32 = _assemble_split(V, 4, eps)
     for k in "STB":
-        per_entry(g32[k], g64[k], V.indptr, 1e-6)
+        print("jittered 60^3 order 1, FP32 vs FP64, %s: %s"
+              % (k, per_entry(g32[k], g64[k], V.indptr, 1e-6)))
     # 1,000 random rows against the oracle: element matrices of the cells
     # that hold those rows' DOFs, added up in FP64 on the space's numbering
     rng = np.random.default_rng(2)
@@ -169,6 +178,7 @@ def test_jittered_60_order1_fp32_vs_fp64_and_oracle_rows():
     coords, cells = mesh.coordinates(), V.cells
     Se, Te = fem.element_matrices(coords, cells[sel], 1, eps[sel], np.ones(len(sel)))
     want = {k: {} for k in "ST"}
+    size = {k: {} for k in "ST"}
     pick = np.zeros(V.n, dtype=bool)
     pick[rows] = True
     for i, c in enumerate(sel):
@@ -177,12 +187,23 @@ def test_jittered_60_order1_fp32_vs_fp64_and_oracle_rows():
             if not pick[d[a]]:
                 continue
             for b in range(6):
-                want["S"][(d[a], d[b])] = want["S"].get((d[a], d[b]), 0.0) + Se[i, a, b]
-                want["T"][(d[a], d[b])] = want["T"].get((d[a], d[b]), 0.0) + Te[i, a, b]
+                for k, E in (("S", Se), ("T", Te)):
+                    key = (d[a], d[b])
+                    want[k][key] = want[k].get(key, 0.0) + E[i, a, b]
+                    size[k][key] = size[k].get(key, 0.0) + abs(E[i, a, b])
     ip, ix = V.indptr, V.indices
+    n_bound = 0
     for k in "ST":
         for r in rows:
             cols = ix[ip[r]:ip[r + 1]]
             ref_row = np.array([want[k].get((r, c), 0.0) for c in cols])
+            size_row = np.array([size[k].get((r, c), 0.0) for c in cols])
             per_entry(g32[k][ip[r]:ip[r + 1]], ref_row, np.array([0, len(cols)]), 1e-6)
-            per_entry(g64[k][ip[r]:ip[r + 1]], ref_row, np.array([0, len(cols)]), 1e-12)
+            err = np.abs(g64[k][ip[r]:ip[r + 1]] - ref_row)
+            ok_rel = err <= 1e-12 * np.abs(ref_row)
+            ok_bound = err <= 2e-16 * size_row
+            zero = np.abs(ref_row) <= 1e-12 * max(np.abs(ref_row).max(), 1e-300)
+            assert np.all(ok_rel | ok_bound | (zero & (err <= 1e-12 * np.abs(ref_row).max())))
+            n_bound += int((~ok_rel & ok_bound).sum())
+    print("jittered 60^3 order 1, FP64 rows vs oracle: %d entries within the rounding bound only"
+          % n_bound)
