@@ -65,7 +65,7 @@ def build(verbose=False, force=False):
             if o.strip():
                 print(o)
     tmp = OUT + ".tmp"
-    _run([NVCC] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", tmp] + objs + ["-lcublas"])
+    _run([NVCC] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", tmp] + objs)
     os.replace(tmp, OUT)
     return OUT
 

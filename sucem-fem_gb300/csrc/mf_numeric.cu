@@ -20,8 +20,6 @@
 #include "../../include/sucem_gb300.h"
 #include "mf.h"
 
-#include <cublas_v2.h>
-
 #include <type_traits>
 
 namespace sucem {
@@ -32,13 +30,13 @@ void count_launch(int k);
 namespace {
 
 
-// levels with at most this many fronts update them with cuBLAS (see blas_update)
-constexpr int kBlasFronts = 16;
+// single precision (real and complex): trailing and panel updates on the
+// tensor cores (mf_tc.cuh); double precision keeps the CUDA-core kernels
 template <typename S>
-constexpr bool kSinglePrecision = std::is_same<S, float>::value || std::is_same<S, float2>::value;
-// complex single precision: Schur-block updates on the tensor cores (mf_tc.cuh)
+constexpr bool kTensorCore = std::is_same<S, float2>::value || std::is_same<S, float>::value;
+// algorithmic flops of one multiply-add
 template <typename S>
-constexpr bool kTensorCore = std::is_same<S, float2>::value;
+constexpr double kMacFlops = std::is_same<S, float2>::value ? 8.0 : 2.0;
 
 // ---- scalar helpers ----
 __device__ __forceinline__ float s_zero(float) { return 0.f; }
@@ -951,9 +949,6 @@ struct MFDevice {
   cudaEvent_t factor_ev = nullptr;
   bool checked = false;
   bool valid = true;
-  // cuBLAS handle for the single-precision Schur updates of the top levels
-  cublasHandle_t blas = nullptr;
-  cublasComputeType_t blas_compute = CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
 };
 
 struct MFHandle {
@@ -995,7 +990,6 @@ void free_dev(MFDevice& d) {
     for (int s = 0; s < 2; ++s)
       if (L.d_kids[s]) cudaFree(L.d_kids[s]);
   }
-  if (d.blas) cublasDestroy(d.blas);
   if (d.solve_exec) cudaGraphExecDestroy(d.solve_exec);
   for (cudaEvent_t ev : d.tc_ev) cudaEventDestroy(ev);
   if (d.cap_stream) cudaStreamDestroy(d.cap_stream);
@@ -1003,47 +997,7 @@ void free_dev(MFDevice& d) {
   d = MFDevice();
 }
 
-// Trailing update of one large front by cuBLAS (a plain GEMM): in the
-// row-major front, C[lo:, lo:] -= L[lo:, p0:p0+nb] U[p0:p0+nb, lo:], i.e. in
-// cuBLAS's column-major view C^T -= U^T L^T with leading dimension f.  The
-// single-precision product runs with FP32-accurate BF16x9 emulation on the
-// tensor cores when cuBLAS offers it for the type, else plain FP32.
-template <typename S>
-cudaError_t blas_gemm(MFDevice& d, const S* U, const S* Lb, S* C, int64_t rows, int64_t cols,
-                      int64_t kk, int64_t f, cudaStream_t st) {
-  // row-major C[rows x cols] -= Lb[rows x kk] U[kk x cols], leading dimension f
-  if (rows <= 0 || cols <= 0 || kk <= 0) return cudaSuccess;
-  if (!d.blas) {
-    if (cublasCreate(&d.blas) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
-  }
-  cublasSetStream(d.blas, st);
-  const bool cplx = sizeof(S) == 8;
-  const cudaDataType_t t = cplx ? CUDA_C_32F : CUDA_R_32F;
-  const float2 am1 = make_float2(-1.f, 0.f), one = make_float2(1.f, 0.f);
-  const void* alpha = &am1;
-  const void* beta = &one;
-  for (int attempt = 0; attempt < 2; ++attempt) {
-    cublasStatus_t s = cublasGemmEx(d.blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)cols, (int)rows, (int)kk,
-                                    alpha, U, t, (int)f, Lb, t, (int)f, beta, C, t, (int)f,
-                                    d.blas_compute, CUBLAS_GEMM_DEFAULT);
-    if (s == CUBLAS_STATUS_SUCCESS) {
-      count_launch(1);
-      return cudaSuccess;
-    }
-    if (s != CUBLAS_STATUS_NOT_SUPPORTED || d.blas_compute == CUBLAS_COMPUTE_32F)
-      return cudaErrorUnknown;
-    d.blas_compute = CUBLAS_COMPUTE_32F;
-  }
-  return cudaErrorUnknown;
-}
-
-// cuBLAS levels work in super-panels of kSuperPanel columns: the panel
-// steps update only the rows and columns of their super-panel (batched
-// kernel), and the last panel of a super-panel [sp0, bnd) applies the
-// trailing block F[bnd:f, bnd:f] -= L[bnd:f, sp0:bnd] U[sp0:bnd, bnd:f] as
-// one GEMM with K = bnd - sp0 (the last of these is the Schur update).
-constexpr int kSuperPanel = 512;
-// complex64 factorisations work in super-panels of d.tc_sp columns on every
+// single-precision factorisations work in super-panels of d.tc_sp columns on every
 // level; for each level, the panels p0 at which some fronts' super-panel
 // ends get one tensor-core launch over exactly those fronts (list on the
 // device).  Narrower super-panels move panel work onto the tensor cores
@@ -1073,7 +1027,7 @@ void add_tiles(std::vector<int32_t>& tl, int32_t node, int64_t r0, int64_t r1, i
     }
 }
 
-cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s) {
+cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s, double mac_flops) {
   d.tc_sp = kTcSuperPanel;
   d.tc_panel_k = kTcPanelMinK;
   if (const char* v = getenv("SUCEM_LU_TC_PANEL_K")) d.tc_panel_k = atoi(v);
@@ -1107,7 +1061,7 @@ cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s) {
         const int64_t sp0 = (t.p0 / sp) * (int64_t)sp;
         const int64_t bnd = std::min<int64_t>(nd.k, sp0 + sp);
         add_tiles(tl, ends[b].second, bnd, nd.f, bnd, nd.f, sp0, bnd - sp0);
-        t.flops += 8.0 * (double)(nd.f - bnd) * (double)(nd.f - bnd) * (double)(bnd - sp0);
+        t.flops += mac_flops * (double)(nd.f - bnd) * (double)(nd.f - bnd) * (double)(bnd - sp0);
       }
       t.ntiles = (int)(tl.size() / 8);
       cudaError_t e = upv(&t.d_tiles, tl);
@@ -1129,7 +1083,7 @@ cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s) {
         if (bnd <= lo) continue;
         add_tiles(tl, i, lo, nd.f, lo, bnd, p0, nb);   // rows [lo, f) x cols [lo, bnd)
         add_tiles(tl, i, lo, bnd, bnd, nd.f, p0, nb);  // rows [lo, bnd) x cols [bnd, f)
-        t.flops += 8.0 * (double)nb *
+        t.flops += mac_flops * (double)nb *
                    ((double)(nd.f - lo) * (bnd - lo) + (double)(bnd - lo) * (nd.f - bnd));
       }
       t.ntiles = (int)(tl.size() / 8);
@@ -1197,7 +1151,8 @@ cudaError_t setup_device(MFHandle& h, int dtype) {
   if (e == cudaSuccess) e = cudaMalloc(&d.arena, (size_t)std::max<int64_t>(s.arena, 1) * d.elem);
   if (e == cudaSuccess) e = cudaMalloc(&d.d_x, (size_t)std::max<int64_t>(s.n, 1) * d.elem);
   if (e == cudaSuccess) e = cudaMalloc((void**)&d.d_flag, 16);
-  if (e == cudaSuccess && dtype == SUCEM_C64) e = plan_tc(d, s);
+  if (e == cudaSuccess && dtype == SUCEM_C64) e = plan_tc(d, s, kMacFlops<float2>);
+  if (e == cudaSuccess && dtype == SUCEM_F32) e = plan_tc(d, s, kMacFlops<float>);
   if (e != cudaSuccess) free_dev(d);
   return e;
 }
@@ -1217,17 +1172,21 @@ cudaError_t tc_event(MFDevice& d, int i, int which, cudaStream_t st) {
 // tile), with events around it for sucem_lu_kernel_stats
 template <typename S>
 cudaError_t tc_launch(MFDevice& d, const TcLaunch& t, S* arena, cudaStream_t st) {
-  const int grid = std::max(1, std::min(t.ntiles, d.sm_count));
-  cudaError_t e = tc_event(d, d.tc_n, 0, st);
-  if (e != cudaSuccess) return e;
-  tc_update_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, st>>>(
-      t.d_tiles, t.ntiles, d.d_nodes, reinterpret_cast<float2*>(arena), d.d_flag + 1);
-  e = tc_event(d, d.tc_n, 1, st);
-  if (e != cudaSuccess) return e;
-  d.tc_n++;
-  d.tc_flops += t.flops;
-  count_launch(1);
-  return cudaSuccess;
+  if constexpr (!kTensorCore<S>) {
+    return cudaErrorInvalidValue;  // double precision has no tensor-core plan
+  } else {
+    const int grid = std::max(1, std::min(t.ntiles, d.sm_count));
+    cudaError_t e = tc_event(d, d.tc_n, 0, st);
+    if (e != cudaSuccess) return e;
+    tc_update_kernel<S><<<grid, tc::THREADS, tc::smem_bytes<S>(), st>>>(
+        t.d_tiles, t.ntiles, d.d_nodes, arena, d.d_flag + 1);
+    e = tc_event(d, d.tc_n, 1, st);
+    if (e != cudaSuccess) return e;
+    d.tc_n++;
+    d.tc_flops += t.flops;
+    count_launch(1);
+    return cudaSuccess;
+  }
 }
 
 template <typename S>
@@ -1252,9 +1211,10 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
     if (ea == cudaSuccess)
       ea = cudaFuncSetAttribute(gemm_update_kernel<S, NBT>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gemm_smem);
-    if (ea == cudaSuccess && kTensorCore<S>)
-      ea = cudaFuncSetAttribute(tc_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                tc::SMEM_BYTES);
+    if constexpr (kTensorCore<S>)
+      if (ea == cudaSuccess)
+        ea = cudaFuncSetAttribute(tc_update_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  tc::smem_bytes<S>());
     if (ea == cudaSuccess)
       ea = cudaFuncSetAttribute(schur_update_kernel<S, kSchurKC>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)schur_smem);
@@ -1314,14 +1274,12 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
       count_launch(1);
       mark(0);
     }
-    // complex64: every level in super-panels of d.tc_sp columns, the
-    // trailing blocks on the tensor cores (precomputed launch lists);
-    // otherwise few large fronts take cuBLAS GEMMs per front with
-    // super-panels of kSuperPanel, the rest one Schur update per level
+    // single precision: every level in super-panels of d.tc_sp columns,
+    // the trailing blocks on the tensor cores (precomputed launch lists);
+    // double precision: one Schur update per level
     const int nall = (int)L.nodes_by_k.size();
     const bool tc_level = kTensorCore<S> && d.tc_sp > 0;
-    const bool use_blas = !tc_level && kSinglePrecision<S> && nall <= kBlasFronts;
-    const int spw = tc_level ? d.tc_sp : (use_blas ? kSuperPanel : 0);
+    const int spw = tc_level ? d.tc_sp : 0;
     size_t next_tc = 0;
     for (int p0 = 0; p0 < L.max_k; p0 += NBT) {
       // active fronts: prefix of the k-descending list with k > p0
@@ -1346,7 +1304,7 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
         if (tc_level && pi < L.tcp.size()) {
           const TcLaunch& t = L.tcp[pi];
           if (t.ntiles > 0) {
-            e = tc_launch(d, t, arena, st);
+            e = tc_launch<S>(d, t, arena, st);
             if (e != cudaSuccess) return e;
           }
           mark(4);
@@ -1363,31 +1321,16 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
         // fronts whose super-panel ends with this panel: trailing block on
         // the tensor cores, one launch over exactly those fronts
         while (next_tc < L.tcl.size() && L.tcl[next_tc].p0 == p0) {
-          e = tc_launch(d, L.tcl[next_tc++], arena, st);
+          e = tc_launch<S>(d, L.tcl[next_tc++], arena, st);
           if (e != cudaSuccess) return e;
           mark(4);
-        }
-      } else if (use_blas && tiles > 0) {
-        // fronts whose super-panel ends with this panel: trailing GEMM
-        for (int q = 0; q < cnt; ++q) {
-          const MFNode& nd = s.nodes[L.nodes_by_k[q]];
-          const int64_t lo = p0 + std::min<int64_t>(NBT, nd.k - p0);
-          const int64_t sp0 = (p0 / kSuperPanel) * (int64_t)kSuperPanel;
-          const int64_t bnd = std::min<int64_t>(nd.k, sp0 + kSuperPanel);
-          if (lo != bnd || bnd >= nd.f) continue;
-          S* F = arena + nd.front_off;
-          const int64_t f = nd.f;
-          e = blas_gemm<S>(d, F + sp0 * f + bnd, F + bnd * f + sp0, F + bnd * f + bnd, f - bnd,
-                           f - bnd, bnd - sp0, f, st);
-          if (e != cudaSuccess) return e;
         }
       }
     }
     // Schur blocks F[k:f, k:f] -= L21 U12 with the full K = k, before the
     // parent level's extend-add reads them
-    if (!tc_level && !use_blas && L.max_u > 0 && nall > 0) {
-      // one batched launch for all fronts of the level (per-front cuBLAS
-      // calls leave the GPU underfilled at these front sizes)
+    if (!tc_level && L.max_u > 0 && nall > 0) {
+      // one batched launch for all fronts of the level
       const int tpd = (L.max_u + 63) / 64;
       dim3 g3(tpd * tpd, nall);
       schur_update_kernel<S, kSchurKC><<<g3, 256, schur_smem, st>>>(L.d_nodes, nall, d.d_nodes,

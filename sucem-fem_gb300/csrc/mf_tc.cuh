@@ -1,10 +1,10 @@
-// Tensor-core (tcgen05) Schur-block update of complex single-precision
-// fronts, included by mf_numeric.cu inside its anonymous namespace (uses
-// DNode and the row-major front arena).
+// Tensor-core (tcgen05) trailing update of single-precision fronts, real
+// (float) or complex (float2), included by mf_numeric.cu inside its
+// anonymous namespace (uses DNode and the row-major front arena).
 //
-// Complex64 fronts are factorised in super-panels; when the super-panel
-// [sp0, bnd) of a front is finished (its last 64-column panel factorised),
-// the trailing block takes
+// Single-precision fronts are factorised in super-panels; when the
+// super-panel [sp0, bnd) of a front is finished (its last 64-column panel
+// factorised), the trailing block takes
 //   F[bnd:f, bnd:f] -= F[bnd:f, sp0:bnd] * F[sp0:bnd, bnd:f]
 // (the last super-panel's trailing block is the Schur complement), and on
 // levels with large pivot blocks every 64-column panel p0 applies its
@@ -13,54 +13,72 @@
 // given by its own descriptor (front, rows, columns, K range), planned on
 // the host.
 //
-// Arithmetic: complex FP32 operands are split into TF32 pairs x = hi + lo
-// (hi = x rounded to TF32, lo = x - hi rounded to TF32), and every real
-// product is formed as hi*hi + hi*lo + lo*hi (the 3xTF32 scheme, ~2^-21
-// relative), so one complex K-step is 12 tcgen05.mma.kind::tf32
-// instructions (M = 128, N = 128, K = 8) accumulating Re and Im in two FP32
-// TMEM blocks; the -Im*Im terms use the instruction's A-negation bit.
+// Arithmetic: FP32 operands are split into TF32 pairs x = hi + lo (hi = x
+// rounded to TF32, lo = x - hi rounded to TF32), and every real product is
+// formed as hi*hi + hi*lo + lo*hi (the 3xTF32 scheme, ~2^-21 relative):
+// a real K-step is 3 tcgen05.mma.kind::tf32 instructions (M = 128, N = 128,
+// K = 8) into one FP32 TMEM accumulator; a complex K-step is 12, Re and Im
+// in two accumulators, the -Im*Im terms through the instruction's
+// A-negation bit.
 //
 // Structure: a persistent, warp-specialised kernel, one CTA per SM walking
 // the tile list round-robin.
 //   warps 4-11 (producers): load a K-chunk of 16 (A: 128 rows, B: 128
 //     columns; two quarter rows and half a column per thread, loads
 //     coalesced along the rows of the front, two chunks ahead through two
-//     register buffers), split it and store eight K-major
-//     operand planes (Re/Im x hi/lo of A and B)
-//     in the canonical no-swizzle core-matrix layout (8 rows x 16 bytes per
-//     core matrix, 128 bytes apart along K, 512 bytes apart along M/N) into
-//     one of three stages, then arrive on the stage's "full" barrier;
+//     register buffers), split it and store the K-major operand planes
+//     (real: hi/lo of A and B; complex: Re/Im x hi/lo) in the canonical
+//     no-swizzle core-matrix layout (8 rows x 16 bytes per core matrix, 128
+//     bytes apart along K, 512 bytes apart along M/N) into one of three
+//     stages, then arrive on the stage's "full" barrier;
 //   warp 12, one thread (MMA issuer): per chunk, waits for "full", issues
-//     the 24 MMAs into the tile's TMEM accumulator and commits them to the
-//     stage's "empty" barrier (the producers' permission to refill it);
-//     after a tile's last chunk it commits to the accumulator's "acc_full"
-//     barrier;
+//     the chunk's MMAs into the tile's TMEM accumulator(s) and commits them
+//     to the stage's "empty" barrier (the producers' permission to refill
+//     it); after a tile's last chunk it commits to the accumulator's
+//     "acc_full" barrier;
 //   warps 0-3 (epilogue): request the tile's first 16 columns of C, wait
-//     for "acc_full", read their 32 TMEM lanes (tile rows) of both
-//     accumulators 16 columns at a time (each block's C requested before its
-//     TMEM reads), turn them through shared memory so that a warp's accesses
-//     to C cover two rows of 16 consecutive columns, apply C -= D and arrive
-//     on "acc_empty".
-// Two accumulators (all 512 TMEM columns) let the epilogue of one tile run
-// under the main loop of the next.  Every wait is bounded: on a timeout the
-// kernel raises *err, every role stops, and all meet at the final barrier.
+//     for "acc_full", read their 32 TMEM lanes (tile rows) 16 columns at a
+//     time (each block's C requested before its TMEM reads), turn them
+//     through shared memory so that a warp's accesses to C cover two rows of
+//     16 consecutive columns, apply C -= D and arrive on "acc_empty".
+// Two accumulator sets let the epilogue of one tile run under the main
+// loop of the next.  Every wait is bounded: on a timeout the kernel raises
+// *err, every role stops, and all meet at the final barrier.
 namespace tc {
 
 constexpr int BM = 128;                        // tile rows (TMEM lanes)
-constexpr int BN = 128;                        // tile columns (complex)
+constexpr int BN = 128;                        // tile columns
 constexpr int KC = 16;                         // K per chunk
 constexpr int STAGES = 3;
 constexpr int THREADS = 416;                   // 4 epilogue + 8 producer warps + 1 MMA warp
 constexpr int PRODUCERS = 256;
 constexpr int MMA_WARP = 12;
 constexpr int PLANE = BM * KC * 4;             // bytes of one operand plane (BN == BM)
-constexpr int STAGE_BYTES = 8 * PLANE;         // A: Re hi/lo, Im hi/lo; then B likewise
-constexpr int EPI_BYTES = 4 * 32 * 17 * 8;     // per epilogue warp: 32 rows x 16 (+1) complex
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EPI_BYTES + 512;
-constexpr int ACC_COLS = 2 * BN;               // Re then Im accumulators of one tile
-constexpr int TMEM_COLS = 2 * ACC_COLS;        // two tiles in flight
+constexpr int EPI_BYTES = 4 * 32 * 17 * 8;     // per epilogue warp: 32 rows x 16 (+1) values
 constexpr int kWaitLimit = 1 << 24;            // polls of one mbarrier before giving up
 static_assert(BN == BM, "planes share one size");
+
+// per element type: operand planes of A (and of B), accumulators per tile
+template <typename S>
+struct Cfg;
+template <>
+struct Cfg<float2> {
+  static constexpr int NP = 4;                 // Re hi, Re lo, Im hi, Im lo
+  static constexpr int NACC = 2;               // Re, Im
+};
+template <>
+struct Cfg<float> {
+  static constexpr int NP = 2;                 // hi, lo
+  static constexpr int NACC = 1;
+};
+template <typename S>
+__host__ __device__ constexpr int stage_bytes() { return 2 * Cfg<S>::NP * PLANE; }  // A planes, then B planes
+template <typename S>
+__host__ __device__ constexpr int smem_bytes() { return STAGES * stage_bytes<S>() + EPI_BYTES + 512; }
+template <typename S>
+__host__ __device__ constexpr int acc_cols() { return Cfg<S>::NACC * BN; }  // the accumulators of one tile
+template <typename S>
+__host__ __device__ constexpr int tmem_cols() { return 2 * acc_cols<S>(); }  // two tiles in flight
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -126,6 +144,21 @@ __device__ __forceinline__ float tf32_hi(float x) {
   return __uint_as_float(r);
 }
 
+// split four real values into hi/lo quads and store them at `off` of the
+// two planes starting at `planes`
+__device__ __forceinline__ void store_split(uint8_t* planes, int off, const float* v) {
+  float4 h, l;
+  float* ph = &h.x;
+  float* pl = &l.x;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    ph[q] = tf32_hi(v[q]);
+    pl[q] = tf32_hi(v[q] - ph[q]);
+  }
+  *reinterpret_cast<float4*>(planes + 0 * PLANE + off) = h;
+  *reinterpret_cast<float4*>(planes + 1 * PLANE + off) = l;
+}
+
 // split four complex values into Re/Im hi/lo quads and store them at `off`
 // of the four planes starting at `planes`
 __device__ __forceinline__ void store_split(uint8_t* planes, int off, const float2* v) {
@@ -169,17 +202,20 @@ __device__ __forceinline__ Tile tile_of(const int32_t* td) {
 }  // namespace tc
 
 // the listed tiles (8-int descriptors, see tile_of), each CTA taking tiles
-// blockIdx.x, blockIdx.x + gridDim.x, ...
+// blockIdx.x, blockIdx.x + gridDim.x, ...; S = float or float2
+template <typename S>
 __global__ void __launch_bounds__(tc::THREADS, 1)
     tc_update_kernel(const int32_t* __restrict__ tiles, int ntiles,
-                     const DNode* __restrict__ nodes, float2* __restrict__ arena,
+                     const DNode* __restrict__ nodes, S* __restrict__ arena,
                      int* __restrict__ err) {
   using namespace tc;
+  constexpr bool CPLX = std::is_same<S, float2>::value;
+  constexpr int NP = Cfg<S>::NP, SB = stage_bytes<S>(), ACC = acc_cols<S>(), TM = tmem_cols<S>();
   extern __shared__ __align__(128) uint8_t tc_smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(tc_smem_raw) + 127) & ~(uintptr_t)127);
-  float2* epi = reinterpret_cast<float2*>(smem + STAGES * STAGE_BYTES);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES + EPI_BYTES);
+  S* epi = reinterpret_cast<S*>(smem + STAGES * SB);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * SB + EPI_BYTES);
   uint64_t* empty = full + STAGES;
   uint64_t* acc_full = empty + STAGES;
   uint64_t* acc_empty = acc_full + 2;
@@ -205,7 +241,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
   if (warp == MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(TMEM_COLS));
+                 "r"(TM));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -219,28 +255,28 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
 
   if (warp >= 4 && warp < MMA_WARP) {
     // ---- producers: thread p stages K-group akg (four consecutive K) of
-    // A rows ar and ar + 64 (a warp's loads cover 128 bytes of each of
-    // eight rows), and half h (K 8*h .. 8*h+7) of B column q (a warp's
-    // loads are 32 consecutive columns of one row) ----
+    // A rows ar and ar + 64 (a warp's loads cover eight rows), and half h
+    // (K 8*h .. 8*h+7) of B column q (a warp's loads are 32 consecutive
+    // columns of one row) ----
     const int p = tid - 128, q = p % 128, h = p / 128;
     // lanes 8a .. 8a+7 of a warp take K-group a of eight consecutive rows,
     // so each quarter-warp's 16-byte stores fill 128 contiguous bytes
     const int ar = 8 * (p >> 5) + (p & 7), akg = (p >> 3) & 3;
-    const float2 zero = make_float2(0.f, 0.f);
-    float2 av0[8], bv0[8], av1[8], bv1[8];
+    S zero;
+    if constexpr (CPLX) zero = make_float2(0.f, 0.f); else zero = 0.f;
+    S av0[8], bv0[8], av1[8], bv1[8];
     int g = 0;  // chunk counter over all tiles of this CTA
     bool ok = true;
     for (int it = blockIdx.x; it < ntiles && ok; it += gridDim.x) {
       const DNode nd = nodes[tiles[8 * it]];
       const Tile tl = tile_of(tiles + 8 * it);
-      const float2* F = arena + nd.off;
+      const S* F = arena + nd.off;
       const bool arow0 = ar < tl.nrow, arow1 = ar + 64 < tl.nrow, bcol = q < tl.ncol;
-      const float2* Arow0 = F + (int64_t)(tl.row0 + (arow0 ? ar : 0)) * nd.f + tl.kk0 + 4 * akg;
-      const float2* Arow1 =
-          F + (int64_t)(tl.row0 + (arow1 ? ar + 64 : 0)) * nd.f + tl.kk0 + 4 * akg;
-      const float2* Bcol = F + (int64_t)tl.kk0 * nd.f + tl.col0 + (bcol ? q : 0);
+      const S* Arow0 = F + (int64_t)(tl.row0 + (arow0 ? ar : 0)) * nd.f + tl.kk0 + 4 * akg;
+      const S* Arow1 = F + (int64_t)(tl.row0 + (arow1 ? ar + 64 : 0)) * nd.f + tl.kk0 + 4 * akg;
+      const S* Bcol = F + (int64_t)tl.kk0 * nd.f + tl.col0 + (bcol ? q : 0);
       const int nch = (tl.K + KC - 1) / KC;
-      auto load = [&](float2* a, float2* b, int c) {
+      auto load = [&](S* a, S* b, int c) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int k = c * KC + 4 * akg + j;
@@ -255,14 +291,15 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
       };
       // store a chunk's half into its stage, then reuse the registers for
       // the chunk two ahead
-      auto stage = [&](float2* a, float2* b, int c) -> bool {
+      auto stage = [&](S* a, S* b, int c) -> bool {
         const int s = g % STAGES;
         if (g >= STAGES && !wait_parity(smem_u32(&empty[s]), ((g / STAGES) - 1) & 1)) return false;
-        uint8_t* st = smem + s * STAGE_BYTES;
+        uint8_t* st = smem + s * SB;
         store_split(st, core_off(ar, akg), a);
         store_split(st, core_off(ar + 64, akg), a + 4);
 #pragma unroll
-        for (int kg = 0; kg < 2; ++kg) store_split(st + 4 * PLANE, core_off(q, 2 * h + kg), b + 4 * kg);
+        for (int kg = 0; kg < 2; ++kg)
+          store_split(st + NP * PLANE, core_off(q, 2 * h + kg), b + 4 * kg);
         asm volatile("fence.proxy.async.shared::cta;");
         arrive(smem_u32(&full[s]));
         ++g;
@@ -294,7 +331,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t dre = tmem + b * ACC_COLS, dim = dre + BN;
+        const uint32_t dre = tmem + b * ACC;
         for (int c = 0; c < nch; ++c, ++g) {
           const int s = g % STAGES;
           if (!wait_parity(smem_u32(&full[s]), (g / STAGES) & 1)) {
@@ -303,30 +340,37 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;");
-          const uint32_t base = smem_u32(smem + s * STAGE_BYTES);
+          const uint32_t base = smem_u32(smem + s * SB);
 #pragma unroll
           for (int ks = 0; ks < KC / 8; ++ks) {
-            uint64_t a[4], bb[4];
+            uint64_t a[NP], bb[NP];
 #pragma unroll
-            for (int p = 0; p < 4; ++p) {
+            for (int p = 0; p < NP; ++p) {
               a[p] = sdesc(base + p * PLANE + ks * 256);
-              bb[p] = sdesc(base + (4 + p) * PLANE + ks * 256);
+              bb[p] = sdesc(base + (NP + p) * PLANE + ks * 256);
             }
             const uint32_t first = (c > 0 || ks > 0) ? 1u : 0u;
-            // Re += Are*Bre - Aim*Bim
-            mma(dre, a[0], bb[0], pos, first);
-            mma(dre, a[0], bb[1], pos, 1);
-            mma(dre, a[1], bb[0], pos, 1);
-            mma(dre, a[2], bb[2], neg, 1);
-            mma(dre, a[2], bb[3], neg, 1);
-            mma(dre, a[3], bb[2], neg, 1);
-            // Im += Are*Bim + Aim*Bre
-            mma(dim, a[0], bb[2], pos, first);
-            mma(dim, a[0], bb[3], pos, 1);
-            mma(dim, a[1], bb[2], pos, 1);
-            mma(dim, a[2], bb[0], pos, 1);
-            mma(dim, a[2], bb[1], pos, 1);
-            mma(dim, a[3], bb[0], pos, 1);
+            if constexpr (CPLX) {
+              const uint32_t dim = dre + BN;
+              // Re += Are*Bre - Aim*Bim
+              mma(dre, a[0], bb[0], pos, first);
+              mma(dre, a[0], bb[1], pos, 1);
+              mma(dre, a[1], bb[0], pos, 1);
+              mma(dre, a[2], bb[2], neg, 1);
+              mma(dre, a[2], bb[3], neg, 1);
+              mma(dre, a[3], bb[2], neg, 1);
+              // Im += Are*Bim + Aim*Bre
+              mma(dim, a[0], bb[2], pos, first);
+              mma(dim, a[0], bb[3], pos, 1);
+              mma(dim, a[1], bb[2], pos, 1);
+              mma(dim, a[2], bb[0], pos, 1);
+              mma(dim, a[2], bb[1], pos, 1);
+              mma(dim, a[3], bb[0], pos, 1);
+            } else {
+              mma(dre, a[0], bb[0], pos, first);
+              mma(dre, a[0], bb[1], pos, 1);
+              mma(dre, a[1], bb[0], pos, 1);
+            }
           }
           commit(smem_u32(&empty[s]));
         }
@@ -350,18 +394,22 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
       const DNode nd = nodes[tiles[8 * it]];
       const Tile tl = tile_of(tiles + 8 * it);
       const int b = i & 1;
-      float2* buf = epi + warp * 32 * 17;  // [32 rows][17]
-      float2* Cw = arena + nd.off + (int64_t)(tl.row0 + warp * 32) * nd.f + tl.col0;
+      S* buf = epi + warp * 32 * 17;  // [32 rows][17]
+      S* Cw = arena + nd.off + (int64_t)(tl.row0 + warp * 32) * nd.f + tl.col0;
       // C of each 16-column block is requested before that block's TMEM
       // reads (the first one before the accumulator is ready): C is not
       // touched by the tile's main loop, so its load latency overlaps them
-      float2 cv[16];
+      S cv[16];
       auto load_c = [&](int cc) {
 #pragma unroll
         for (int t = 0; t < 16; ++t) {
           const int r = 2 * t + (lane >> 4), col = cc * 16 + (lane & 15);
-          cv[t] = (warp * 32 + r < tl.nrow && col < tl.ncol) ? Cw[(int64_t)r * nd.f + col]
-                                                           : make_float2(0.f, 0.f);
+          if (warp * 32 + r < tl.nrow && col < tl.ncol)
+            cv[t] = Cw[(int64_t)r * nd.f + col];
+          else if constexpr (CPLX)
+            cv[t] = make_float2(0.f, 0.f);
+          else
+            cv[t] = 0.f;
         }
       };
       load_c(0);
@@ -373,7 +421,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t tre = tmem + b * ACC_COLS + ((uint32_t)(warp * 32) << 16);
+      const uint32_t tre = tmem + b * ACC + ((uint32_t)(warp * 32) << 16);
 #pragma unroll 1
       for (int cc = 0; cc < BN / 16; ++cc) {
         if (cc > 0) load_c(cc);
@@ -384,24 +432,32 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
               "=r"(re[6]), "=r"(re[7]), "=r"(re[8]), "=r"(re[9]), "=r"(re[10]), "=r"(re[11]),
               "=r"(re[12]), "=r"(re[13]), "=r"(re[14]), "=r"(re[15])
             : "r"(tre + cc * 16));
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-            : "=r"(im[0]), "=r"(im[1]), "=r"(im[2]), "=r"(im[3]), "=r"(im[4]), "=r"(im[5]),
-              "=r"(im[6]), "=r"(im[7]), "=r"(im[8]), "=r"(im[9]), "=r"(im[10]), "=r"(im[11]),
-              "=r"(im[12]), "=r"(im[13]), "=r"(im[14]), "=r"(im[15])
-            : "r"(tre + BN + cc * 16));
+        if constexpr (CPLX)
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+              : "=r"(im[0]), "=r"(im[1]), "=r"(im[2]), "=r"(im[3]), "=r"(im[4]), "=r"(im[5]),
+                "=r"(im[6]), "=r"(im[7]), "=r"(im[8]), "=r"(im[9]), "=r"(im[10]), "=r"(im[11]),
+                "=r"(im[12]), "=r"(im[13]), "=r"(im[14]), "=r"(im[15])
+              : "r"(tre + BN + cc * 16));
         asm volatile("tcgen05.wait::ld.sync.aligned;");
         // lane = row: park the 16 values, then read them back column-major
 #pragma unroll
-        for (int j = 0; j < 16; ++j)
-          buf[lane * 17 + j] = make_float2(__uint_as_float(re[j]), __uint_as_float(im[j]));
+        for (int j = 0; j < 16; ++j) {
+          if constexpr (CPLX)
+            buf[lane * 17 + j] = make_float2(__uint_as_float(re[j]), __uint_as_float(im[j]));
+          else
+            buf[lane * 17 + j] = __uint_as_float(re[j]);
+        }
         __syncwarp();
 #pragma unroll
         for (int t = 0; t < 16; ++t) {
           const int r = 2 * t + (lane >> 4), col = cc * 16 + (lane & 15);
           if (warp * 32 + r < tl.nrow && col < tl.ncol) {
-            const float2 dv = buf[r * 17 + (lane & 15)];
-            Cw[(int64_t)r * nd.f + col] = make_float2(cv[t].x - dv.x, cv[t].y - dv.y);
+            const S dv = buf[r * 17 + (lane & 15)];
+            if constexpr (CPLX)
+              Cw[(int64_t)r * nd.f + col] = make_float2(cv[t].x - dv.x, cv[t].y - dv.y);
+            else
+              Cw[(int64_t)r * nd.f + col] = cv[t] - dv;
           }
         }
         __syncwarp();
@@ -414,6 +470,5 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   if (warp == MMA_WARP)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TM));
 }
