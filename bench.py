@@ -208,6 +208,8 @@ def run_gpu(args):
     V = FunctionSpace(mesh, order=ORDER)
     h = V.upload()
     lu = lu_for_space(V)
+    from sucemfem import autotune
+    tuner = autotune.Autotuner()
     stream = torch.cuda.current_stream(dev)
     sp = stream.cuda_stream
     d_eps32 = torch.as_tensor(eps, dtype=torch.float32, device=dev)
@@ -260,6 +262,12 @@ def run_gpu(args):
         launches = lib.sucem_launch_count() - l0
         return lat, fac, infos, launches, x
 
+    # LU plan (super-panel width, tensor-core panel threshold) from the
+    # autotuner: cached per device and size class, else timed trials now,
+    # before the timed region
+    call("sucem_assemble_helmholtz", h, 4, ptr(d_eps32), None, float(k0), ptr(A32), sp)
+    trials0 = tuner.trials
+    plan = autotune.tune_lu(lu, A32, "c64", tuner)
     clocks = ClockSampler()
     clocks.start()
     time.sleep(0.3)
@@ -362,7 +370,18 @@ def run_gpu(args):
                 "h2d_bytes_per_step": int(V.n * 16), "d2h_bytes_per_step": int(V.n * 16)},
         "gpu_launches": int(launches32),
         "clocks": clk,
+        "lu_plan": {"superpanel": int(plan[0]), "panel_min_k": int(plan[1]),
+                    "autotune_trials_this_run": tuner.trials - trials0,
+                    "note": "chosen by sucemfem.autotune from timed factorisations (cached per "
+                            "device and size class)"},
     }
+    if not args.no_secondary and world == 1:
+        # the batched-eigen and serving configurations, each with its own
+        # clock record (after the headline's timed region)
+        torch.cuda.empty_cache()
+        line["eigen_batch"] = measure_eigen_batch(args.cavities, with_oracle=True)
+        torch.cuda.empty_cache()
+        line["serve"] = measure_serve(args, tuner)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:
@@ -649,37 +668,65 @@ def run_postproc(args):
     print(json.dumps(out))
 
 
-def run_eigen_batch(args):
-    """Batched cavities: 256 PEC boxes, sides U[0.3,1.5] m, divisions U{4..24}
-    per axis, order 1, eps_r U[1,4] per cell; one space, one assembly launch,
-    one LU of the stacked problem, one batched shift-invert Lanczos for the 6
-    smallest k^2 above sigma=1 of every cavity (FP32 LU, FP64 Lanczos/RR)."""
-    import torch
-    from sucemfem import _device
-    from sucemfem._native import call, ptr
-    from sucemfem.eigen import BatchedShiftInvertLanczos
-    from sucemfem.mesh import BoxMesh, Mesh
-    from sucemfem.space import FunctionSpace
-    dev = _device.device()
-    rng = np.random.default_rng(0)
-    ncav = args.cavities
-    coords, cells, seg_cells, off, x0 = [], [], [], 0, 0.0
+def eigen_cavities(ncav, seed=0):
+    """The batched-cavity configuration: ncav PEC boxes, sides U[0.3,1.5] m,
+    divisions U{4..24} per axis, eps_r U[1,4] per cell (one stacked mesh,
+    boxes side by side)."""
+    from sucemfem.mesh import BoxMesh
+    rng = np.random.default_rng(seed)
+    boxes, coords, cells, seg_cells, off, x0 = [], [], [], [], 0, 0.0
     for k in range(ncav):
         L = rng.uniform(0.3, 1.5, 3)
         n = rng.integers(4, 25, 3)
         m = BoxMesh(L[0], L[1], L[2], int(n[0]), int(n[1]), int(n[2]), origin=(x0, 0.0, 0.0))
         x0 += L[0] + 0.5
+        boxes.append((m.coordinates(), m.cells()))
         coords.append(m.coordinates())
         cells.append(m.cells() + off)
         off += len(m.coordinates())
         seg_cells.append(np.full(m.num_cells(), k))
+    return boxes, np.concatenate(coords), np.concatenate(cells), np.concatenate(seg_cells), rng
+
+
+def oracle_cavity_k2(coords, cells, eps, nev, sigma=1.0):
+    """FP64 CPU oracle: the nev smallest k^2 above sigma of a PEC cavity
+    (oracle assembly, PEC DOFs removed, scipy shift-invert eigsh)."""
+    import scipy.sparse.linalg as spl
+    from oracle import fem
+    A = fem.assemble(coords, cells, 1, eps_r=eps, with_abc=False)
+    pec = fem.pec_dofs(A.topo, 1)
+    keep = np.setdiff1d(np.arange(A.n), pec)
+    S = A.S[keep][:, keep].tocsc()
+    T = A.T[keep][:, keep].tocsc()
+    w = spl.eigsh(S, M=T, k=nev + 4, sigma=sigma, which="LM", return_eigenvectors=False)
+    w = np.sort(w[w > sigma + 1e-6])
+    return w[:nev]
+
+
+def measure_eigen_batch(ncav, with_oracle=False, nev=6):
+    """Batched cavities through one space, one assembly launch, one FP32 LU
+    of the stacked problem and one batched shift-invert Lanczos for the nev
+    smallest k^2 above sigma=1 of every cavity (FP64 Lanczos/RR), wall time
+    from assembly to eigenvalues on the host; with_oracle: the largest
+    relative k^2 error against the FP64 oracle on the three cavities with
+    the fewest cells."""
+    import torch
+    from sucemfem import _device
+    from sucemfem._native import call, ptr
+    from sucemfem.eigen import BatchedShiftInvertLanczos
+    from sucemfem.mesh import Mesh
+    from sucemfem.space import FunctionSpace
+    dev = _device.device()
+    boxes, coords, cells, seg_cells, rng = eigen_cavities(ncav)
     t0 = time.perf_counter()
-    V = FunctionSpace(Mesh(np.concatenate(coords), np.concatenate(cells)), order=1)
-    seg_cells = np.concatenate(seg_cells)
+    V = FunctionSpace(Mesh(coords, cells), order=1)
     dof_seg = np.zeros(V.n, dtype=np.int64)
     dof_seg[V.cell_dofs.ravel()] = np.repeat(seg_cells, 6)
     eps = rng.uniform(1.0, 4.0, V.nt)
     t_host = time.perf_counter() - t0
+    clocks = ClockSampler()
+    clocks.start()
+    time.sleep(0.3)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     S = torch.empty(V.nnz, dtype=torch.float64, device=dev)
@@ -688,37 +735,86 @@ def run_eigen_batch(args):
     call("sucem_assemble", V.upload(), 8, ptr(d_eps), None, ptr(S), ptr(T), None, _device.stream_ptr())
     sol = BatchedShiftInvertLanczos(V, S, T, V.boundary_dofs, 1.0, dof_segment=dof_seg)
     t2 = time.perf_counter()
-    k2, Z = sol.solve(6)
+    k2, _ = sol.solve(nev)
     torch.cuda.synchronize()
     t3 = time.perf_counter()
-    print(json.dumps({"case": "eigen-batch", "cavities": ncav, "tets": V.nt, "n_dofs": V.n,
-                      "host_build_s": t_host, "setup_s": t2 - t1, "solve_s": t3 - t2,
-                      "cavity_solves_per_s": ncav / (t3 - t1),
-                      "lanczos_steps": sol.stats.get("m"), "lu_arena_gb": sol.lu.info["arena"] * 4 / 1e9,
-                      "k2_first_cavity": [float(v) for v in np.sort(k2[0])]}))
+    clk = clocks.stop()
+    out = {"cavities": ncav, "tets": V.nt, "n_dofs": V.n, "nev": nev,
+           "cavity_solves_per_s": ncav / (t3 - t1), "seconds": t3 - t1,
+           "host_build_s": t_host, "setup_s": t2 - t1, "solve_s": t3 - t2,
+           "lanczos_steps": sol.stats.get("m"), "lu_arena_gb": sol.lu.info["arena"] * 4 / 1e9,
+           "precision": "FP32 LU (tensor-core updates) + FP64 Lanczos and Rayleigh-Ritz",
+           "clocks": clk}
+    if with_oracle:
+        sizes = [len(c) for _, c in boxes]
+        order = np.argsort(sizes)[:3]
+        starts = np.concatenate([[0], np.cumsum(sizes)])
+        errs = []
+        for k in order:
+            bc, bcells = boxes[k]
+            ek = eps[starts[k]:starts[k + 1]]
+            ref = oracle_cavity_k2(bc, bcells, ek, nev)
+            got = np.sort(k2[k])[:len(ref)]
+            errs.append(float(np.max(np.abs(got - ref) / ref)))
+        out["max_rel_k2_error_vs_oracle"] = max(errs)
+        out["oracle_cavities"] = [int(k) for k in order]
+    return out
 
 
-def run_serve(args):
-    """Serving workload (Poisson arrivals of driven ABC solves, divisions
-    log-uniform, order 1/2 at 50/50, 1-6 wavelengths per box, complex64 LU +
-    FP64 refinement to 1e-8) through the continuous-batching server, and the
-    same requests one at a time on the plain FP64 path."""
+def run_eigen_batch(args):
+    print(json.dumps(dict(case="eigen-batch", **measure_eigen_batch(args.cavities,
+                                                                     with_oracle=True))))
+
+
+def measure_serve(args, tuner=None):
+    """The serving configuration: a Poisson stream (mean args.serve_rate per
+    second) of driven ABC-box solves, divisions log-uniform in [6,
+    args.serve_max_cubes], order 1 or 2 at 50/50, k0 so that the box spans
+    1-6 wavelengths, complex64 LU + FP64 refinement to 1e-8, through the
+    continuous-batching server with HBM-budget admission (slot count from
+    the autotuner); the first args.serve_requests requests of the stream;
+    beside it the same kind of requests one at a time on the plain FP64
+    path (a sample)."""
+    from sucemfem import autotune
     from sucemfem.serving import SolveServer, make_request_stream
+    tuner = tuner or autotune.Autotuner()
     reqs = make_request_stream(args.serve_requests, args.serve_rate,
                                cubes=(6, args.serve_max_cubes), seed=0)
-    srv = SolveServer(slots=args.serve_slots, tol=1e-8)
+    # slot count: timed trials on a small fixed sample of the stream's kind
+    # (divisions 6-16), cached per device
+    sample = make_request_stream(12, 1000.0, cubes=(6, 16), seed=1)
+
+    def run_sample(slots):
+        t0 = time.perf_counter()
+        SolveServer(slots=slots, tol=1e-8).run(sample, realtime=False)
+        return time.perf_counter() - t0
+    trials0 = tuner.trials
+    slots = autotune.tune_slots(run_sample, tuner, key="serve_driven_abc")
+    clocks = ClockSampler()
+    clocks.start()
+    srv = SolveServer(slots=slots, tol=1e-8, tuner=tuner)
     res = srv.run(reqs, realtime=True)
+    clk = clocks.stop()
     n64 = min(len(reqs), args.serve_fp64_sample)
     one = SolveServer(slots=1, precision="fp64", tol=1e-8)
     one.run(reqs[:n64], realtime=False)
-    print(json.dumps({
-        "case": "serve", "requests": len(reqs), "rate_per_s": args.serve_rate,
-        "cubes": [6, args.serve_max_cubes], "slots": args.serve_slots,
-        "server": srv.stats,
-        "max_residual": max(r.residual for r in res if r.status == "ok"),
-        "fp64_one_at_a_time": {"requests": n64, "solves_per_s": one.stats["solves_per_s"],
-                               "p50_ms": one.stats["p50_ms"]},
-    }))
+    ok = [r for r in res if r.status == "ok"]
+    return {"requests": len(reqs), "rate_per_s": args.serve_rate,
+            "stream": "first %d requests of the seeded Poisson stream (%.1f s of arrivals)"
+                      % (len(reqs), reqs[-1].arrival if reqs else 0.0),
+            "cubes": [6, args.serve_max_cubes], "orders": [1, 2], "wavelengths": [1, 6],
+            "slots": slots, "slot_trials_this_run": tuner.trials - trials0,
+            "solves_per_s": srv.stats["solves_per_s"], "p50_ms": srv.stats["p50_ms"],
+            "p99_ms": srv.stats["p99_ms"], "completed": srv.stats["completed"],
+            "rejected": srv.stats["rejected"], "max_inflight": srv.stats["max_inflight"],
+            "max_residual": max(r.residual for r in ok) if ok else None,
+            "fp64_one_at_a_time": {"requests": n64, "solves_per_s": one.stats["solves_per_s"],
+                                   "p50_ms": one.stats["p50_ms"]},
+            "clocks": clk}
+
+
+def run_serve(args):
+    print(json.dumps(dict(case="serve", **measure_serve(args))))
 
 
 def run_high_order(args):
@@ -819,11 +915,12 @@ def main():
                     help="profiling cases: factor / assemble at --cubes, --order; serve; precision")
     ap.add_argument("--precision-solve-cubes", type=int, default=30)
     ap.add_argument("--cavities", type=int, default=256)
-    ap.add_argument("--serve-requests", type=int, default=200)
-    ap.add_argument("--serve-rate", type=float, default=20.0)
-    ap.add_argument("--serve-max-cubes", type=int, default=16)
-    ap.add_argument("--serve-slots", type=int, default=4)
-    ap.add_argument("--serve-fp64-sample", type=int, default=20)
+    ap.add_argument("--serve-requests", type=int, default=300)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-max-cubes", type=int, default=48)
+    ap.add_argument("--serve-fp64-sample", type=int, default=10)
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="headline solve only (no batched-eigen and serving keys)")
     ap.add_argument("--cubes", type=int, default=N_CUBES)
     ap.add_argument("--order", type=int, default=ORDER)
     ap.add_argument("--gpus", type=int, default=1)

@@ -345,6 +345,14 @@ int sucem_lu_inject_timeout(sucem_lu* lu);
  * algorithmic flops (8 per complex multiply-add)}.  No reference
  * counterpart (measurement hook). */
 int sucem_lu_kernel_stats(sucem_lu* lu, double* out);
+/* Plan parameters of the single-precision factorisation (tensor-core path),
+ * 0 = default: the super-panel width (a positive multiple of 64; default
+ * 512) and the smallest pivot block for which a level of two or more
+ * fronts applies its 64-column panel updates on the tensor cores (default
+ * 64).  The device state is rebuilt at the next sucem_lu_factor.  Used by
+ * the autotuner (sucemfem/autotune.py).  No reference counterpart
+ * (dolfin.LUSolver / UMFPACK take no such parameters). */
+int sucem_lu_configure(sucem_lu* lu, int superpanel, int panel_min_k);
 
 /* Self-test of the device-side failure detection: one thread of a one-block
  * kernel waits, with the tensor-core kernel's bounded mbarrier wait limited

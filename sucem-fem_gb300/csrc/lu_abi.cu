@@ -167,6 +167,15 @@ int sucem_selftest_bounded_wait(int polls, int* gave_up) {
   return SUCEM_OK;
 }
 
+int sucem_lu_configure(sucem_lu* lu, int superpanel, int panel_min_k) {
+  if (!lu) return fail("null argument", SUCEM_ERR_ARG);
+  cudaError_t e = sucem::mf_configure(*lu->h, superpanel, panel_min_k);
+  if (e == cudaErrorInvalidValue)
+    return fail("superpanel must be 0 or a positive multiple of 64, panel_min_k >= 0", SUCEM_ERR_ARG);
+  if (e != cudaSuccess) return cuda_fail(e, "sucem_lu_configure");
+  return SUCEM_OK;
+}
+
 int sucem_lu_kernel_stats(sucem_lu* lu, double* out) {
   if (!lu || !out) return fail("null argument", SUCEM_ERR_ARG);
   sucem::mf_tc_stats(*lu->h, out);

@@ -75,6 +75,10 @@ int mf_factor_status(MFHandle& h);
 // host-side failure injection for tests: marks the last factorisation as if
 // a bounded wait of its tensor-core update had given up
 cudaError_t mf_mark_timed_out(MFHandle& h);
+// plan parameters of the single-precision factorisation (0 = default):
+// super-panel width (a multiple of 64) and the pivot-block threshold of the
+// tensor-core panel updates; the device state is rebuilt at the next factor
+cudaError_t mf_configure(MFHandle& h, int superpanel, int panel_k);
 // tensor-core update launches of the last factorisation: out[0] launches,
 // out[1] their summed event-timed duration (ms), out[2] algorithmic flops
 void mf_tc_stats(MFHandle& h, double* out);

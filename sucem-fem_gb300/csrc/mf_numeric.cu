@@ -954,6 +954,11 @@ struct MFDevice {
 struct MFHandle {
   MFSymbolic sym;
   MFDevice dev;
+  // plan parameters chosen by the caller (sucem_lu_configure; 0 = default):
+  // super-panel width and the pivot-block threshold of the tensor-core
+  // panel updates
+  int cfg_superpanel = 0;
+  int cfg_panel_k = 0;
 };
 
 namespace {
@@ -1027,15 +1032,17 @@ void add_tiles(std::vector<int32_t>& tl, int32_t node, int64_t r0, int64_t r1, i
     }
 }
 
-cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s, double mac_flops) {
+cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s, double mac_flops, int cfg_sp, int cfg_pk) {
   d.tc_sp = kTcSuperPanel;
   d.tc_panel_k = kTcPanelMinK;
   if (const char* v = getenv("SUCEM_LU_TC_PANEL_K")) d.tc_panel_k = atoi(v);
+  if (cfg_pk > 0) d.tc_panel_k = cfg_pk;
   cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, d.device);
   if (const char* v = getenv("SUCEM_LU_SUPERPANEL")) {
     const int w = atoi(v);
     if (w >= kTcPanel && w % kTcPanel == 0) d.tc_sp = w;
   }
+  if (cfg_sp >= kTcPanel && cfg_sp % kTcPanel == 0) d.tc_sp = cfg_sp;
   const int sp = d.tc_sp;
   for (auto& L : d.levels) {
     std::vector<std::pair<int, int32_t>> ends;  // (p0, node)
@@ -1151,8 +1158,10 @@ cudaError_t setup_device(MFHandle& h, int dtype) {
   if (e == cudaSuccess) e = cudaMalloc(&d.arena, (size_t)std::max<int64_t>(s.arena, 1) * d.elem);
   if (e == cudaSuccess) e = cudaMalloc(&d.d_x, (size_t)std::max<int64_t>(s.n, 1) * d.elem);
   if (e == cudaSuccess) e = cudaMalloc((void**)&d.d_flag, 16);
-  if (e == cudaSuccess && dtype == SUCEM_C64) e = plan_tc(d, s, kMacFlops<float2>);
-  if (e == cudaSuccess && dtype == SUCEM_F32) e = plan_tc(d, s, kMacFlops<float>);
+  if (e == cudaSuccess && dtype == SUCEM_C64)
+    e = plan_tc(d, s, kMacFlops<float2>, h.cfg_superpanel, h.cfg_panel_k);
+  if (e == cudaSuccess && dtype == SUCEM_F32)
+    e = plan_tc(d, s, kMacFlops<float>, h.cfg_superpanel, h.cfg_panel_k);
   if (e != cudaSuccess) free_dev(d);
   return e;
 }
@@ -1519,6 +1528,19 @@ int mf_perturbed(MFHandle& h) {
   if (st == -2) return 0;
   // d_flag[1]: a bounded wait of the tensor-core update gave up
   return st < 0 ? -1 : h.dev.perturbed;
+}
+
+// new plan parameters: the device state (arena, plan) is rebuilt at the
+// next factorisation
+cudaError_t mf_configure(MFHandle& h, int superpanel, int panel_k) {
+  if (superpanel != 0 && (superpanel < kTcPanel || superpanel % kTcPanel != 0))
+    return cudaErrorInvalidValue;
+  if (panel_k < 0) return cudaErrorInvalidValue;
+  if (superpanel == h.cfg_superpanel && panel_k == h.cfg_panel_k) return cudaSuccess;
+  h.cfg_superpanel = superpanel;
+  h.cfg_panel_k = panel_k;
+  free_dev(h.dev);
+  return cudaSuccess;
 }
 
 void mf_tc_stats(MFHandle& h, double* out) {

@@ -24,6 +24,7 @@ _native.declare("sucem_lu_perturbed", ctypes.c_int, [c_vp])
 _native.declare("sucem_lu_kernel_stats", ctypes.c_int, [c_vp, c_vp])
 _native.declare("sucem_lu_status", ctypes.c_int, [c_vp])
 _native.declare("sucem_lu_inject_timeout", ctypes.c_int, [c_vp])
+_native.declare("sucem_lu_configure", ctypes.c_int, [c_vp, ctypes.c_int, ctypes.c_int])
 
 DTYPES = {"f32": _native.F32, "f64": _native.F64, "c64": _native.C64, "c128": _native.C128}
 
@@ -60,6 +61,7 @@ class SparseLU:
         self.info = dict(n=int(info[0]), nnz=int(info[1]), nodes=int(info[2]), levels=int(info[3]),
                          arena=int(info[4]), flops=float(info[5]), max_front=int(info[6]))
         self.dtype = None
+        self.params = (0, 0)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -87,6 +89,15 @@ class SparseLU:
         call("sucem_lu_factor", self._h, code, ptr(values), float(pivot_tol),
              stream if stream is not None else _device.stream_ptr())
         self.dtype = dtype
+        return self
+
+    def configure(self, superpanel=0, panel_min_k=0):
+        """Plan parameters of the single-precision factorisation (0 =
+        default): super-panel width (multiple of 64) and the pivot-block
+        threshold of the tensor-core panel updates.  Takes effect at the
+        next factor()."""
+        call("sucem_lu_configure", self._h, int(superpanel), int(panel_min_k))
+        self.params = (int(superpanel), int(panel_min_k))
         return self
 
     @staticmethod

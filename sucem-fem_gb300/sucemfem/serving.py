@@ -25,7 +25,7 @@ from dataclasses import dataclass, field
 import numpy as np
 import torch
 
-from . import _device
+from . import _device, autotune
 from .Consts import c0, Z0
 from .mesh import BoxMesh
 from .Sources.point_source import evaluate_point_sources
@@ -76,12 +76,20 @@ def make_request_stream(n, rate, cubes=(6, 48), orders=(1, 2), wavelengths=(1.0,
 
 
 class _Prepared:
-    def __init__(self, req):
+    def __init__(self, req, tuner=None):
         self.req = req
         mesh = BoxMesh(req.size, req.size, req.size, req.cubes, req.cubes, req.cubes)
         self.V = FunctionSpace(mesh, order=req.order)
         self.eps = np.random.default_rng(req.seed).uniform(1.0, 4.0, self.V.nt)
         self.lu = lu_for_space(self.V, leaf_size=96)
+        if tuner is not None:
+            # an LU plan tuned earlier for this size class (no trials here:
+            # they would add to this request's latency)
+            key = autotune.size_class(self.lu.info["n"], self.lu.info["nnz"],
+                                      "c64_f%d" % self.lu.info["max_front"])
+            plan = tuner.lookup("lu_plan", key)
+            if plan is not None:
+                self.lu.configure(*plan)
         n, nnz = self.V.n, self.V.nnz
         # complex64 arena + A32 + A64 + 3x pattern ints + solver vectors (~40 n complex128)
         self.bytes = (self.lu.info["arena"] * 8 + nnz * (8 + 16 + 4) + (n + 1) * 4 + n * 16 * 40
@@ -90,7 +98,7 @@ class _Prepared:
 
 class SolveServer:
     def __init__(self, hbm_budget_bytes=None, slots=4, precision="fp32-ir", tol=1e-8,
-                 prep_workers=4, keep_solutions=False):
+                 prep_workers=4, keep_solutions=False, tuner=None):
         dev = _device.device()
         free, total = torch.cuda.mem_get_info(dev)
         self.budget = int(hbm_budget_bytes if hbm_budget_bytes is not None else 0.8 * free)
@@ -99,6 +107,7 @@ class SolveServer:
         self.tol = tol
         self.prep_workers = prep_workers
         self.keep = keep_solutions
+        self.tuner = tuner
         self._lock = threading.Lock()
         self._reserved = 0
         self.stats = {}
@@ -151,7 +160,7 @@ class SolveServer:
                         wait = r.arrival * time_scale - (time.perf_counter() - t0)
                         if wait > 0:
                             time.sleep(wait)
-                    futs.append(ex.submit(_Prepared, r))
+                    futs.append(ex.submit(_Prepared, r, self.tuner))
                     futs[-1].add_done_callback(lambda f: prepared.put(f))
                 for f in futs:
                     f.exception()
