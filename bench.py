@@ -698,9 +698,10 @@ def oracle_cavity_k2(coords, cells, eps, nev, sigma=1.0):
     keep = np.setdiff1d(np.arange(A.n), pec)
     S = A.S[keep][:, keep].tocsc()
     T = A.T[keep][:, keep].tocsc()
-    w = spl.eigsh(S, M=T, k=nev + 4, sigma=sigma, which="LM", return_eigenvectors=False)
-    w = np.sort(w[w > sigma + 1e-6])
-    return w[:nev]
+    # shift-invert: 'LA' on nu = 1/(k^2 - sigma) picks the k^2 just above
+    # sigma (the gradient null space, k^2 = 0, lies below it)
+    w = spl.eigsh(S, M=T, k=nev, sigma=sigma, which="LA", return_eigenvectors=False)
+    return np.sort(w)
 
 
 def measure_eigen_batch(ncav, with_oracle=False, nev=6):
