@@ -345,6 +345,26 @@ int sucem_lu_inject_timeout(sucem_lu* lu);
  * algorithmic flops (8 per complex multiply-add)}.  No reference
  * counterpart (measurement hook). */
 int sucem_lu_kernel_stats(sucem_lu* lu, double* out);
+/* Preconditioned BiCGStab on the device, every scalar kept in device
+ * memory.  Replaces BiCGStabSolver (sucemfem/Utilities/LinalgSolvers.py:
+ * 239-248: scipy.sparse.linalg.bicgstab with the preconditioner of :107-127).
+ * A: CSR of n rows (int32 indptr[n+1], indices; values of dtype SUCEM_C64 or
+ * SUCEM_C128); b, x: device vectors of that dtype (x holds the initial
+ * guess on entry, the solution on exit).  precond: 0 none, 1 diagonal
+ * (inverse of A's diagonal), 2 the factorisation `lu` (sucem_lu_solve).
+ * Stops at ||b - A x|| <= tol ||b|| or after maxit iterations.  Without an
+ * LU preconditioner `batch` iterations are captured once into a CUDA graph
+ * and replayed; the host reads one status word per batch (with LU: per
+ * iteration).  work: device buffer of sucem_bicgstab_work_bytes(n, dtype)
+ * bytes.  info[4] = {iterations, ||r||/||b|| (recurrence residual),
+ * status (1 converged, 2 iteration limit, -1 breakdown rho = 0,
+ * -2 breakdown omega = 0), host synchronisations}. */
+int64_t sucem_bicgstab_work_bytes(int64_t n, int dtype);
+int sucem_bicgstab(int64_t n, const int32_t* indptr, const int32_t* indices, int dtype,
+                   const void* vals, const void* b, void* x, int precond, sucem_lu* lu,
+                   double tol, int maxit, int batch, void* work, int64_t work_bytes, double* info,
+                   void* stream);
+
 /* Plan parameters of the single-precision factorisation (tensor-core path),
  * 0 = default: the super-panel width (a positive multiple of 64; default
  * 512) and the smallest pivot block for which a level of two or more

@@ -44,7 +44,7 @@ def _driven(order=1):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("cls", ["BiCGStabSolver", "GMRESSolver", "UMFPACKSolver"])
+@pytest.mark.parametrize("cls", ["BiCGStabSolver", "HostBiCGStabSolver", "GMRESSolver", "UMFPACKSolver"])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_solvers_on_driven_system(cls, precision):
     LS = _ls()
