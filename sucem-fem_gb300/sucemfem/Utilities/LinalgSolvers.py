@@ -166,20 +166,19 @@ class BiCGStabSolver(SystemSolverBase):
     """Preconditioned BiCGStab (right preconditioning) on the GPU, every
     scalar on the device (sucemfem.krylov): the host reads a status word
     once per batch of iterations (per iteration with the LU
-    preconditioner), not once per dot product.  Real systems run in complex
-    arithmetic with zero imaginary parts.  The residual log gets the final
-    relative residual (the iteration does not stop for the host)."""
+    preconditioner), not once per dot product.  Real systems (whose LU is
+    real) take the host-driven iteration of HostBiCGStabSolver.  The
+    residual log gets the final relative residual (the iteration does not
+    stop for the host)."""
     batch = 32
 
     def _call_solver(self):
         from ..krylov import bicgstab
         s = self._sys
-        b = s.to_dev(self._b)
         if not s.complex:
-            A = DeviceCSR(s.csr.indptr, s.csr.indices, s.csr.values.to(torch.complex128), s.n)
-            b = b.to(torch.complex128)
-        else:
-            A = s.csr
+            return HostBiCGStabSolver._call_solver(self)
+        b = s.to_dev(self._b)
+        A = s.csr
         M = None
         if self._M is not None:
             M = s.lu() if self._M_type == "ilu" else "diagonal"
@@ -188,8 +187,6 @@ class BiCGStabSolver(SystemSolverBase):
         self._callback(info["residual"])
         self.info_device = info
         xh = x.cpu().numpy()
-        if not s.complex:
-            xh = xh.real.copy()
         if info["status"] == 1:
             return xh, 0
         if info["status"] == 2:
