@@ -120,7 +120,6 @@ class SolveServer:
         with torch.cuda.stream(stream):
             sp = stream.cuda_stream
             h = V.upload()
-            e32 = torch.as_tensor(p.eps, dtype=torch.float32, device=dev)
             e64 = torch.as_tensor(p.eps, dtype=torch.float64, device=dev)
             A64 = torch.empty(V.nnz, dtype=torch.complex128, device=dev)
             call("sucem_assemble_helmholtz", h, 8, ptr(e64), None, float(req.k0), ptr(A64), sp)
@@ -130,8 +129,9 @@ class SolveServer:
             if self.precision == "fp64":
                 rs.factor(A64, "c128")
             else:
-                A32 = torch.empty(V.nnz, dtype=torch.complex64, device=dev)
-                call("sucem_assemble_helmholtz", h, 4, ptr(e32), None, float(req.k0), ptr(A32), sp)
+                # the single-precision LU input: the FP64 matrix rounded
+                # (one refinement iteration fewer than the FP32 assembly's)
+                A32 = rs.vec.convert(A64, torch.empty(V.nnz, dtype=torch.complex64, device=dev))
                 rs.factor(A32, "c64")
             c = req.size / 2
             _, dofs, con = evaluate_point_sources(V, np.array([[c, c, c]]), np.array([[0, 0, 1.0]]))

@@ -217,8 +217,13 @@ def lu_for_space(V, leaf_size=128):
 class DrivenSolver:
     """Assemble and solve (S - k0^2 T + j k0 B) x = b on the GPU.
 
-    precision 'fp32-ir': FP32 assembly and complex64 LU, FP64-assembled
-    matrix for the FGMRES refinement; 'fp64': everything in double."""
+    precision 'fp32-ir': complex64 LU of the FP64-assembled matrix rounded
+    to single precision, the FP64 matrix for the FGMRES refinement (the
+    refinement needs the FP64 matrix anyway, and its rounding is the most
+    accurate single-precision input: on the 20^3 order-2 box it takes 5
+    refinement iterations where the single-precision assembly's matrix,
+    2e-7 of its row scale off, takes 6); 'fp32-asm': the LU input from the
+    single-precision assembly instead; 'fp64': everything in double."""
 
     def __init__(self, V, eps_r=None, mu_r_inv=None, lu=None):
         self.V = V
@@ -259,7 +264,11 @@ class DrivenSolver:
         if precision == "fp64":
             rs.factor(self.A64, "c128")
         else:
-            self.A32 = self.assemble(k0, 4)
+            if precision == "fp32-asm":
+                self.A32 = self.assemble(k0, 4)
+            else:
+                self.A32 = rs.vec.convert(self.A64, torch.empty(self.V.nnz, dtype=torch.complex64,
+                                                                 device=self.A64.device))
             rs.factor(self.A32, "c64")
         x, info = rs.solve(b, tol=tol, method=method, maxit=maxit)
         info["perturbed_pivots"] = self.lu.perturbed()
