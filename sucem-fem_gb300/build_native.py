@@ -41,7 +41,7 @@ def build(verbose=False, force=False):
     if not all(os.path.exists(p) for p in (tables, tables_hi, contract)):
         _run([sys.executable, os.path.join(CSRC, "gen_tables.py"), tables, tables_hi, contract])
     srcs = _sources()
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "sucem_gb300.h"))
     newest_dep = max(os.path.getmtime(p) for p in srcs + headers)
     if not force and os.path.exists(OUT) and os.path.getmtime(OUT) >= newest_dep:

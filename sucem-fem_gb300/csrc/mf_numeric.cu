@@ -14,6 +14,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
+#include <map>
 #include <cstdio>
 #include <cstring>
 
@@ -902,9 +904,11 @@ __global__ void permute_out_kernel(int64_t n, const int64_t* __restrict__ perm,
 // one tensor-core trailing update: the fronts of a level whose super-panel
 // ends with the panel at p0
 struct TcLaunch {
-  int p0 = 0, ntiles = 0;
+  int p0 = 0, ntiles = 0, nchunks = 0;
   double flops = 0;                 // algorithmic flops (8 per complex MAC)
-  int32_t* d_tiles = nullptr;       // 8 ints per tile: node, row0, col0, nrow, ncol, kk0, K, 0
+  int32_t* d_tiles = nullptr;       // tc::TD ints per tile (see tc::tile_of)
+  int32_t* d_strips = nullptr;      // 8 ints per operand strip (see tc_presplit_kernel)
+  int32_t* d_chunk_strip = nullptr; // the strip of every K-chunk image
 };
 
 struct MFLevel {
@@ -940,6 +944,7 @@ struct MFDevice {
   int tc_sp = 0;                    // super-panel width of the tensor-core path (complex64)
   int sm_count = 1;                 // multiprocessors of the device
   int tc_panel_k = 0;               // see kTcPanelMinK
+  uint8_t* d_img = nullptr;         // split operand chunk images of one tensor-core launch
   std::vector<MFLevel> levels;
   bool factored = false;
   int perturbed = 0;
@@ -983,15 +988,19 @@ cudaError_t upv(T** d, const std::vector<T>& h) {
 }
 
 void free_dev(MFDevice& d) {
-  void* ptrs[] = {d.arena, d.d_nodes, d.d_U, d.d_ea, d.d_src, d.d_dst, d.d_perm, d.d_x, d.d_flag};
+  void* ptrs[] = {d.arena, d.d_nodes, d.d_U, d.d_ea, d.d_src, d.d_dst, d.d_perm, d.d_x, d.d_flag,
+                  d.d_img};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  d.d_img = nullptr;
   for (auto& L : d.levels) {
     if (L.d_nodes) cudaFree(L.d_nodes);
-    for (auto& t : L.tcl)
-      if (t.d_tiles) cudaFree(t.d_tiles);
-    for (auto& t : L.tcp)
-      if (t.d_tiles) cudaFree(t.d_tiles);
+    for (auto* v : {&L.tcl, &L.tcp})
+      for (auto& t : *v) {
+        int32_t* q[] = {t.d_tiles, t.d_strips, t.d_chunk_strip};
+        for (int32_t* p : q)
+          if (p) cudaFree(p);
+      }
     for (int s = 0; s < 2; ++s)
       if (L.d_kids[s]) cudaFree(L.d_kids[s]);
   }
@@ -1019,20 +1028,70 @@ constexpr int kTcSuperPanel = 512;
 constexpr int kTcPanelMinK = 64;
 constexpr int kTcPanel = 64;  // panel width of the complex64 factorisation
 
+// the tiles of one tensor-core launch and the operand strips they read
+struct TcPlan {
+  std::vector<int32_t> tiles;                                  // tc::TD ints per tile
+  std::vector<int32_t> strips;                                 // 8 ints per strip
+  std::map<std::array<int64_t, 5>, int32_t> strip_of;          // (node, side, first, kk0, K)
+  int32_t strip(int32_t node, int side, int64_t first, int64_t n, int64_t kk0, int64_t K) {
+    const std::array<int64_t, 5> key = {node, side, first, kk0, K};
+    auto it = strip_of.find(key);
+    if (it != strip_of.end()) {
+      // one strip serves tiles of different extents: stage the widest (the
+      // extra rows/columns only reach outputs that the narrower tile skips)
+      int32_t& m = strips[8 * it->second + 2];
+      m = std::max<int32_t>(m, (int32_t)n);
+      return it->second;
+    }
+    const int32_t id = (int32_t)(strips.size() / 8);
+    const int32_t v[8] = {node, (int32_t)first, (int32_t)n, (int32_t)kk0, (int32_t)K, 0, side, 0};
+    strips.insert(strips.end(), v, v + 8);
+    strip_of.emplace(key, id);
+    return id;
+  }
+};
+
 // 128 x 128 tiles of rows [r0, r1) x columns [c0, c1) of front `node`, K
-// range [kk0, kk0 + K), appended as 8-int descriptors
-void add_tiles(std::vector<int32_t>& tl, int32_t node, int64_t r0, int64_t r1, int64_t c0,
-               int64_t c1, int64_t kk0, int64_t K) {
+// range [kk0, kk0 + K), appended with their A and B strips
+void add_tiles(TcPlan& pl, int32_t node, int64_t r0, int64_t r1, int64_t c0, int64_t c1,
+               int64_t kk0, int64_t K) {
   if (r1 <= r0 || c1 <= c0 || K <= 0) return;
   for (int64_t r = r0; r < r1; r += tc::BM)
     for (int64_t c = c0; c < c1; c += tc::BN) {
-      const int32_t v[8] = {node, (int32_t)r, (int32_t)c, (int32_t)std::min<int64_t>(tc::BM, r1 - r),
-                            (int32_t)std::min<int64_t>(tc::BN, c1 - c), (int32_t)kk0, (int32_t)K, 0};
-      tl.insert(tl.end(), v, v + 8);
+      const int64_t nr = std::min<int64_t>(tc::BM, r1 - r), nc = std::min<int64_t>(tc::BN, c1 - c);
+      const int32_t a = pl.strip(node, 0, r, nr, kk0, K), b = pl.strip(node, 1, c, nc, kk0, K);
+      const int32_t v[tc::TD] = {node, (int32_t)r, (int32_t)c, (int32_t)nr, (int32_t)nc, (int32_t)kk0,
+                                 (int32_t)K, a, b, 0, 0, 0};
+      pl.tiles.insert(pl.tiles.end(), v, v + tc::TD);
     }
 }
 
-cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s, double mac_flops, int cfg_sp, int cfg_pk) {
+// uploads a launch's tiles and strips: numbers the strips' K-chunk images
+// and points every tile at the first image of its A and its B strip
+cudaError_t upload_plan(TcPlan& pl, TcLaunch& t) {
+  std::vector<int32_t> chunk_strip;
+  const int32_t nstrips = (int32_t)(pl.strips.size() / 8);
+  for (int32_t i = 0; i < nstrips; ++i) {
+    pl.strips[8 * i + 5] = (int32_t)chunk_strip.size();
+    const int32_t nch = (pl.strips[8 * i + 4] + tc::KC - 1) / tc::KC;
+    chunk_strip.insert(chunk_strip.end(), nch, i);
+  }
+  t.ntiles = (int)(pl.tiles.size() / tc::TD);
+  for (int i = 0; i < t.ntiles; ++i) {
+    int32_t* td = &pl.tiles[(size_t)tc::TD * i];
+    td[7] = pl.strips[8 * td[7] + 5];
+    td[8] = pl.strips[8 * td[8] + 5];
+  }
+  t.nchunks = (int)chunk_strip.size();
+  cudaError_t e = upv(&t.d_tiles, pl.tiles);
+  if (e == cudaSuccess) e = upv(&t.d_strips, pl.strips);
+  if (e == cudaSuccess) e = upv(&t.d_chunk_strip, chunk_strip);
+  return e;
+}
+
+cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s, double mac_flops, size_t chunk_bytes,
+                    int cfg_sp, int cfg_pk) {
+  int max_chunks = 0;
   d.tc_sp = kTcSuperPanel;
   d.tc_panel_k = kTcPanelMinK;
   if (const char* v = getenv("SUCEM_LU_TC_PANEL_K")) d.tc_panel_k = atoi(v);
@@ -1062,18 +1121,18 @@ cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s, double mac_flops, int cfg_
       size_t b = a;
       TcLaunch t;
       t.p0 = ends[a].first;
-      std::vector<int32_t> tl;  // the tiles of every front, front by front
+      TcPlan pl;  // the tiles of every front, front by front
       for (; b < ends.size() && ends[b].first == t.p0; ++b) {
         const MFNode& nd = s.nodes[ends[b].second];
         const int64_t sp0 = (t.p0 / sp) * (int64_t)sp;
         const int64_t bnd = std::min<int64_t>(nd.k, sp0 + sp);
-        add_tiles(tl, ends[b].second, bnd, nd.f, bnd, nd.f, sp0, bnd - sp0);
+        add_tiles(pl, ends[b].second, bnd, nd.f, bnd, nd.f, sp0, bnd - sp0);
         t.flops += mac_flops * (double)(nd.f - bnd) * (double)(nd.f - bnd) * (double)(bnd - sp0);
       }
-      t.ntiles = (int)(tl.size() / 8);
-      cudaError_t e = upv(&t.d_tiles, tl);
+      cudaError_t e = upload_plan(pl, t);
+      L.tcl.push_back(t);  // registered before a failure so that free_dev releases it
       if (e != cudaSuccess) return e;
-      L.tcl.push_back(t);
+      max_chunks = std::max(max_chunks, t.nchunks);
       a = b;
     }
     // panel updates on the tensor cores
@@ -1081,24 +1140,26 @@ cudaError_t plan_tc(MFDevice& d, const MFSymbolic& s, double mac_flops, int cfg_
     for (int p0 = 0; p0 < L.max_k; p0 += kTcPanel) {
       TcLaunch t;
       t.p0 = p0;
-      std::vector<int32_t> tl;
+      TcPlan pl;
       for (int32_t i : L.nodes_by_k) {
         const MFNode& nd = s.nodes[i];
         if (nd.k <= p0) break;  // k-descending
         const int64_t nb = std::min<int64_t>(kTcPanel, nd.k - p0), lo = p0 + nb;
         const int64_t bnd = std::min<int64_t>(nd.k, (p0 / sp) * (int64_t)sp + sp);
         if (bnd <= lo) continue;
-        add_tiles(tl, i, lo, nd.f, lo, bnd, p0, nb);   // rows [lo, f) x cols [lo, bnd)
-        add_tiles(tl, i, lo, bnd, bnd, nd.f, p0, nb);  // rows [lo, bnd) x cols [bnd, f)
+        add_tiles(pl, i, lo, nd.f, lo, bnd, p0, nb);   // rows [lo, f) x cols [lo, bnd)
+        add_tiles(pl, i, lo, bnd, bnd, nd.f, p0, nb);  // rows [lo, bnd) x cols [bnd, f)
         t.flops += mac_flops * (double)nb *
                    ((double)(nd.f - lo) * (bnd - lo) + (double)(bnd - lo) * (nd.f - bnd));
       }
-      t.ntiles = (int)(tl.size() / 8);
-      cudaError_t e = upv(&t.d_tiles, tl);
-      if (e != cudaSuccess) return e;
+      cudaError_t e = upload_plan(pl, t);
       L.tcp.push_back(t);
+      if (e != cudaSuccess) return e;
+      max_chunks = std::max(max_chunks, t.nchunks);
     }
   }
+  // one image buffer serves every launch (launches are stream-ordered)
+  if (max_chunks > 0) return cudaMalloc((void**)&d.d_img, (size_t)max_chunks * chunk_bytes);
   return cudaSuccess;
 }
 
@@ -1159,9 +1220,9 @@ cudaError_t setup_device(MFHandle& h, int dtype) {
   if (e == cudaSuccess) e = cudaMalloc(&d.d_x, (size_t)std::max<int64_t>(s.n, 1) * d.elem);
   if (e == cudaSuccess) e = cudaMalloc((void**)&d.d_flag, 16);
   if (e == cudaSuccess && dtype == SUCEM_C64)
-    e = plan_tc(d, s, kMacFlops<float2>, h.cfg_superpanel, h.cfg_panel_k);
+    e = plan_tc(d, s, kMacFlops<float2>, tc::chunk_bytes<float2>(), h.cfg_superpanel, h.cfg_panel_k);
   if (e == cudaSuccess && dtype == SUCEM_F32)
-    e = plan_tc(d, s, kMacFlops<float>, h.cfg_superpanel, h.cfg_panel_k);
+    e = plan_tc(d, s, kMacFlops<float>, tc::chunk_bytes<float>(), h.cfg_superpanel, h.cfg_panel_k);
   if (e != cudaSuccess) free_dev(d);
   return e;
 }
@@ -1184,16 +1245,19 @@ cudaError_t tc_launch(MFDevice& d, const TcLaunch& t, S* arena, cudaStream_t st)
   if constexpr (!kTensorCore<S>) {
     return cudaErrorInvalidValue;  // double precision has no tensor-core plan
   } else {
+    if (t.ntiles == 0) return cudaSuccess;
     const int grid = std::max(1, std::min(t.ntiles, d.sm_count));
     cudaError_t e = tc_event(d, d.tc_n, 0, st);
     if (e != cudaSuccess) return e;
+    tc_presplit_kernel<S><<<t.nchunks, 256, 0, st>>>(t.d_strips, t.d_chunk_strip, d.d_nodes, arena,
+                                                      d.d_img);
     tc_update_kernel<S><<<grid, tc::THREADS, tc::smem_bytes<S>(), st>>>(
-        t.d_tiles, t.ntiles, d.d_nodes, arena, d.d_flag + 1);
+        t.d_tiles, t.ntiles, d.d_nodes, arena, d.d_img, d.d_flag + 1);
     e = tc_event(d, d.tc_n, 1, st);
     if (e != cudaSuccess) return e;
     d.tc_n++;
     d.tc_flops += t.flops;
-    count_launch(1);
+    count_launch(2);
     return cudaSuccess;
   }
 }

@@ -21,17 +21,20 @@
 // in two accumulators, the -Im*Im terms through the instruction's
 // A-negation bit.
 //
+// Operands are split once per launch by tc_presplit_kernel: every strip of
+// A (128 rows x K) and of B (K x 128 columns) that the launch's tiles use
+// is written, K-chunk by K-chunk (16), as the exact shared-memory image the
+// MMAs read: the K-major operand planes (real: hi/lo; complex: Re/Im x
+// hi/lo) in the canonical no-swizzle core-matrix layout (8 rows x 16 bytes
+// per core matrix, 128 bytes apart along K, 512 bytes apart along M/N).
+//
 // Structure: a persistent, warp-specialised kernel, one CTA per SM walking
 // the tile list round-robin.
-//   warps 4-11 (producers): load a K-chunk of 16 (A: 128 rows, B: 128
-//     columns; two quarter rows and half a column per thread, loads
-//     coalesced along the rows of the front, two chunks ahead through two
-//     register buffers), split it and store the K-major operand planes
-//     (real: hi/lo of A and B; complex: Re/Im x hi/lo) in the canonical
-//     no-swizzle core-matrix layout (8 rows x 16 bytes per core matrix, 128
-//     bytes apart along K, 512 bytes apart along M/N) into one of three
-//     stages, then arrive on the stage's "full" barrier;
-//   warp 12, one thread (MMA issuer): per chunk, waits for "full", issues
+//   warp 4, one thread (producer): per K-chunk of a tile, waits for the
+//     stage's "empty" barrier, announces the stage's bytes on its "full"
+//     barrier and issues two bulk asynchronous copies (the A and the B
+//     chunk image, cp.async.bulk) that complete on "full";
+//   warp 5, one thread (MMA issuer): per chunk, waits for "full", issues
 //     the chunk's MMAs into the tile's TMEM accumulator(s) and commits them
 //     to the stage's "empty" barrier (the producers' permission to refill
 //     it); after a tile's last chunk it commits to the accumulator's
@@ -50,9 +53,10 @@ constexpr int BM = 128;                        // tile rows (TMEM lanes)
 constexpr int BN = 128;                        // tile columns
 constexpr int KC = 16;                         // K per chunk
 constexpr int STAGES = 3;
-constexpr int THREADS = 416;                   // 4 epilogue + 8 producer warps + 1 MMA warp
-constexpr int PRODUCERS = 256;
-constexpr int MMA_WARP = 12;
+constexpr int THREADS = 192;                   // 4 epilogue warps, 1 producer warp, 1 MMA warp
+constexpr int PRODUCER_WARP = 4;
+constexpr int MMA_WARP = 5;
+constexpr int TD = 12;                         // ints per tile descriptor
 constexpr int PLANE = BM * KC * 4;             // bytes of one operand plane (BN == BM)
 constexpr int EPI_BYTES = 4 * 32 * 17 * 8;     // per epilogue warp: 32 rows x 16 (+1) values
 constexpr int kWaitLimit = 1 << 24;            // polls of one mbarrier before giving up
@@ -72,7 +76,9 @@ struct Cfg<float> {
   static constexpr int NACC = 1;
 };
 template <typename S>
-__host__ __device__ constexpr int stage_bytes() { return 2 * Cfg<S>::NP * PLANE; }  // A planes, then B planes
+__host__ __device__ constexpr int chunk_bytes() { return Cfg<S>::NP * PLANE; }  // one operand's K-chunk image
+template <typename S>
+__host__ __device__ constexpr int stage_bytes() { return 2 * chunk_bytes<S>(); }  // A planes, then B planes
 template <typename S>
 __host__ __device__ constexpr int smem_bytes() { return STAGES * stage_bytes<S>() + EPI_BYTES + 512; }
 template <typename S>
@@ -118,6 +124,23 @@ __device__ __forceinline__ void commit(uint32_t bar) {
 
 __device__ __forceinline__ void arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar));
+}
+
+// arrive on `bar` and add `bytes` to the transaction count its phase waits for
+__device__ __forceinline__ void arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+// bulk asynchronous copy global -> shared (16-byte aligned, size a multiple
+// of 16), completing `bytes` transactions on `bar`
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes,
+                                          uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
 }
 
 // bounded wait for the phase with the given parity; with backoff, a failed
@@ -186,8 +209,8 @@ struct Tile {
   int row0, nrow, col0, ncol, kk0, K;
 };
 
-// a tile from its descriptor: 8 ints {front node, row0, col0, nrow, ncol,
-// kk0, K, unused}
+// a tile from its descriptor: TD ints {front node, row0, col0, nrow, ncol,
+// kk0, K, first chunk image of its A strip, of its B strip, 0, 0, 0}
 __device__ __forceinline__ Tile tile_of(const int32_t* td) {
   Tile t;
   t.row0 = td[1];
@@ -201,16 +224,55 @@ __device__ __forceinline__ Tile tile_of(const int32_t* td) {
 
 }  // namespace tc
 
-// the listed tiles (8-int descriptors, see tile_of), each CTA taking tiles
-// blockIdx.x, blockIdx.x + gridDim.x, ...; S = float or float2
+// One block per K-chunk image of a launch: strip descriptors of 8 ints
+// {front node, first row (A) or column (B), rows/columns in use (<= 128),
+// kk0, K, first chunk image, side (0: A rows, 1: B columns), 0} and the
+// strip of every chunk image.  Values outside the strip (rows past n, K
+// past the range) are zero.
+template <typename S>
+__global__ void __launch_bounds__(256)
+    tc_presplit_kernel(const int32_t* __restrict__ strips, const int32_t* __restrict__ chunk_strip,
+                       const DNode* __restrict__ nodes, const S* __restrict__ arena,
+                       uint8_t* __restrict__ img) {
+  using namespace tc;
+  const int32_t* sd = strips + 8 * __ldg(&chunk_strip[blockIdx.x]);
+  const DNode nd = nodes[sd[0]];
+  const int r0 = sd[1], n = sd[2], kk0 = sd[3], K = sd[4], side = sd[6];
+  const int c = (int)blockIdx.x - sd[5];
+  const S* F = arena + nd.off;
+  uint8_t* dst = img + (int64_t)blockIdx.x * chunk_bytes<S>();
+  S zero;
+  if constexpr (std::is_same<S, float2>::value) zero = make_float2(0.f, 0.f); else zero = 0.f;
+  for (int it = threadIdx.x; it < BM * (KC / 4); it += blockDim.x) {
+    // A: four threads per row (consecutive K groups, 128 contiguous bytes);
+    // B: consecutive threads on consecutive columns
+    const int r = side == 0 ? it >> 2 : it & (BM - 1);
+    const int kg = side == 0 ? it & 3 : it >> 7;
+    S v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int k = c * KC + 4 * kg + j;
+      if (r < n && k < K)
+        v[j] = side == 0 ? F[(int64_t)(r0 + r) * nd.f + kk0 + k] : F[(int64_t)(kk0 + k) * nd.f + r0 + r];
+      else
+        v[j] = zero;
+    }
+    store_split(dst, core_off(r, kg), v);
+  }
+}
+
+// the listed tiles (TD-int descriptors, see tile_of), each CTA taking tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ...; S = float or float2; img: the
+// launch's chunk images (tc_presplit_kernel)
 template <typename S>
 __global__ void __launch_bounds__(tc::THREADS, 1)
     tc_update_kernel(const int32_t* __restrict__ tiles, int ntiles,
                      const DNode* __restrict__ nodes, S* __restrict__ arena,
-                     int* __restrict__ err) {
+                     const uint8_t* __restrict__ img, int* __restrict__ err) {
   using namespace tc;
   constexpr bool CPLX = std::is_same<S, float2>::value;
-  constexpr int NP = Cfg<S>::NP, SB = stage_bytes<S>(), ACC = acc_cols<S>(), TM = tmem_cols<S>();
+  constexpr int NP = Cfg<S>::NP, SB = stage_bytes<S>(), CB = chunk_bytes<S>(), ACC = acc_cols<S>(),
+                TM = tmem_cols<S>();
   extern __shared__ __align__(128) uint8_t tc_smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(tc_smem_raw) + 127) & ~(uintptr_t)127);
@@ -226,8 +288,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
     for (int s = 0; s < STAGES; ++s) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&full[s])),
-                   "r"(PRODUCERS));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full[s])));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&empty[s])));
     }
     for (int b = 0; b < 2; ++b) {
@@ -253,68 +314,38 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
     atomicExch(err, 1);
   };
 
-  if (warp >= 4 && warp < MMA_WARP) {
-    // ---- producers: thread p stages K-group akg (four consecutive K) of
-    // A rows ar and ar + 64 (a warp's loads cover eight rows), and half h
-    // (K 8*h .. 8*h+7) of B column q (a warp's loads are 32 consecutive
-    // columns of one row) ----
-    const int p = tid - 128, q = p % 128, h = p / 128;
-    // lanes 8a .. 8a+7 of a warp take K-group a of eight consecutive rows,
-    // so each quarter-warp's 16-byte stores fill 128 contiguous bytes
-    const int ar = 8 * (p >> 5) + (p & 7), akg = (p >> 3) & 3;
-    S zero;
-    if constexpr (CPLX) zero = make_float2(0.f, 0.f); else zero = 0.f;
-    S av0[8], bv0[8], av1[8], bv1[8];
-    int g = 0;  // chunk counter over all tiles of this CTA
-    bool ok = true;
-    for (int it = blockIdx.x; it < ntiles && ok; it += gridDim.x) {
-      const DNode nd = nodes[tiles[8 * it]];
-      const Tile tl = tile_of(tiles + 8 * it);
-      const S* F = arena + nd.off;
-      const bool arow0 = ar < tl.nrow, arow1 = ar + 64 < tl.nrow, bcol = q < tl.ncol;
-      const S* Arow0 = F + (int64_t)(tl.row0 + (arow0 ? ar : 0)) * nd.f + tl.kk0 + 4 * akg;
-      const S* Arow1 = F + (int64_t)(tl.row0 + (arow1 ? ar + 64 : 0)) * nd.f + tl.kk0 + 4 * akg;
-      const S* Bcol = F + (int64_t)tl.kk0 * nd.f + tl.col0 + (bcol ? q : 0);
-      const int nch = (tl.K + KC - 1) / KC;
-      auto load = [&](S* a, S* b, int c) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int k = c * KC + 4 * akg + j;
-          a[j] = (arow0 && k < tl.K) ? Arow0[c * KC + j] : zero;
-          a[4 + j] = (arow1 && k < tl.K) ? Arow1[c * KC + j] : zero;
+  if (warp == PRODUCER_WARP) {
+    // ---- producer: one thread fills each stage with two bulk copies ----
+    if (lane == 0) {
+      int g = 0;  // chunk counter over all tiles of this CTA
+      bool ok = true;
+      for (int it = blockIdx.x; it < ntiles && ok; it += gridDim.x) {
+        const int32_t* td = tiles + TD * it;
+        const int nch = (td[6] + KC - 1) / KC;
+        const uint8_t* ia = img + (int64_t)td[7] * CB;
+        const uint8_t* ib = img + (int64_t)td[8] * CB;
+        for (int c = 0; c < nch; ++c, ++g) {
+          const int s = g % STAGES;
+          if (*fail || (g >= STAGES && !wait_parity(smem_u32(&empty[s]), ((g / STAGES) - 1) & 1))) {
+            ok = false;
+            break;
+          }
+          const uint32_t st = smem_u32(smem + s * SB), fb = smem_u32(&full[s]);
+          arrive_expect_tx(fb, 2 * CB);
+          bulk_copy(st, ia + (int64_t)c * CB, CB, fb);
+          bulk_copy(st + CB, ib + (int64_t)c * CB, CB, fb);
         }
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int k = c * KC + 8 * h + j;
-          b[j] = (bcol && k < tl.K) ? Bcol[(int64_t)k * nd.f] : zero;
-        }
-      };
-      // store a chunk's half into its stage, then reuse the registers for
-      // the chunk two ahead
-      auto stage = [&](S* a, S* b, int c) -> bool {
-        const int s = g % STAGES;
-        if (g >= STAGES && !wait_parity(smem_u32(&empty[s]), ((g / STAGES) - 1) & 1)) return false;
-        uint8_t* st = smem + s * SB;
-        store_split(st, core_off(ar, akg), a);
-        store_split(st, core_off(ar + 64, akg), a + 4);
-#pragma unroll
-        for (int kg = 0; kg < 2; ++kg)
-          store_split(st + NP * PLANE, core_off(q, 2 * h + kg), b + 4 * kg);
-        asm volatile("fence.proxy.async.shared::cta;");
-        arrive(smem_u32(&full[s]));
-        ++g;
-        if (c + 2 < nch) load(a, b, c + 2);
-        return true;
-      };
-      if (nch > 0) load(av0, bv0, 0);
-      if (nch > 1) load(av1, bv1, 1);
-      for (int c = 0; c < nch && ok; c += 2) {
-        ok = stage(av0, bv0, c);
-        if (ok && c + 1 < nch) ok = stage(av1, bv1, c + 1);
+        if (*fail) ok = false;
       }
-      if (!ok) raise();
-      if (*fail) ok = false;
+      if (!ok) {
+        raise();
+        // giving up: let the copies this thread issued land before the
+        // shared memory is released (bounded waits on their stages)
+        for (int q = g - STAGES; q < g; ++q)
+          if (q >= 0) wait_parity(smem_u32(&full[q % STAGES]), (q / STAGES) & 1);
+      }
     }
+    __syncwarp();
   } else if (warp == MMA_WARP) {
     // ---- MMA issuer ----
     if (lane == 0) {
@@ -322,7 +353,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
       bool ok = true;
       const uint32_t pos = idesc(false), neg = idesc(true);
       for (int it = blockIdx.x; it < ntiles && ok; it += gridDim.x, ++i) {
-        const Tile tl = tile_of(tiles + 8 * it);
+        const Tile tl = tile_of(tiles + TD * it);
         const int nch = (tl.K + KC - 1) / KC;
         const int b = i & 1;
         if (i >= 2 && !wait_parity(smem_u32(&acc_empty[b]), ((i / 2) - 1) & 1)) {
@@ -391,8 +422,8 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
     // ---- epilogue: warp w reads TMEM lanes 32w .. 32w + 31 (tile rows) ----
     int i = 0;
     for (int it = blockIdx.x; it < ntiles; it += gridDim.x, ++i) {
-      const DNode nd = nodes[tiles[8 * it]];
-      const Tile tl = tile_of(tiles + 8 * it);
+      const DNode nd = nodes[tiles[TD * it]];
+      const Tile tl = tile_of(tiles + TD * it);
       const int b = i & 1;
       S* buf = epi + warp * 32 * 17;  // [32 rows][17]
       S* Cw = arena + nd.off + (int64_t)(tl.row0 + warp * 32) * nd.f + tl.col0;
