@@ -5,6 +5,7 @@ links a shared library next to this file: sucem-fem_gb300/libsucem_gb300.so.
 """
 import concurrent.futures as cf
 import os
+import platform
 import subprocess
 import sys
 
@@ -12,7 +13,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "libsucem_gb300.so")
-BUILD = os.path.join(HERE, "_build")
+# objects per host architecture: a tree copied to another machine never links them
+BUILD = os.path.join(HERE, "_build", platform.machine() or "host")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 
@@ -31,6 +33,19 @@ def _run(cmd):
     if r.returncode != 0:
         raise RuntimeError("build failed: %s\n%s" % (" ".join(cmd), r.stdout))
     return r.stdout
+
+
+def _local_deps(path, seen=None):
+    """The file and the local headers it includes (recursively)."""
+    import re
+    seen = set() if seen is None else seen
+    if path in seen or not os.path.exists(path):
+        return seen
+    seen.add(path)
+    with open(path, errors="replace") as f:
+        for m in re.finditer(r'^\s*#\s*include\s+"([^"]+)"', f.read(), re.M):
+            _local_deps(os.path.normpath(os.path.join(os.path.dirname(path), m.group(1))), seen)
+    return seen
 
 
 def build(verbose=False, force=False):
@@ -53,12 +68,15 @@ def build(verbose=False, force=False):
     for s in srcs:
         obj = os.path.join(BUILD, os.path.basename(s) + ".o")
         objs.append(obj)
+        if (not force and os.path.exists(obj) and
+                os.path.getmtime(obj) >= max(os.path.getmtime(p) for p in _local_deps(s))):
+            continue  # object newer than its source and the headers it includes
         if s.endswith(".cu"):
             cmd = [NVCC] + ARCH + common + ["-lineinfo", "-c", s, "-o", obj]
         else:
             cmd = [NVCC] + common + ["-x", "cu", "-c", s, "-o", obj] + ARCH
         jobs.append(cmd)
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(8, len(jobs)))) as ex:
         outs = list(ex.map(_run, jobs))
     if verbose:
         for o in outs:
