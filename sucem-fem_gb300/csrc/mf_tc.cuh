@@ -30,18 +30,19 @@
 //
 // Structure: a persistent, warp-specialised kernel, one CTA per SM walking
 // the tile list round-robin.
-//   warp 4, one thread (producer): per K-chunk of a tile, waits for the
+//   warp 8, one thread (producer): per K-chunk of a tile, waits for the
 //     stage's "empty" barrier, announces the stage's bytes on its "full"
 //     barrier and issues two bulk asynchronous copies (the A and the B
 //     chunk image, cp.async.bulk) that complete on "full";
-//   warp 5, one thread (MMA issuer): per chunk, waits for "full", issues
+//   warp 9, one thread (MMA issuer): per chunk, waits for "full", issues
 //     the chunk's MMAs into the tile's TMEM accumulator(s) and commits them
 //     to the stage's "empty" barrier (the producers' permission to refill
 //     it); after a tile's last chunk it commits to the accumulator's
 //     "acc_full" barrier;
-//   warps 0-3 (epilogue): request the tile's first 16 columns of C, wait
-//     for "acc_full", read their 32 TMEM lanes (tile rows) 16 columns at a
-//     time (each block's C requested before its TMEM reads), turn them
+//   warps 0-7 (epilogue, two per TMEM lane quarter, one per column half):
+//     request the first 16 columns of their C block, wait for "acc_full",
+//     read their 32 TMEM lanes (tile rows) 16 columns at a time (each
+//     block's C requested before its TMEM reads), turn them
 //     through shared memory so that a warp's accesses to C cover two rows of
 //     16 consecutive columns, apply C -= D and arrive on "acc_empty".
 // Two accumulator sets let the epilogue of one tile run under the main
@@ -53,12 +54,13 @@ constexpr int BM = 128;                        // tile rows (TMEM lanes)
 constexpr int BN = 128;                        // tile columns
 constexpr int KC = 16;                         // K per chunk
 constexpr int STAGES = 3;
-constexpr int THREADS = 192;                   // 4 epilogue warps, 1 producer warp, 1 MMA warp
-constexpr int PRODUCER_WARP = 4;
-constexpr int MMA_WARP = 5;
+constexpr int EPI_WARPS = 8;                   // two per TMEM lane quarter (column halves)
+constexpr int THREADS = 32 * (EPI_WARPS + 2);  // epilogue warps, 1 producer warp, 1 MMA warp
+constexpr int PRODUCER_WARP = EPI_WARPS;
+constexpr int MMA_WARP = EPI_WARPS + 1;
 constexpr int TD = 12;                         // ints per tile descriptor
 constexpr int PLANE = BM * KC * 4;             // bytes of one operand plane (BN == BM)
-constexpr int EPI_BYTES = 4 * 32 * 17 * 8;     // per epilogue warp: 32 rows x 16 (+1) values
+constexpr int EPI_BYTES = EPI_WARPS * 32 * 17 * 8;  // per epilogue warp: 32 rows x 16 (+1) values
 constexpr int kWaitLimit = 1 << 24;            // polls of one mbarrier before giving up
 static_assert(BN == BM, "planes share one size");
 
@@ -293,7 +295,8 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
     }
     for (int b = 0; b < 2; ++b) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&acc_full[b])));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(smem_u32(&acc_empty[b])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&acc_empty[b])),
+                   "r"(32 * EPI_WARPS));
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(drain)));
     *fail = 0;
@@ -419,14 +422,17 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
     }
     __syncwarp();
   } else {
-    // ---- epilogue: warp w reads TMEM lanes 32w .. 32w + 31 (tile rows) ----
+    // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (tile rows),
+    // columns of half w / 4 ----
     int i = 0;
     for (int it = blockIdx.x; it < ntiles; it += gridDim.x, ++i) {
       const DNode nd = nodes[tiles[TD * it]];
       const Tile tl = tile_of(tiles + TD * it);
       const int b = i & 1;
       S* buf = epi + warp * 32 * 17;  // [32 rows][17]
-      S* Cw = arena + nd.off + (int64_t)(tl.row0 + warp * 32) * nd.f + tl.col0;
+      // TMEM lanes (tile rows) 32 q .. 32 q + 31, columns [64 h, 64 h + 64)
+      const int q = warp & 3, h = warp >> 2;
+      S* Cw = arena + nd.off + (int64_t)(tl.row0 + q * 32) * nd.f + tl.col0;
       // C of each 16-column block is requested before that block's TMEM
       // reads (the first one before the accumulator is ready): C is not
       // touched by the tile's main loop, so its load latency overlaps them
@@ -435,7 +441,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
 #pragma unroll
         for (int t = 0; t < 16; ++t) {
           const int r = 2 * t + (lane >> 4), col = cc * 16 + (lane & 15);
-          if (warp * 32 + r < tl.nrow && col < tl.ncol)
+          if (q * 32 + r < tl.nrow && col < tl.ncol)
             cv[t] = Cw[(int64_t)r * nd.f + col];
           else if constexpr (CPLX)
             cv[t] = make_float2(0.f, 0.f);
@@ -443,7 +449,8 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
             cv[t] = 0.f;
         }
       };
-      load_c(0);
+      const int cc0 = h * (BN / 32);
+      load_c(cc0);
       // uniform per warp: the TMEM loads below are warp-collective
       const bool got =
           __all_sync(~0u, wait_parity(smem_u32(&acc_full[b]), (i / 2) & 1, true));
@@ -452,10 +459,10 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t tre = tmem + b * ACC + ((uint32_t)(warp * 32) << 16);
+      const uint32_t tre = tmem + b * ACC + ((uint32_t)(q * 32) << 16);
 #pragma unroll 1
-      for (int cc = 0; cc < BN / 16; ++cc) {
-        if (cc > 0) load_c(cc);
+      for (int cc = cc0; cc < cc0 + BN / 32; ++cc) {
+        if (cc > cc0) load_c(cc);
         uint32_t re[16], im[16];
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -483,7 +490,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
 #pragma unroll
         for (int t = 0; t < 16; ++t) {
           const int r = 2 * t + (lane >> 4), col = cc * 16 + (lane & 15);
-          if (warp * 32 + r < tl.nrow && col < tl.ncol) {
+          if (q * 32 + r < tl.nrow && col < tl.ncol) {
             const S dv = buf[r * 17 + (lane & 15)];
             if constexpr (CPLX)
               Cw[(int64_t)r * nd.f + col] = make_float2(cv[t].x - dv.x, cv[t].y - dv.y);
