@@ -711,9 +711,11 @@ __device__ __forceinline__ void fwd_trsv_front(const DNode& nd, const S* __restr
 
 // forward, sub-step j, row q of the rows [c1, f) of the front outside the
 // sub-panel (one warp): row r takes -= L[r, c0:c1] . y[c0:c1]; rows inside
-// the pivot block update y (one writer), rows of the update set go to the
-// ancestors' x[U[r - k]] (atomic, sibling fronts share ancestors)
-template <typename S>
+// the pivot block update y (one writer, or atomically when ATOM: the
+// look-ahead schedule runs two launches on the same rows concurrently),
+// rows of the update set go to the ancestors' x[U[r - k]] (atomic, sibling
+// fronts share ancestors)
+template <typename S, bool ATOM>
 __device__ __forceinline__ void fwd_gemv_row(const DNode& nd, const int32_t* __restrict__ U,
                                              const S* __restrict__ arena, S* __restrict__ x,
                                              int c0, int c1, int q, int lane) {
@@ -722,25 +724,30 @@ __device__ __forceinline__ void fwd_gemv_row(const DNode& nd, const int32_t* __r
   const S* row = arena + nd.off + (int64_t)r * nd.f;
   const S acc = warp_row_dot<S, false>(row, y, nullptr, c0, c1, lane);
   if (lane == 0) {
-    if (r < nd.k)
+    if (r < nd.k && !ATOM)
       y[r] = s_add(y[r], acc);
+    else if (r < nd.k)
+      s_atomic_sub(&y[r], s_fms(s_zero(S()), acc, s_real(S(), 1.0)));
     else
       s_atomic_sub(&x[U[nd.u_off + r - nd.k]], s_fms(s_zero(S()), acc, s_real(S(), 1.0)));
   }
 }
 
 // backward, sub-step j, work item w of rows [c0, c1) x chunks of kBwdChunk
-// columns outside the sub-panel (one warp): row r takes -= U[r, c1:f] . x
-// over its chunk (own variables y[c] for c < k, the ancestors' x[U[c - k]]
-// beyond); with several chunks the partial sums are added atomically
-template <typename S>
+// of the columns [cb, ce) outside the sub-panel (one warp): row r takes
+// -= U[r, cb:ce] . x over its chunk (own variables y[c] for c < k, the
+// ancestors' x[U[c - k]] beyond); with several chunks (or ATOM: another
+// launch adds to the same rows concurrently) the partial sums are added
+// atomically
+template <typename S, bool ATOM>
 __device__ __forceinline__ void bwd_gemv_item(const DNode& nd, const int32_t* __restrict__ U,
                                               const S* __restrict__ arena, S* __restrict__ x,
-                                              int c0, int c1, int nch, int w, int lane) {
+                                              int c0, int c1, int cb, int ce, int nch, int w,
+                                              int lane) {
   S* y = x + nd.start;
   const int rows = c1 - c0;
   const int r = c0 + w % rows, ch = w / rows;
-  const int lo = c1 + ch * kBwdChunk, hi = min(nd.f, lo + kBwdChunk);
+  const int lo = cb + ch * kBwdChunk, hi = min(ce, lo + kBwdChunk);
   const S* row = arena + nd.off + (int64_t)r * nd.f;
   S acc = s_zero(S());
   if (lo < nd.k) acc = warp_row_dot<S, false>(row, y, nullptr, lo, min(hi, nd.k), lane);
@@ -748,7 +755,7 @@ __device__ __forceinline__ void bwd_gemv_item(const DNode& nd, const int32_t* __
     acc = s_add(acc, warp_row_dot<S, true>(row + nd.k, x, U + nd.u_off, max(lo, nd.k) - nd.k,
                                            hi - nd.k, lane));
   if (lane == 0) {
-    if (nch == 1)
+    if (nch == 1 && !ATOM)
       y[r] = s_add(y[r], acc);
     else
       s_atomic_sub(&y[r], s_fms(s_zero(S()), acc, s_real(S(), 1.0)));
@@ -821,11 +828,13 @@ __global__ void __launch_bounds__(1024) fwd_trsv_kernel(const int32_t* __restric
   fwd_trsv_front<S>(nodes[list[blockIdx.x]], arena, x, j, trsv_smem);
 }
 
-// a warp per row of the listed front blockIdx.y
-template <typename S>
+// a warp per row of the listed front blockIdx.y, rows [c1 + q_lo, c1 + q_hi)
+// of the rows [c1, f) outside the sub-panel
+template <typename S, bool ATOM>
 __global__ void fwd_gemv_kernel(const int32_t* __restrict__ list, int count,
                                 const DNode* __restrict__ nodes, const int32_t* __restrict__ U,
-                                const S* __restrict__ arena, S* __restrict__ x, int j) {
+                                const S* __restrict__ arena, S* __restrict__ x, int j, int q_lo,
+                                int q_hi) {
   constexpr int P = solve_panel<S>();
   const int fi = blockIdx.y;
   if (fi >= count) return;
@@ -833,17 +842,21 @@ __global__ void fwd_gemv_kernel(const int32_t* __restrict__ list, int count,
   const int c0 = j * P;
   if (nd.k <= c0) return;
   const int c1 = min(nd.k, c0 + P);
-  const int rows = nd.f - c1;
+  const int rows = min(nd.f - c1, q_hi);
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int q = warp; q < rows; q += nwarps) fwd_gemv_row<S>(nd, U, arena, x, c0, c1, q, lane);
+  for (int q = q_lo + warp; q < rows; q += nwarps)
+    fwd_gemv_row<S, ATOM>(nd, U, arena, x, c0, c1, q, lane);
 }
 
-// a warp per (row, kBwdChunk columns) of the listed front blockIdx.y
-template <typename S>
+// a warp per (row, kBwdChunk columns) of the listed front blockIdx.y, the
+// columns [c1 + col_lo, c1 + col_hi) of the columns [c1, f) outside the
+// sub-panel
+template <typename S, bool ATOM>
 __global__ void bwd_gemv_kernel(const int32_t* __restrict__ list, int count,
                                 const DNode* __restrict__ nodes, const int32_t* __restrict__ U,
-                                const S* __restrict__ arena, S* __restrict__ x, int j) {
+                                const S* __restrict__ arena, S* __restrict__ x, int j, int col_lo,
+                                int col_hi) {
   constexpr int P = solve_panel<S>();
   const int fi = blockIdx.y;
   if (fi >= count) return;
@@ -851,13 +864,14 @@ __global__ void bwd_gemv_kernel(const int32_t* __restrict__ list, int count,
   const int c0 = j * P;
   if (nd.k <= c0) return;
   const int c1 = min(nd.k, c0 + P);
-  if (c1 >= nd.f) return;
-  const int rows = c1 - c0, ncol = nd.f - c1;
+  const int cb = c1 + col_lo, ce = c1 + min(nd.f - c1, col_hi);
+  if (cb >= ce) return;
+  const int rows = c1 - c0, ncol = ce - cb;
   const int nch = (ncol + kBwdChunk - 1) / kBwdChunk;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int w = warp; w < rows * nch; w += nwarps)
-    bwd_gemv_item<S>(nd, U, arena, x, c0, c1, nch, w, lane);
+    bwd_gemv_item<S, ATOM>(nd, U, arena, x, c0, c1, cb, ce, nch, w, lane);
 }
 
 template <typename S>
@@ -936,6 +950,8 @@ struct MFDevice {
   void* d_x = nullptr;              // solve work vector (new ordering)
   int* d_flag = nullptr;            // perturbed pivot count
   cudaStream_t cap_stream = nullptr;  // private stream for capturing the solve graph
+  cudaStream_t cap_side = nullptr;    // its look-ahead side stream (see solve_launches)
+  std::vector<cudaEvent_t> solve_ev;  // fork/join events of the solve capture
   std::vector<cudaEvent_t> tc_ev;   // start/stop events around tensor-core launches
   int tc_n = 0;                     // tensor-core launches in the last factorisation
   double tc_flops = 0;              // their algorithmic flops (8 per complex MAC)
@@ -1007,6 +1023,8 @@ void free_dev(MFDevice& d) {
   if (d.solve_exec) cudaGraphExecDestroy(d.solve_exec);
   for (cudaEvent_t ev : d.tc_ev) cudaEventDestroy(ev);
   if (d.cap_stream) cudaStreamDestroy(d.cap_stream);
+  if (d.cap_side) cudaStreamDestroy(d.cap_side);
+  for (cudaEvent_t ev : d.solve_ev) cudaEventDestroy(ev);
   if (d.factor_ev) cudaEventDestroy(d.factor_ev);
   d = MFDevice();
 }
@@ -1447,40 +1465,129 @@ cudaError_t solve_prepare() {
   return e;
 }
 
-// the launches of one solve on the work vector d_x; returns their count
+// The launches of one solve on the work vector d_x (captured into a graph);
+// returns their count, or -1 when an event or stream call failed.
+//
+// Levels of three or more sub-steps (the few large fronts at the top of the
+// tree, whose sub-steps form the solve's critical path) take a look-ahead
+// schedule over two streams: each sub-step's products are split into the
+// part the next sub-step's triangular solve needs (the next 128 rows
+// forward, the just-solved 128 columns backward), kept on the main stream
+// between the triangular solves, and the rest, issued on a side stream
+// that runs beside the next sub-step (forward: rows beyond the next
+// sub-panel; backward: columns solved two sub-steps earlier).  The two
+// launches that add to the same rows concurrently do so atomically.
+// SUCEM_LU_SOLVE_SEQUENTIAL keeps one stream throughout.
 template <typename S>
 int solve_launches(MFDevice& d, cudaStream_t st) {
   constexpr int P = solve_panel<S>();
   const size_t smem = sizeof(S) * (size_t)P * (P + 2);
   S* x = (S*)d.d_x;
   const S* arena = (const S*)d.arena;
+  const bool look = !getenv("SUCEM_LU_SOLVE_SEQUENTIAL");
+  cudaStream_t side = d.cap_side;
   int n = 0;
-  for (size_t lv = 0; lv < d.levels.size(); ++lv) {
+  // events of one level, reused level after level (a wait captures the
+  // event's node at the time of the call)
+  int evi = 0;
+  bool ok = true;
+  auto ev = [&]() -> cudaEvent_t {
+    while ((int)d.solve_ev.size() <= evi) {
+      cudaEvent_t e;
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+        ok = false;
+        return nullptr;
+      }
+      d.solve_ev.push_back(e);
+    }
+    return d.solve_ev[evi++];
+  };
+  auto record = [&](cudaEvent_t e, cudaStream_t s) { ok = ok && e && cudaEventRecord(e, s) == cudaSuccess; };
+  auto wait = [&](cudaStream_t s, cudaEvent_t e) { ok = ok && e && cudaStreamWaitEvent(s, e, 0) == cudaSuccess; };
+  const int kAll = 1 << 30;
+  for (size_t lv = 0; lv < d.levels.size() && ok; ++lv) {
     const MFLevel& L = d.levels[lv];
     const int cnt = (int)L.nodes_by_k.size();
     const int nsub = (L.max_k + P - 1) / P;
-    for (int j = 0; j < nsub; ++j) {
+    if (!look || nsub < 3 || !side) {
+      for (int j = 0; j < nsub; ++j) {
+        fwd_trsv_kernel<S><<<cnt, kTrsvThreads, smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x, j);
+        const int rows = L.max_rest - std::min(L.max_k, j * P + 1);
+        dim3 g(std::max(1, std::min(512, (rows + 7) / 8)), cnt);
+        fwd_gemv_kernel<S, false><<<g, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
+                                                      j, 0, kAll);
+        n += 2;
+      }
+      continue;
+    }
+    evi = 0;
+    std::vector<cudaEvent_t> done_rest(nsub, nullptr);
+    for (int j = 0; j < nsub && ok; ++j) {
+      if (j >= 2) wait(st, done_rest[j - 2]);
       fwd_trsv_kernel<S><<<cnt, kTrsvThreads, smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x, j);
-      const int rows = L.max_rest - std::min(L.max_k, j * P + 1);
-      dim3 g(std::max(1, std::min(512, (rows + 7) / 8)), cnt);
-      fwd_gemv_kernel<S><<<g, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x, j);
-      n += 2;
+      cudaEvent_t solved = ev();
+      record(solved, st);
+      // the next sub-panel's rows, then the rest beside the next sub-step
+      fwd_gemv_kernel<S, true><<<dim3(P / 8, cnt), 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U,
+                                                                 arena, x, j, 0, P);
+      const int rows = L.max_rest - std::min(L.max_k, j * P + 1) - P;
+      wait(side, solved);
+      if (rows > 0) {
+        dim3 g(std::max(1, std::min(512, (rows + 7) / 8)), cnt);
+        fwd_gemv_kernel<S, true><<<g, 256, 0, side>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
+                                                      j, P, kAll);
+      }
+      done_rest[j] = ev();
+      record(done_rest[j], side);
+      n += 3;
     }
+    wait(st, done_rest[nsub - 1]);  // the side stream's launches are ordered
   }
-  for (int lv = (int)d.levels.size() - 1; lv >= 0; --lv) {
+  for (int lv = (int)d.levels.size() - 1; lv >= 0 && ok; --lv) {
     const MFLevel& L = d.levels[lv];
     const int cnt = (int)L.nodes_by_k.size();
     const int nsub = (L.max_k + P - 1) / P;
-    for (int j = nsub - 1; j >= 0; --j) {
-      const int rows = std::min(P, L.max_k);
-      const int chunks = (L.max_rest - std::min(L.max_k, j * P + 1) + kBwdChunk - 1) / kBwdChunk;
-      dim3 g(std::max(1, std::min(512, (rows * std::max(chunks, 1) + 7) / 8)), cnt);
-      bwd_gemv_kernel<S><<<g, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x, j);
+    if (!look || nsub < 3 || !side) {
+      for (int j = nsub - 1; j >= 0; --j) {
+        const int rows = std::min(P, L.max_k);
+        const int chunks = (L.max_rest - std::min(L.max_k, j * P + 1) + kBwdChunk - 1) / kBwdChunk;
+        dim3 g(std::max(1, std::min(512, (rows * std::max(chunks, 1) + 7) / 8)), cnt);
+        bwd_gemv_kernel<S, false><<<g, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
+                                                      j, 0, kAll);
+        bwd_trsv_kernel<S><<<cnt, kTrsvThreads, smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x, j);
+        n += 2;
+      }
+      continue;
+    }
+    evi = 0;
+    std::vector<cudaEvent_t> solved(nsub, nullptr);
+    cudaEvent_t start = ev();
+    record(start, st);
+    wait(side, start);
+    for (int j = nsub - 1; j >= 0 && ok; --j) {
+      // side: the columns solved two or more sub-steps ago (and the
+      // ancestors'), beside the triangular solve of sub-step j + 1
+      if (j + 2 < nsub) wait(side, solved[j + 2]);
+      const int rest = L.max_rest - std::min(L.max_k, j * P + 1) - P;
+      if (rest > 0) {
+        const int chunks = (rest + kBwdChunk - 1) / kBwdChunk;
+        dim3 g(std::max(1, std::min(512, (P * chunks + 7) / 8)), cnt);
+        bwd_gemv_kernel<S, true><<<g, 256, 0, side>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
+                                                      j, P, kAll);
+      }
+      cudaEvent_t rest_done = ev();
+      record(rest_done, side);
+      // main: the columns of sub-step j + 1, just solved
+      bwd_gemv_kernel<S, true><<<dim3(P / 8, cnt), 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U,
+                                                                 arena, x, j, 0, P);
+      wait(st, rest_done);
       bwd_trsv_kernel<S><<<cnt, kTrsvThreads, smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x, j);
-      n += 2;
+      solved[j] = ev();
+      record(solved[j], st);
+      n += 3;
     }
   }
-  return n;
+  return ok ? n : -1;
 }
 
 // one solve on d_x: the launch sequence is fixed by the symbolic structure
@@ -1494,12 +1601,14 @@ cudaError_t solve_t(MFHandle& h, cudaStream_t st) {
     e = solve_prepare<S>();
     if (e != cudaSuccess) return e;
     if (!d.cap_stream) e = cudaStreamCreateWithFlags(&d.cap_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess && !d.cap_side) e = cudaStreamCreateWithFlags(&d.cap_side, cudaStreamNonBlocking);
     if (e != cudaSuccess) return e;
     cudaGraph_t g = nullptr;
     e = cudaStreamBeginCapture(d.cap_stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
     const int n = solve_launches<S>(d, d.cap_stream);
     e = cudaStreamEndCapture(d.cap_stream, &g);
+    if (e == cudaSuccess && n < 0) e = cudaErrorInvalidResourceHandle;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&d.solve_exec, g, 0);
     if (g) cudaGraphDestroy(g);
     if (e != cudaSuccess) {
