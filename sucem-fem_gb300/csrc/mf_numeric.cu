@@ -115,6 +115,20 @@ __device__ __forceinline__ double2 s_recip(double2 v, double m2) {
   return make_double2(v.x * r, -v.y * r);
 }
 // barrier over the first `threads` threads that reach it (a multiple of 32)
+// programmatic dependent launch (the solve's kernels are launched with it):
+// a kernel may start while the kernel before it on its stream finishes; it
+// reads nothing that kernel wrote before pdl_wait(), and lets the next
+// kernel start launching (pdl_trigger) only once its own wait is over, so
+// at most one launch waits ahead.  Both are no-ops for a plain launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+// one 128-byte line of a row segment into L2 per lane (lanes beyond the
+// segment idle)
+__device__ __forceinline__ void prefetch_l2(const void* base, int bytes, int lane) {
+  if (lane * 128 < bytes)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"((const char*)base + lane * 128));
+}
+
 __device__ __forceinline__ void named_barrier(int id, int threads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
 }
@@ -680,6 +694,8 @@ __device__ __forceinline__ void fwd_trsv_front(const DNode& nd, const S* __restr
     const int i = t / P, jj = t % P;
     if (i < m && jj < i) Dt[i][jj] = F[(int64_t)i * nd.f + jj];
   }
+  pdl_wait();  // y[c0:c1] is the previous kernels' output
+  pdl_trigger();
   for (int t = threadIdx.x; t < m; t += kTrsvThreads) ys[t] = y[t];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = kTrsvThreads >> 5;
@@ -784,6 +800,8 @@ __device__ __forceinline__ void bwd_trsv_front(const DNode& nd, const S* __restr
     const int i = t / P, jj = t % P;
     if (i < m && jj >= i && jj < m) Dt[i][jj] = F[(int64_t)i * nd.f + jj];
   }
+  pdl_wait();
+  pdl_trigger();
   for (int t = threadIdx.x; t < m; t += kTrsvThreads) ys[t] = y[t];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = kTrsvThreads >> 5;
@@ -845,6 +863,13 @@ __global__ void fwd_gemv_kernel(const int32_t* __restrict__ list, int count,
   const int rows = min(nd.f - c1, q_hi);
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  // the factor rows do not depend on the kernels before: the first one is
+  // requested while they finish
+  if (q_lo + warp < rows)
+    prefetch_l2(arena + nd.off + (int64_t)(c1 + q_lo + warp) * nd.f + c0, (c1 - c0) * (int)sizeof(S),
+                lane);
+  pdl_wait();
+  pdl_trigger();
   for (int q = q_lo + warp; q < rows; q += nwarps)
     fwd_gemv_row<S, ATOM>(nd, U, arena, x, c0, c1, q, lane);
 }
@@ -870,6 +895,13 @@ __global__ void bwd_gemv_kernel(const int32_t* __restrict__ list, int count,
   const int nch = (ncol + kBwdChunk - 1) / kBwdChunk;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  if (warp < rows * nch) {
+    const int lo = cb + (warp / rows) * kBwdChunk;
+    prefetch_l2(arena + nd.off + (int64_t)(c0 + warp % rows) * nd.f + lo,
+                (min(ce, lo + kBwdChunk) - lo) * (int)sizeof(S), lane);
+  }
+  pdl_wait();
+  pdl_trigger();
   for (int w = warp; w < rows * nch; w += nwarps)
     bwd_gemv_item<S, ATOM>(nd, U, arena, x, c0, c1, cb, ce, nch, w, lane);
 }
@@ -1465,6 +1497,24 @@ cudaError_t solve_prepare() {
   return e;
 }
 
+// a solve kernel launched with programmatic dependent launch on its stream
+// (see pdl_wait / pdl_trigger)
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, ((KArgs)args)...);
+}
+
 // The launches of one solve on the work vector d_x (captured into a graph);
 // returns their count, or -1 when an event or stream call failed.
 //
@@ -1511,10 +1561,10 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
     const int nsub = (L.max_k + P - 1) / P;
     if (!look || nsub < 3 || !side) {
       for (int j = 0; j < nsub; ++j) {
-        fwd_trsv_kernel<S><<<cnt, kTrsvThreads, smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x, j);
+        launch_pdl(fwd_trsv_kernel<S>, cnt, kTrsvThreads, smem, st, L.d_nodes, cnt, d.d_nodes, arena, x, j);
         const int rows = L.max_rest - std::min(L.max_k, j * P + 1);
         dim3 g(std::max(1, std::min(512, (rows + 7) / 8)), cnt);
-        fwd_gemv_kernel<S, false><<<g, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
+        launch_pdl(fwd_gemv_kernel<S, false>, g, 256, 0, st, L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
                                                       j, 0, kAll);
         n += 2;
       }
@@ -1524,17 +1574,17 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
     std::vector<cudaEvent_t> done_rest(nsub, nullptr);
     for (int j = 0; j < nsub && ok; ++j) {
       if (j >= 2) wait(st, done_rest[j - 2]);
-      fwd_trsv_kernel<S><<<cnt, kTrsvThreads, smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x, j);
+      launch_pdl(fwd_trsv_kernel<S>, cnt, kTrsvThreads, smem, st, L.d_nodes, cnt, d.d_nodes, arena, x, j);
       cudaEvent_t solved = ev();
       record(solved, st);
       // the next sub-panel's rows, then the rest beside the next sub-step
-      fwd_gemv_kernel<S, true><<<dim3(P / 8, cnt), 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U,
+      launch_pdl(fwd_gemv_kernel<S, true>, dim3(P / 8, cnt), 256, 0, st, L.d_nodes, cnt, d.d_nodes, d.d_U,
                                                                  arena, x, j, 0, P);
       const int rows = L.max_rest - std::min(L.max_k, j * P + 1) - P;
       wait(side, solved);
       if (rows > 0) {
         dim3 g(std::max(1, std::min(512, (rows + 7) / 8)), cnt);
-        fwd_gemv_kernel<S, true><<<g, 256, 0, side>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
+        launch_pdl(fwd_gemv_kernel<S, true>, g, 256, 0, side, L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
                                                       j, P, kAll);
       }
       done_rest[j] = ev();
@@ -1552,9 +1602,9 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
         const int rows = std::min(P, L.max_k);
         const int chunks = (L.max_rest - std::min(L.max_k, j * P + 1) + kBwdChunk - 1) / kBwdChunk;
         dim3 g(std::max(1, std::min(512, (rows * std::max(chunks, 1) + 7) / 8)), cnt);
-        bwd_gemv_kernel<S, false><<<g, 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
+        launch_pdl(bwd_gemv_kernel<S, false>, g, 256, 0, st, L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
                                                       j, 0, kAll);
-        bwd_trsv_kernel<S><<<cnt, kTrsvThreads, smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x, j);
+        launch_pdl(bwd_trsv_kernel<S>, cnt, kTrsvThreads, smem, st, L.d_nodes, cnt, d.d_nodes, arena, x, j);
         n += 2;
       }
       continue;
@@ -1572,16 +1622,16 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
       if (rest > 0) {
         const int chunks = (rest + kBwdChunk - 1) / kBwdChunk;
         dim3 g(std::max(1, std::min(512, (P * chunks + 7) / 8)), cnt);
-        bwd_gemv_kernel<S, true><<<g, 256, 0, side>>>(L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
+        launch_pdl(bwd_gemv_kernel<S, true>, g, 256, 0, side, L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
                                                       j, P, kAll);
       }
       cudaEvent_t rest_done = ev();
       record(rest_done, side);
       // main: the columns of sub-step j + 1, just solved
-      bwd_gemv_kernel<S, true><<<dim3(P / 8, cnt), 256, 0, st>>>(L.d_nodes, cnt, d.d_nodes, d.d_U,
+      launch_pdl(bwd_gemv_kernel<S, true>, dim3(P / 8, cnt), 256, 0, st, L.d_nodes, cnt, d.d_nodes, d.d_U,
                                                                  arena, x, j, 0, P);
       wait(st, rest_done);
-      bwd_trsv_kernel<S><<<cnt, kTrsvThreads, smem, st>>>(L.d_nodes, cnt, d.d_nodes, arena, x, j);
+      launch_pdl(bwd_trsv_kernel<S>, cnt, kTrsvThreads, smem, st, L.d_nodes, cnt, d.d_nodes, arena, x, j);
       solved[j] = ev();
       record(solved[j], st);
       n += 3;
