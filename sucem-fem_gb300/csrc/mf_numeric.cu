@@ -211,6 +211,8 @@ template <typename S>
 __global__ void extend_add_kernel(const int32_t* __restrict__ kids, int nkids,
                                   const DNode* __restrict__ nodes, const int32_t* __restrict__ ea,
                                   S* __restrict__ arena) {
+  pdl_wait();  // launched with programmatic dependent launch (launch_pdl)
+  pdl_trigger();
   const int ci = blockIdx.y;
   if (ci >= nkids) return;
   const DNode c = nodes[kids[ci]];
@@ -260,6 +262,8 @@ __global__ void __launch_bounds__(256) diag_lu_kernel(const int32_t* __restrict_
                                                       S* __restrict__ arena, int p0,
                                                       const unsigned long long* __restrict__ amax,
                                                       double rel_tol, int* __restrict__ n_perturbed) {
+  pdl_wait();  // launched with programmatic dependent launch (launch_pdl)
+  pdl_trigger();
   constexpr int LPR = 256 / NBT;  // lanes per row
   constexpr int CPL = NBT / LPR;  // columns per lane
   constexpr int RPW = 32 / LPR;   // rows per warp
@@ -344,6 +348,8 @@ __global__ void __launch_bounds__(256) panel_trsm_kernel(const int32_t* __restri
                                                          int count,
                                                          const DNode* __restrict__ nodes,
                                                          S* __restrict__ arena, int p0) {
+  pdl_wait();  // launched with programmatic dependent launch (launch_pdl)
+  pdl_trigger();
   constexpr int CPT = NBT / 4;
   extern __shared__ __align__(16) unsigned char trsm_smem[];
   S(*D)[NBT + 1] = reinterpret_cast<S(*)[NBT + 1]>(trsm_smem);
@@ -467,6 +473,8 @@ __global__ void __launch_bounds__(256) gemm_update_kernel(const int32_t* __restr
                                                           const DNode* __restrict__ nodes,
                                                           S* __restrict__ arena, int p0,
                                                           int sp) {
+  pdl_wait();  // launched with programmatic dependent launch (launch_pdl)
+  pdl_trigger();
   extern __shared__ __align__(16) unsigned char gemm_smem[];
   S(*As)[65] = reinterpret_cast<S(*)[65]>(gemm_smem);
   S(*Bs)[64] = reinterpret_cast<S(*)[64]>(gemm_smem + sizeof(S) * NBT * 65);
@@ -559,6 +567,8 @@ __global__ void __launch_bounds__(256) schur_update_kernel(const int32_t* __rest
                                                            int count,
                                                            const DNode* __restrict__ nodes,
                                                            S* __restrict__ arena) {
+  pdl_wait();  // launched with programmatic dependent launch (launch_pdl)
+  pdl_trigger();
   extern __shared__ __align__(16) unsigned char schur_smem[];
   S(*As)[65] = reinterpret_cast<S(*)[65]>(schur_smem);
   S(*Bs)[64] = reinterpret_cast<S(*)[64]>(schur_smem + sizeof(S) * KC * 65);
@@ -1277,6 +1287,25 @@ cudaError_t setup_device(MFHandle& h, int dtype) {
   return e;
 }
 
+// a kernel launched with programmatic dependent launch on its stream (see
+// pdl_wait / pdl_trigger): the solve kernels and the factorisation's level
+// kernels
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, ((KArgs)args)...);
+}
+
 // events around the i-th tensor-core launch of a factorisation
 cudaError_t tc_event(MFDevice& d, int i, int which, cudaStream_t st) {
   while ((int)d.tc_ev.size() < 2 * (i + 1)) {
@@ -1299,9 +1328,9 @@ cudaError_t tc_launch(MFDevice& d, const TcLaunch& t, S* arena, cudaStream_t st)
     const int grid = std::max(1, std::min(t.ntiles, d.sm_count));
     cudaError_t e = tc_event(d, d.tc_n, 0, st);
     if (e != cudaSuccess) return e;
-    tc_presplit_kernel<S><<<t.nchunks, 256, 0, st>>>(t.d_strips, t.d_chunk_strip, d.d_nodes, arena,
+    launch_pdl(tc_presplit_kernel<S>, t.nchunks, 256, 0, st, t.d_strips, t.d_chunk_strip, d.d_nodes, arena,
                                                       d.d_img);
-    tc_update_kernel<S><<<grid, tc::THREADS, tc::smem_bytes<S>(), st>>>(
+    launch_pdl(tc_update_kernel<S>, grid, tc::THREADS, tc::smem_bytes<S>(), st, 
         t.d_tiles, t.ntiles, d.d_nodes, arena, d.d_img, d.d_flag + 1);
     e = tc_event(d, d.tc_n, 1, st);
     if (e != cudaSuccess) return e;
@@ -1393,7 +1422,7 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
       const int nk = (int)L.kids[c].size();
       if (nk == 0) continue;
       dim3 grid(std::max(16, std::min(1024, 8192 / nk)), nk);
-      extend_add_kernel<S><<<grid, 256, 0, st>>>(L.d_kids[c], nk, d.d_nodes, d.d_ea, arena);
+      launch_pdl(extend_add_kernel<S>, grid, 256, 0, st, L.d_kids[c], nk, d.d_nodes, d.d_ea, arena);
       count_launch(1);
       mark(0);
     }
@@ -1409,7 +1438,7 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
       int cnt = 0;
       while (cnt < (int)L.k_sorted.size() && L.k_sorted[cnt] > p0) ++cnt;
       if (cnt == 0) break;
-      diag_lu_kernel<S, NBT><<<cnt, 256, cnt <= d.sm_count ? kSoloSmem : 0, st>>>(
+      launch_pdl(diag_lu_kernel<S, NBT>, cnt, 256, cnt <= d.sm_count ? kSoloSmem : 0, st, 
           L.d_nodes, cnt, d.d_nodes, arena, p0, amax, tau, d.d_flag);
       count_launch(1);
       mark(1);
@@ -1419,7 +1448,7 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
         dim3 g1(2 * tiles, cnt);
         const size_t tsm = (int64_t)g1.x * g1.y <= d.sm_count ? std::max(trsm_smem, kSoloSmem)
                                                                : trsm_smem;
-        panel_trsm_kernel<S, NBT><<<g1, 256, tsm, st>>>(L.d_nodes, cnt, d.d_nodes, arena, p0);
+        launch_pdl(panel_trsm_kernel<S, NBT>, g1, 256, tsm, st, L.d_nodes, cnt, d.d_nodes, arena, p0);
         count_launch(1);
         mark(2);
         // K = nb panel update outside the deferred block
@@ -1434,7 +1463,7 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
         } else {
           const int tpd = (rest + 63) / 64;
           dim3 g2(tpd * tpd, cnt);
-          gemm_update_kernel<S, NBT><<<g2, 256, gemm_smem, st>>>(L.d_nodes, cnt, d.d_nodes,
+          launch_pdl(gemm_update_kernel<S, NBT>, g2, 256, gemm_smem, st, L.d_nodes, cnt, d.d_nodes,
                                                                   arena, p0, spw);
           count_launch(1);
           mark(3);
@@ -1456,7 +1485,7 @@ cudaError_t factor_t(MFHandle& h, const void* vals, double tau, cudaStream_t st)
       // one batched launch for all fronts of the level
       const int tpd = (L.max_u + 63) / 64;
       dim3 g3(tpd * tpd, nall);
-      schur_update_kernel<S, kSchurKC><<<g3, 256, schur_smem, st>>>(L.d_nodes, nall, d.d_nodes,
+      launch_pdl(schur_update_kernel<S, kSchurKC>, g3, 256, schur_smem, st, L.d_nodes, nall, d.d_nodes,
                                                                      arena);
       count_launch(1);
       mark(5);
@@ -1495,24 +1524,6 @@ cudaError_t solve_prepare() {
     e = cudaFuncSetAttribute(bwd_trsv_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
   return e;
-}
-
-// a solve kernel launched with programmatic dependent launch on its stream
-// (see pdl_wait / pdl_trigger)
-template <typename... KArgs, typename... Args>
-void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
-                Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kern, ((KArgs)args)...);
 }
 
 // The launches of one solve on the work vector d_x (captured into a graph);

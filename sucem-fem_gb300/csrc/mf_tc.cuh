@@ -236,6 +236,8 @@ __global__ void __launch_bounds__(256)
     tc_presplit_kernel(const int32_t* __restrict__ strips, const int32_t* __restrict__ chunk_strip,
                        const DNode* __restrict__ nodes, const S* __restrict__ arena,
                        uint8_t* __restrict__ img) {
+  pdl_wait();  // launched with programmatic dependent launch
+  pdl_trigger();
   using namespace tc;
   const int32_t* sd = strips + 8 * __ldg(&chunk_strip[blockIdx.x]);
   const DNode nd = nodes[sd[0]];
@@ -311,6 +313,11 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
+  // launched with programmatic dependent launch: the barrier and TMEM setup
+  // above overlap the kernel before; the arena and the chunk images are
+  // read only after this
+  pdl_wait();
+  pdl_trigger();
   const uint32_t tmem = *tmem_slot;
   auto raise = [&]() {
     *fail = 1;
