@@ -590,6 +590,53 @@ def run_precision(args):
                                "rel_error": float(torch.linalg.norm(x32 - x64) / torch.linalg.norm(x64)),
                                "fp32_ir_residual": i32["residual"], "fp64_residual": i64["residual"],
                                "fp32_ir_s": i32["seconds"], "fp64_s": i64["seconds"]}
+    del ds, x32, x64
+    torch.cuda.empty_cache()
+
+    # order 2.  The LU requirement of the 60^3 order-2 system from the
+    # symbolic analysis (host only): far beyond the device, so the largest
+    # jittered order-2 box whose complex64 LU fits is solved FP32+IR to 1e-8
+    # instead, and FP32+IR is compared with the FP64 path where the complex128
+    # LU fits too.
+    from sucemfem.solvers import lu_for_space
+    free_b, total_b = torch.cuda.mem_get_info()
+    V60 = FunctionSpace(mesh, order=2)
+    lu60 = lu_for_space(V60)
+    out["order2_lu_requirement"] = {
+        "cubes": args.cubes, "n_dofs": V60.n, "nnz": V60.nnz,
+        "lu_arena_gb_c64": lu60.info["arena"] * 8 / 1e9, "lu_tflop": lu60.info["flops"] * 8 / 1e12,
+        "largest_front": lu60.info["max_front"], "device_gb": total_b / 1e9,
+        "fits": lu60.info["arena"] * 8 < free_b}
+    del lu60, V60
+
+    def order2_case(cubes, seed, precisions):
+        m2 = jittered_box(cubes)
+        e2 = np.random.default_rng(seed).uniform(1.0, 4.0, m2.num_cells())
+        V2 = FunctionSpace(m2, order=2)
+        _, dofs2, con2 = evaluate_point_sources(V2, np.array([[0.5, 0.5, 0.5]]), np.array([[0, 0, 1.0]]))
+        b2 = np.zeros(V2.n, dtype=np.complex128)
+        b2[dofs2[0]] += -1j * k0 * Z0 * con2[0]
+        ds2 = DrivenSolver(V2, eps_r=e2)
+        res = {"cubes": cubes, "order": 2, "n_dofs": V2.n, "nnz": V2.nnz,
+               "lu_arena_gb_c64": ds2.lu.info["arena"] * 8 / 1e9,
+               "lu_tflop": ds2.lu.info["flops"] * 8 / 1e12}
+        xs = {}
+        for prec, tol in precisions:
+            x2, inf2 = ds2.solve(k0, b2, precision=prec, tol=tol)
+            torch.cuda.synchronize()
+            res[prec] = {"seconds": inf2["seconds"], "iterations": inf2["iterations"],
+                         "residual": inf2["residual"], "tolerance": tol}
+            xs[prec] = x2
+        if len(xs) == 2:
+            res["rel_error_fp32_ir_vs_fp64"] = float(torch.linalg.norm(xs["fp32-ir"] - xs["fp64"]) /
+                                                     torch.linalg.norm(xs["fp64"]))
+        del ds2, xs
+        torch.cuda.empty_cache()
+        return res
+
+    out["order2_solve"] = order2_case(args.precision_solve2_cubes, 3, [("fp32-ir", 1e-8)])
+    out["order2_solution_vs_fp64"] = order2_case(args.precision_fp64_cubes2, 4,
+                                                 [("fp32-ir", 1e-8), ("fp64", 1e-12)])
     print(json.dumps(out))
 
 
@@ -927,6 +974,10 @@ def main():
                              "eigen-batch", "postproc", "high-order"],
                     help="profiling cases: factor / assemble at --cubes, --order; serve; precision")
     ap.add_argument("--precision-solve-cubes", type=int, default=30)
+    ap.add_argument("--precision-solve2-cubes", type=int, default=40,
+                    help="jittered order-2 box solved FP32+IR in --only precision")
+    ap.add_argument("--precision-fp64-cubes2", type=int, default=24,
+                    help="jittered order-2 box where FP32+IR is compared with the FP64 path")
     ap.add_argument("--cavities", type=int, default=256)
     ap.add_argument("--serve-requests", type=int, default=300)
     ap.add_argument("--serve-rate", type=float, default=200.0)

@@ -86,6 +86,14 @@ __device__ __forceinline__ void cell_jacobian<double>(const float4*, const float
 __device__ __forceinline__ int sym_p(int m) { return m < 3 ? m : (m == 5 ? 1 : 0); }
 __device__ __forceinline__ int sym_q(int m) { return m < 3 ? m : (m == 3 ? 1 : 2); }
 
+// programmatic dependent launch between the two kernels of an order-1/2
+// assembly: the geometry kernel lets the entity kernel start launching at
+// once; the entity kernel clears its accumulators and loads its schedule
+// before it waits (griddepcontrol.wait) for the coefficients.  No-ops for a
+// plain launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 // ---- kernel 1: per-cell coefficients ----
 // Computed in Real, written as Out (the assembly's precision).  HILO (Real
 // double, Out float): each coefficient is written as float hi + lo, the 12
@@ -102,6 +110,7 @@ __global__ void cell_geometry_kernel(int64_t nt, const int4* __restrict__ cells,
                                      const Out* __restrict__ mu_inv, Out* __restrict__ g,
                                      Out* __restrict__ h, bool with_b, Real tscale,
                                      Real hscale) {
+  pdl_trigger();
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nt) return;
   const int4 v = __ldg(&cells[c]);
@@ -519,6 +528,7 @@ __device__ __forceinline__ void ent_task(int64_t task, const int4 meta, int P, i
   r0.cell = r1.cell = -1;
   if (nsteps > 0) r0 = load_step<C::PL>(blk0, lane);
   if (nsteps > 1) r1 = load_step<C::PL>(blk0 + C::WPS, lane);
+  pdl_wait();  // the cell coefficients are the geometry kernel's output
   Real g0[C::NG];
   load_g<Real, C::NG>(gcell, r0.cell, g0);
   int s = 0;
@@ -784,8 +794,22 @@ cudaError_t launch_t(DeviceSpace& d, const AssembleArgs& a, cudaStream_t stream)
   err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tb->smem);
   if (err != cudaSuccess) return err;
   const Real* kt = sizeof(Real) == 4 ? (const Real*)d.kt_f : (const Real*)d.kt_d;
-  kern<<<(unsigned)grid, C::BLOCK_WARPS * 32, (size_t)tb->smem, stream>>>(
-      p, g, h, kt, d.kt_lo_f, (Real*)a.S, (Real*)a.T, (Real*)a.B, (typename Cplx<Real>::T*)a.A);
+  {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(C::BLOCK_WARPS * 32);
+    cfg.dynamicSmemBytes = (size_t)tb->smem;
+    cfg.stream = stream;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    err = cudaLaunchKernelEx(&cfg, kern, p, (const Real*)g, (const Real*)h, kt,
+                             (const float*)d.kt_lo_f, (Real*)a.S, (Real*)a.T, (Real*)a.B,
+                             (typename Cplx<Real>::T*)a.A);
+    if (err != cudaSuccess) return err;
+  }
   count_launch(2);
   return cudaGetLastError();
 }
