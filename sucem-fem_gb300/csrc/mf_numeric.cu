@@ -156,6 +156,16 @@ template <>
 __device__ __forceinline__ double2 s_shfl_down(double2 v, int o) {
   return make_double2(__shfl_down_sync(~0u, v.x, o), __shfl_down_sync(~0u, v.y, o));
 }
+// c ? a : b without a branch
+__device__ __forceinline__ float s_sel(bool c, float a, float b) { return c ? a : b; }
+__device__ __forceinline__ double s_sel(bool c, double a, double b) { return c ? a : b; }
+__device__ __forceinline__ float2 s_sel(bool c, float2 a, float2 b) {
+  return make_float2(c ? a.x : b.x, c ? a.y : b.y);
+}
+__device__ __forceinline__ double2 s_sel(bool c, double2 a, double2 b) {
+  return make_double2(c ? a.x : b.x, c ? a.y : b.y);
+}
+
 template <typename S>
 __device__ __forceinline__ S s_shfl(S v, int src);
 template <>
@@ -721,12 +731,16 @@ __device__ __forceinline__ void fwd_trsv_front(const DNode& nd, const S* __restr
       __syncthreads();
     }
     if (warp == 0) {
+      // the chain: every step is shuffle -> multiply-add -> select on all
+      // lanes, no divergent branch (the lanes that keep v discard a product
+      // formed from whatever the unused triangle of Dt holds)
       const int rl = min(lane, mb - 1);
       S v = lane < mb ? ys[b0 + lane] : s_zero(S());
 #pragma unroll
       for (int jj = 0; jj < 31; ++jj) {
         const S yj = s_shfl(v, jj);
-        if (lane > jj && lane < mb) v = s_fms(v, Dt[b0 + rl][b0 + jj], yj);
+        const S t = s_fms(v, Dt[b0 + rl][b0 + jj], yj);
+        v = s_sel(lane > jj && lane < mb, t, v);
       }
       if (lane < mb) ys[b0 + lane] = v;
     }
@@ -833,10 +847,11 @@ __device__ __forceinline__ void bwd_trsv_front(const DNode& nd, const S* __restr
       S v = lane < mb ? ys[b0 + lane] : s_zero(S());
 #pragma unroll
       for (int jj = 31; jj >= 0; --jj) {
-        if (jj < mb) {
-          if (lane == jj) v = s_mul(v, rinv);
+        if (jj < mb) {  // uniform over the warp
+          v = s_sel(lane == jj, s_mul(v, rinv), v);
           const S xj = s_shfl(v, jj);
-          if (lane < jj) v = s_fms(v, Dt[b0 + rl][b0 + jj], xj);
+          const S t = s_fms(v, Dt[b0 + rl][b0 + jj], xj);
+          v = s_sel(lane < jj, t, v);
         }
       }
       if (lane < mb) ys[b0 + lane] = v;
