@@ -274,6 +274,18 @@ int sucem_vec_dot(int64_t n, int dtype, const void* x, const void* y, int conj, 
                   double* out, void* stream);
 int sucem_vec_convert(int64_t count, int dst_real_bytes, void* dst, int src_real_bytes,
                       const void* src, void* stream);
+/* Block Gram-Schmidt step of FGMRES (the orthogonalisation inside
+ * GMRESSolver, sucemfem/Utilities/LinalgSolvers.py:251-260, scipy's gmres):
+ * w is made orthogonal to the k rows V_i of V (leading dimension ldv
+ * elements) by classical Gram-Schmidt with one reorthogonalisation, all on
+ * the device; h[0:k] (complex as double pairs, real parts for F64) receive
+ * the summed coefficients conj(V_i)·w of both passes and h[k] the squared
+ * norm of the result (real part), so one copy to the host serves a whole
+ * Arnoldi step.  dtype F64 or C128; 0 <= k <= 63; work holds
+ * sucem_vec_gs_work_bytes(k) bytes; h is device memory of (k + 1) pairs. */
+int64_t sucem_vec_gs_work_bytes(int k);
+int sucem_vec_gs(int64_t n, int dtype, const void* V, int64_t ldv, int k, void* w, void* work,
+                 double* h, void* stream);
 
 /* Segmented (batched) double vectors for the batched Lanczos of
  * DefaultEigenSolver.solve_problem (EMVectorWaveEigenproblem.py:61-105,

@@ -3,6 +3,7 @@
 // value arrays and exact-zero compaction.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <mutex>
 #include <string>
@@ -292,6 +293,122 @@ __global__ void dot_final_kernel(int nparts, const double2* __restrict__ partial
   }
 }
 
+// ---- block Gram-Schmidt of FGMRES (vec_gs) ----
+// partial[b * k + i] = sum over block b's grid-stride slice of conj(V_i) w
+// (V_i = V + i * ldv), one basis vector after the other (w is re-read from
+// L2), each block reduced in a fixed order
+template <typename R, bool CPLX>
+__global__ void multidot_partial_kernel(int64_t n, const R* __restrict__ V, int64_t ldv, int k,
+                                        const R* __restrict__ w, double2* __restrict__ partial) {
+  __shared__ double sr[32], si[32];
+  const int wi = threadIdx.x >> 5, l = threadIdx.x & 31;
+  for (int i = 0; i < k; ++i) {
+    const R* v = V + (CPLX ? 2 : 1) * (int64_t)i * ldv;
+    double ar = 0, ai = 0;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (int64_t)gridDim.x * blockDim.x) {
+      if (!CPLX) {
+        ar += (double)v[e] * (double)w[e];
+      } else {
+        const double vr = v[2 * e], vi = -(double)v[2 * e + 1];
+        const double wr = w[2 * e], wim = w[2 * e + 1];
+        ar += vr * wr - vi * wim;
+        ai += vr * wim + vi * wr;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      ar += __shfl_down_sync(~0u, ar, o);
+      ai += __shfl_down_sync(~0u, ai, o);
+    }
+    if (l == 0) {
+      sr[wi] = ar;
+      si[wi] = ai;
+    }
+    __syncthreads();
+    if (wi == 0) {
+      const int nw = blockDim.x >> 5;
+      ar = l < nw ? sr[l] : 0.0;
+      ai = l < nw ? si[l] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) {
+        ar += __shfl_down_sync(~0u, ar, o);
+        ai += __shfl_down_sync(~0u, ai, o);
+      }
+      if (l == 0) partial[(int64_t)blockIdx.x * k + i] = make_double2(ar, ai);
+    }
+    __syncthreads();
+  }
+}
+
+// h[i] (+)= sum_b partial[b * k + i], one thread per i, blocks in order
+__global__ void multidot_final_kernel(int nparts, int k, const double2* __restrict__ partial,
+                                      double2* __restrict__ h, int accumulate) {
+  const int i = threadIdx.x;
+  if (i >= k) return;
+  double ar = 0, ai = 0;
+  for (int b = 0; b < nparts; ++b) {
+    ar += partial[(int64_t)b * k + i].x;
+    ai += partial[(int64_t)b * k + i].y;
+  }
+  if (accumulate) {
+    h[i].x += ar;
+    h[i].y += ai;
+  } else {
+    h[i] = make_double2(ar, ai);
+  }
+}
+
+// w -= sum_i c[i] V_i with the coefficients c = h (device memory)
+template <typename R, bool CPLX>
+__global__ void multiaxpy_kernel(int64_t n, const R* __restrict__ V, int64_t ldv, int k,
+                                 const double2* __restrict__ c, R* __restrict__ w) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    if (!CPLX) {
+      double acc = w[e];
+      for (int i = 0; i < k; ++i) acc -= c[i].x * (double)V[(int64_t)i * ldv + e];
+      w[e] = (R)acc;
+    } else {
+      double ar = w[2 * e], ai = w[2 * e + 1];
+      for (int i = 0; i < k; ++i) {
+        const R* v = V + 2 * (int64_t)i * ldv;
+        const double vr = v[2 * e], vi = v[2 * e + 1];
+        ar -= c[i].x * vr - c[i].y * vi;
+        ai -= c[i].x * vi + c[i].y * vr;
+      }
+      w[2 * e] = (R)ar;
+      w[2 * e + 1] = (R)ai;
+    }
+  }
+}
+
+constexpr int kGsBlocks = 256;
+
+// classical Gram-Schmidt with one reorthogonalisation of w against the k
+// basis vectors V_i (rows of V, leading dimension ldv elements), all on
+// the device: h[0:k] = the two passes' coefficients summed, h[k].x = |w|^2
+// after both.  work: kGsBlocks * (k + 1) double2 partials.
+template <typename R, bool CPLX>
+cudaError_t gs_t(int64_t n, const R* V, int64_t ldv, int k, R* w, double2* work, double2* h,
+                 cudaStream_t s) {
+  const int threads = 256;
+  const unsigned blocks = (unsigned)std::min<int64_t>(kGsBlocks * 4, (n + threads - 1) / threads);
+  for (int pass = 0; pass < 2 && k > 0; ++pass) {
+    multidot_partial_kernel<R, CPLX><<<kGsBlocks, threads, 0, s>>>(n, V, ldv, k, w, work);
+    multidot_final_kernel<<<1, 64, 0, s>>>(kGsBlocks, k, work, h, pass);
+    // the second pass subtracts only its own coefficients: they follow
+    // h's first-pass values in work's tail, so reduce them there first
+    if (pass == 0) {
+      multiaxpy_kernel<R, CPLX><<<blocks, threads, 0, s>>>(n, V, ldv, k, h, w);
+    } else {
+      multidot_final_kernel<<<1, 64, 0, s>>>(kGsBlocks, k, work, work + (int64_t)kGsBlocks * k, 0);
+      multiaxpy_kernel<R, CPLX><<<blocks, threads, 0, s>>>(n, V, ldv, k, work + (int64_t)kGsBlocks * k, w);
+    }
+  }
+  multidot_partial_kernel<R, CPLX><<<kGsBlocks, threads, 0, s>>>(n, w, 0, 1, w, work);
+  multidot_final_kernel<<<1, 64, 0, s>>>(kGsBlocks, 1, work, h + k, 0);
+  return cudaGetLastError();
+}
+
 // segmented dot products of real double vectors: out[s] = sum_{i in seg s} x_i y_i
 // one block per segment, fixed-order reduction
 __global__ void seg_dot_kernel(int nseg, const int64_t* __restrict__ seg, const double* __restrict__ x,
@@ -466,6 +583,27 @@ int sucem_vec_axpby(int64_t n, int dtype, double ar, double ai, const void* x, d
 }
 
 int64_t sucem_vec_dot_work_bytes(void) { return (int64_t)sucem::kDotBlocks * 16; }
+
+int64_t sucem_vec_gs_work_bytes(int k) {
+  return (int64_t)sucem::kGsBlocks * (k + 1) * 16 + (int64_t)(k + 1) * 16;
+}
+
+int sucem_vec_gs(int64_t n, int dtype, const void* V, int64_t ldv, int k, void* w, void* work,
+                 double* h, void* stream) {
+  if (!w || !work || !h || (k > 0 && !V)) return fail("null argument", SUCEM_ERR_ARG);
+  if (k < 0 || k > 63 || ldv < n) return fail("0 <= k <= 63 and ldv >= n required", SUCEM_ERR_ARG);
+  cudaStream_t s = (cudaStream_t)stream;
+  double2* wk = (double2*)work;
+  double2* hh = (double2*)h;
+  cudaError_t e;
+  switch (dtype) {
+    case SUCEM_F64: e = sucem::gs_t<double, false>(n, (const double*)V, ldv, k, (double*)w, wk, hh, s); break;
+    case SUCEM_C128: e = sucem::gs_t<double, true>(n, (const double*)V, ldv, k, (double*)w, wk, hh, s); break;
+    default: return fail("block Gram-Schmidt: dtype must be F64 or C128", SUCEM_ERR_ARG);
+  }
+  sucem::count_launch(k > 0 ? 9 : 2);
+  return e == cudaSuccess ? SUCEM_OK : cuda_fail(e, "sucem_vec_gs");
+}
 
 int sucem_vec_dot(int64_t n, int dtype, const void* x, const void* y, int conj, void* work,
                   double* out, void* stream) {

@@ -27,6 +27,10 @@ _native.declare("sucem_vec_dot", ctypes.c_int,
                 [ctypes.c_int64, ctypes.c_int, c_vp, c_vp, ctypes.c_int, c_vp, c_vp, c_vp])
 _native.declare("sucem_vec_convert", ctypes.c_int,
                 [ctypes.c_int64, ctypes.c_int, c_vp, ctypes.c_int, c_vp, c_vp])
+_native.declare("sucem_vec_gs_work_bytes", ctypes.c_int64, [ctypes.c_int])
+_native.declare("sucem_vec_gs", ctypes.c_int,
+                [ctypes.c_int64, ctypes.c_int, c_vp, ctypes.c_int64, ctypes.c_int, c_vp, c_vp, c_vp,
+                 c_vp])
 
 DT = {torch.float32: _native.F32, torch.float64: _native.F64,
       torch.complex64: _native.C64, torch.complex128: _native.C128}
@@ -51,6 +55,21 @@ class Vec:
              ptr(self.out), _device.stream_ptr())
         o = self.out.cpu().numpy()
         return complex(o[0], o[1]) if x.is_complex() else float(o[0])
+
+    def gs(self, V, k, w):
+        """Orthogonalise w (in place) against rows 0..k-1 of the 2-D device
+        tensor V by block Gram-Schmidt on the device (two classical passes);
+        returns (coefficients as a numpy array of k values, norm of w)."""
+        if getattr(self, "_gs_k", -1) < k:
+            nb = int(_native.lib().sucem_vec_gs_work_bytes(k))
+            self._gs_work = torch.empty((nb + 7) // 8, dtype=torch.float64, device=w.device)
+            self._gs_h = torch.empty(2 * (k + 1), dtype=torch.float64, device=w.device)
+            self._gs_k = k
+        call("sucem_vec_gs", w.numel(), DT[w.dtype], ptr(V), V.stride(0), k, ptr(w),
+             ptr(self._gs_work), ptr(self._gs_h), _device.stream_ptr())
+        hv = self._gs_h[:2 * (k + 1)].cpu().numpy()
+        c = hv[0:2 * k:2] + 1j * hv[1:2 * k:2] if w.is_complex() else hv[0:2 * k:2].copy()
+        return c, float(np.sqrt(max(hv[2 * k], 0.0)))
 
     def norm(self, x):
         return float(np.sqrt(abs(self.dot(x, x, True).real if x.is_complex() else self.dot(x, x))))
@@ -153,7 +172,12 @@ class RefinedDirectSolver:
             beta = v.norm(r)
             if beta / bn <= tol:
                 break
-            V = [r / beta]
+            # the Krylov basis as the rows of one device matrix, so that a
+            # whole Arnoldi step's orthogonalisation is one device call
+            # (classical Gram-Schmidt with one reorthogonalisation) and one
+            # copy of its coefficients to the host
+            Vb = torch.empty((m + 1, b.numel()), dtype=b.dtype, device=b.device)
+            v.axpby(1.0 / beta, r, 0.0, Vb[0])
             Z = []
             H = np.zeros((m + 1, m), dtype=np.complex128)
             g = np.zeros(m + 1, dtype=np.complex128)
@@ -163,14 +187,12 @@ class RefinedDirectSolver:
             k_used = 0
             for j in range(m):
                 z = torch.empty_like(b)
-                self._precond(V[j], z)
+                self._precond(Vb[j], z)
                 Z.append(z)
-                w = self.A.matvec(z)
-                for i in range(j + 1):                       # modified Gram-Schmidt
-                    hij = v.dot(V[i], w, True)
-                    H[i, j] = hij
-                    v.axpby(-hij, V[i], 1.0, w)
-                hn = v.norm(w)
+                w = Vb[j + 1]
+                self.A.matvec(z, w)
+                hcol, hn = v.gs(Vb, j + 1, w)
+                H[:j + 1, j] = hcol
                 H[j + 1, j] = hn
                 # Givens rotations G = [[conj(c), conj(s)], [-s, c]] with
                 # c = a/|(a,b)|, s = b/|(a,b)| map (a, b) to (|(a,b)|, 0)
@@ -191,7 +213,7 @@ class RefinedDirectSolver:
                 hist.append(est)
                 if est <= tol or hn == 0:
                     break
-                V.append(w / hn)
+                v.axpby(0.0, None, 1.0 / hn, w)  # w /= hn in place
             y = np.linalg.solve(np.triu(H[:k_used, :k_used]), g[:k_used])
             for i in range(k_used):
                 yi = complex(y[i]) if cplx else float(np.real(y[i]))

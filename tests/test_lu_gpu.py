@@ -165,3 +165,32 @@ def test_lookahead_solve_matches_the_sequential_schedule(dtype, monkeypatch):
     assert np.linalg.norm(xs[0] - xs[1]) / np.linalg.norm(xs[1]) < tol
     res = np.linalg.norm(M @ xs[0] - b) / np.linalg.norm(b)
     assert res < {"c64": 1e-4, "f32": 1e-3, "c128": 1e-11}[dtype], res
+
+
+@pytest.mark.parametrize("dtype", ["c128", "f64"])
+def test_block_gram_schmidt_matches_two_pass_projection(dtype):
+    """sucem_vec_gs (FGMRES's orthogonalisation on the device): against a
+    numpy two-pass classical Gram-Schmidt of the same vectors, the
+    coefficients, the orthogonalised vector and its norm agree to 1e-12."""
+    import torch
+    from sucemfem import _device
+    from sucemfem.solvers import Vec
+    rng = np.random.default_rng(7)
+    n, k = 5000, 6
+    cplx = dtype == "c128"
+    A = rng.standard_normal((k + 1, n)) + (1j * rng.standard_normal((k + 1, n)) if cplx else 0)
+    Q, _ = np.linalg.qr(A[:k].T)
+    Vh = np.zeros((k + 1, n), dtype=A.dtype)
+    Vh[:k] = Q.T
+    wh = A[k].copy()
+    tdt = torch.complex128 if cplx else torch.float64
+    V = torch.as_tensor(Vh, device=_device.device()).to(tdt)
+    w = torch.as_tensor(wh, device=_device.device()).to(tdt)
+    c, nrm = Vec().gs(V, k, w)
+    c1 = Vh[:k].conj() @ wh
+    w1 = wh - Vh[:k].T @ c1
+    c2 = Vh[:k].conj() @ w1
+    w2 = w1 - Vh[:k].T @ c2
+    assert np.allclose(c, c1 + c2, rtol=1e-12, atol=1e-12)
+    assert np.allclose(w.cpu().numpy(), w2, rtol=1e-12, atol=1e-12)
+    assert abs(nrm - np.linalg.norm(w2)) < 1e-12 * np.linalg.norm(w2)
