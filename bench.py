@@ -270,7 +270,12 @@ def run_gpu(args):
     # before the timed region
     call("sucem_assemble_helmholtz", h, 4, ptr(d_eps32), None, float(k0), ptr(A32), sp)
     trials0 = tuner.trials
-    plan = autotune.tune_lu(lu, A32, "c64", tuner)
+    if args.lu_plan:
+        # a fixed plan (profiling runs: no autotuning trials before the steps)
+        plan = tuple(int(v) for v in args.lu_plan.split(","))
+        lu.configure(*plan)
+    else:
+        plan = autotune.tune_lu(lu, A32, "c64", tuner)
     clocks = ClockSampler()
     clocks.start()
     time.sleep(0.3)
@@ -384,8 +389,9 @@ def run_gpu(args):
         "clocks": clk,
         "lu_plan": {"superpanel": int(plan[0]), "panel_min_k": int(plan[1]),
                     "autotune_trials_this_run": tuner.trials - trials0,
-                    "note": "chosen by sucemfem.autotune from timed factorisations (cached per "
-                            "device and size class)"},
+                    "note": ("given by --lu-plan" if args.lu_plan else
+                             "chosen by sucemfem.autotune from timed factorisations (cached per "
+                             "device and size class)")},
     }
     if not args.no_secondary and world == 1:
         # the batched-eigen and serving configurations, each with its own
@@ -994,6 +1000,8 @@ def main():
     ap.add_argument("--asm-reps", type=int, default=50)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lu-plan", default="",
+                    help="SUPERPANEL,PANEL_MIN_K: a fixed LU plan instead of the autotuner's")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

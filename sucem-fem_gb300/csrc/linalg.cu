@@ -343,21 +343,44 @@ __global__ void multidot_partial_kernel(int64_t n, const R* __restrict__ V, int6
   }
 }
 
-// h[i] (+)= sum_b partial[b * k + i], one thread per i, blocks in order
+// h[i] (+)= sum_b partial[b * k + i]: block i, a fixed-order tree over the
+// blocks' partials (deterministic)
 __global__ void multidot_final_kernel(int nparts, int k, const double2* __restrict__ partial,
                                       double2* __restrict__ h, int accumulate) {
-  const int i = threadIdx.x;
+  __shared__ double sr[32], si[32];
+  const int i = blockIdx.x;
   if (i >= k) return;
   double ar = 0, ai = 0;
-  for (int b = 0; b < nparts; ++b) {
+  for (int b = threadIdx.x; b < nparts; b += blockDim.x) {
     ar += partial[(int64_t)b * k + i].x;
     ai += partial[(int64_t)b * k + i].y;
   }
-  if (accumulate) {
-    h[i].x += ar;
-    h[i].y += ai;
-  } else {
-    h[i] = make_double2(ar, ai);
+  for (int o = 16; o > 0; o >>= 1) {
+    ar += __shfl_down_sync(~0u, ar, o);
+    ai += __shfl_down_sync(~0u, ai, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sr[w] = ar;
+    si[w] = ai;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    ar = l < nw ? sr[l] : 0.0;
+    ai = l < nw ? si[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      ar += __shfl_down_sync(~0u, ar, o);
+      ai += __shfl_down_sync(~0u, ai, o);
+    }
+    if (l == 0) {
+      if (accumulate) {
+        h[i].x += ar;
+        h[i].y += ai;
+      } else {
+        h[i] = make_double2(ar, ai);
+      }
+    }
   }
 }
 
@@ -398,18 +421,18 @@ cudaError_t gs_t(int64_t n, const R* V, int64_t ldv, int k, R* w, double2* work,
   const unsigned blocks = (unsigned)std::min<int64_t>(kGsBlocks * 4, (n + threads - 1) / threads);
   for (int pass = 0; pass < 2 && k > 0; ++pass) {
     multidot_partial_kernel<R, CPLX><<<kGsBlocks, threads, 0, s>>>(n, V, ldv, k, w, work);
-    multidot_final_kernel<<<1, 64, 0, s>>>(kGsBlocks, k, work, h, pass);
+    multidot_final_kernel<<<k, 256, 0, s>>>(kGsBlocks, k, work, h, pass);
     // the second pass subtracts only its own coefficients: they follow
     // h's first-pass values in work's tail, so reduce them there first
     if (pass == 0) {
       multiaxpy_kernel<R, CPLX><<<blocks, threads, 0, s>>>(n, V, ldv, k, h, w);
     } else {
-      multidot_final_kernel<<<1, 64, 0, s>>>(kGsBlocks, k, work, work + (int64_t)kGsBlocks * k, 0);
+      multidot_final_kernel<<<k, 256, 0, s>>>(kGsBlocks, k, work, work + (int64_t)kGsBlocks * k, 0);
       multiaxpy_kernel<R, CPLX><<<blocks, threads, 0, s>>>(n, V, ldv, k, work + (int64_t)kGsBlocks * k, w);
     }
   }
   multidot_partial_kernel<R, CPLX><<<kGsBlocks, threads, 0, s>>>(n, w, 0, 1, w, work);
-  multidot_final_kernel<<<1, 64, 0, s>>>(kGsBlocks, 1, work, h + k, 0);
+  multidot_final_kernel<<<1, 256, 0, s>>>(kGsBlocks, 1, work, h + k, 0);
   return cudaGetLastError();
 }
 
