@@ -991,6 +991,7 @@ struct MFLevel {
   int32_t* d_nodes = nullptr;
   int32_t* d_kids[2] = {nullptr, nullptr};
   std::vector<int> k_sorted;        // k of nodes_by_k
+  std::vector<int> f_sorted;        // f of nodes_by_k
 };
 
 struct MFDevice {
@@ -1277,6 +1278,7 @@ cudaError_t setup_device(MFHandle& h, int dtype) {
               [&](int32_t a, int32_t b) { return s.nodes[a].k > s.nodes[b].k; });
     for (int32_t i : L.nodes_by_k) {
       L.k_sorted.push_back((int)s.nodes[i].k);
+      L.f_sorted.push_back((int)s.nodes[i].f);
       L.max_k = std::max<int>(L.max_k, (int)s.nodes[i].k);
       L.max_rest = std::max<int>(L.max_rest, (int)s.nodes[i].f);
       L.max_u = std::max<int>(L.max_u, (int)(s.nodes[i].f - s.nodes[i].k));
@@ -1581,16 +1583,42 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
   auto record = [&](cudaEvent_t e, cudaStream_t s) { ok = ok && e && cudaEventRecord(e, s) == cudaSuccess; };
   auto wait = [&](cudaStream_t s, cudaEvent_t e) { ok = ok && e && cudaStreamWaitEvent(s, e, 0) == cudaSuccess; };
   const int kAll = 1 << 30;
+  // the fronts a sub-step touches (the k-descending prefix with k > j P)
+  // and the grid width of its products: the mean work per active front in
+  // warps of 8 per block (grid-stride loops take the larger fronts), so a
+  // level of many small fronts and a few large ones launches no empty blocks
+  auto active = [&](const MFLevel& L, int j) {
+    int c = 0;
+    while (c < (int)L.k_sorted.size() && L.k_sorted[c] > j * P) ++c;
+    return c;
+  };
+  auto fwd_width = [&](const MFLevel& L, int j, int na, int lo, int hi) {
+    int64_t rows = 0;
+    for (int a = 0; a < na; ++a) {
+      const int c1 = std::min(L.k_sorted[a], (j + 1) * P);
+      rows += std::max(0, std::min(L.f_sorted[a] - c1, hi) - lo);
+    }
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(512, (rows / std::max(na, 1) + 7) / 8));
+  };
+  auto bwd_width = [&](const MFLevel& L, int j, int na, int lo, int hi) {
+    int64_t items = 0;
+    for (int a = 0; a < na; ++a) {
+      const int c0 = j * P, c1 = std::min(L.k_sorted[a], c0 + P);
+      const int cols = std::max(0, std::min(L.f_sorted[a] - c1, hi) - lo);
+      items += (int64_t)(c1 - c0) * ((cols + kBwdChunk - 1) / kBwdChunk);
+    }
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(512, (items / std::max(na, 1) + 7) / 8));
+  };
   for (size_t lv = 0; lv < d.levels.size() && ok; ++lv) {
     const MFLevel& L = d.levels[lv];
     const int cnt = (int)L.nodes_by_k.size();
     const int nsub = (L.max_k + P - 1) / P;
     if (!look || nsub < 3 || !side) {
       for (int j = 0; j < nsub; ++j) {
-        launch_pdl(fwd_trsv_kernel<S>, cnt, kTrsvThreads, smem, st, L.d_nodes, cnt, d.d_nodes, arena, x, j);
-        const int rows = L.max_rest - std::min(L.max_k, j * P + 1);
-        dim3 g(std::max(1, std::min(512, (rows + 7) / 8)), cnt);
-        launch_pdl(fwd_gemv_kernel<S, false>, g, 256, 0, st, L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
+        const int na = active(L, j);
+        launch_pdl(fwd_trsv_kernel<S>, na, kTrsvThreads, smem, st, L.d_nodes, na, d.d_nodes, arena, x, j);
+        dim3 g(fwd_width(L, j, na, 0, kAll), na);
+        launch_pdl(fwd_gemv_kernel<S, false>, g, 256, 0, st, L.d_nodes, na, d.d_nodes, d.d_U, arena, x,
                                                       j, 0, kAll);
         n += 2;
       }
@@ -1600,17 +1628,17 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
     std::vector<cudaEvent_t> done_rest(nsub, nullptr);
     for (int j = 0; j < nsub && ok; ++j) {
       if (j >= 2) wait(st, done_rest[j - 2]);
-      launch_pdl(fwd_trsv_kernel<S>, cnt, kTrsvThreads, smem, st, L.d_nodes, cnt, d.d_nodes, arena, x, j);
+      const int na = active(L, j);
+      launch_pdl(fwd_trsv_kernel<S>, na, kTrsvThreads, smem, st, L.d_nodes, na, d.d_nodes, arena, x, j);
       cudaEvent_t solved = ev();
       record(solved, st);
       // the next sub-panel's rows, then the rest beside the next sub-step
-      launch_pdl(fwd_gemv_kernel<S, true>, dim3(P / 8, cnt), 256, 0, st, L.d_nodes, cnt, d.d_nodes, d.d_U,
+      launch_pdl(fwd_gemv_kernel<S, true>, dim3(P / 8, na), 256, 0, st, L.d_nodes, na, d.d_nodes, d.d_U,
                                                                  arena, x, j, 0, P);
-      const int rows = L.max_rest - std::min(L.max_k, j * P + 1) - P;
       wait(side, solved);
-      if (rows > 0) {
-        dim3 g(std::max(1, std::min(512, (rows + 7) / 8)), cnt);
-        launch_pdl(fwd_gemv_kernel<S, true>, g, 256, 0, side, L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
+      {
+        dim3 g(fwd_width(L, j, na, P, kAll), na);
+        launch_pdl(fwd_gemv_kernel<S, true>, g, 256, 0, side, L.d_nodes, na, d.d_nodes, d.d_U, arena, x,
                                                       j, P, kAll);
       }
       done_rest[j] = ev();
@@ -1625,12 +1653,11 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
     const int nsub = (L.max_k + P - 1) / P;
     if (!look || nsub < 3 || !side) {
       for (int j = nsub - 1; j >= 0; --j) {
-        const int rows = std::min(P, L.max_k);
-        const int chunks = (L.max_rest - std::min(L.max_k, j * P + 1) + kBwdChunk - 1) / kBwdChunk;
-        dim3 g(std::max(1, std::min(512, (rows * std::max(chunks, 1) + 7) / 8)), cnt);
-        launch_pdl(bwd_gemv_kernel<S, false>, g, 256, 0, st, L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
+        const int na = active(L, j);
+        dim3 g(bwd_width(L, j, na, 0, kAll), na);
+        launch_pdl(bwd_gemv_kernel<S, false>, g, 256, 0, st, L.d_nodes, na, d.d_nodes, d.d_U, arena, x,
                                                       j, 0, kAll);
-        launch_pdl(bwd_trsv_kernel<S>, cnt, kTrsvThreads, smem, st, L.d_nodes, cnt, d.d_nodes, arena, x, j);
+        launch_pdl(bwd_trsv_kernel<S>, na, kTrsvThreads, smem, st, L.d_nodes, na, d.d_nodes, arena, x, j);
         n += 2;
       }
       continue;
@@ -1644,20 +1671,19 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
       // side: the columns solved two or more sub-steps ago (and the
       // ancestors'), beside the triangular solve of sub-step j + 1
       if (j + 2 < nsub) wait(side, solved[j + 2]);
-      const int rest = L.max_rest - std::min(L.max_k, j * P + 1) - P;
-      if (rest > 0) {
-        const int chunks = (rest + kBwdChunk - 1) / kBwdChunk;
-        dim3 g(std::max(1, std::min(512, (P * chunks + 7) / 8)), cnt);
-        launch_pdl(bwd_gemv_kernel<S, true>, g, 256, 0, side, L.d_nodes, cnt, d.d_nodes, d.d_U, arena, x,
+      const int na = active(L, j);
+      {
+        dim3 g(bwd_width(L, j, na, P, kAll), na);
+        launch_pdl(bwd_gemv_kernel<S, true>, g, 256, 0, side, L.d_nodes, na, d.d_nodes, d.d_U, arena, x,
                                                       j, P, kAll);
       }
       cudaEvent_t rest_done = ev();
       record(rest_done, side);
       // main: the columns of sub-step j + 1, just solved
-      launch_pdl(bwd_gemv_kernel<S, true>, dim3(P / 8, cnt), 256, 0, st, L.d_nodes, cnt, d.d_nodes, d.d_U,
+      launch_pdl(bwd_gemv_kernel<S, true>, dim3(P / 8, na), 256, 0, st, L.d_nodes, na, d.d_nodes, d.d_U,
                                                                  arena, x, j, 0, P);
       wait(st, rest_done);
-      launch_pdl(bwd_trsv_kernel<S>, cnt, kTrsvThreads, smem, st, L.d_nodes, cnt, d.d_nodes, arena, x, j);
+      launch_pdl(bwd_trsv_kernel<S>, na, kTrsvThreads, smem, st, L.d_nodes, na, d.d_nodes, arena, x, j);
       solved[j] = ev();
       record(solved[j], st);
       n += 3;
