@@ -697,28 +697,31 @@ constexpr int kBwdChunk = 1024;         // columns per warp in the backward prod
 // the solved rows (a warp per row), then the 32 x 32 diagonal part by one
 // warp.  Shared memory (smem): Dt[P][P+1], ys[P].  Uniform over the block;
 // the caller separates two calls with a barrier.
-template <typename S>
+template <typename S, int PT = solve_panel<S>(), int THR = kTrsvThreads>
 __device__ __forceinline__ void fwd_trsv_front(const DNode& nd, const S* __restrict__ arena,
                                                S* __restrict__ x, int j, unsigned char* smem) {
   constexpr int P = solve_panel<S>();
-  S(*Dt)[P + 1] = reinterpret_cast<S(*)[P + 1]>(smem);
-  S* ys = reinterpret_cast<S*>(smem + sizeof(S) * P * (P + 1));
+  // the tile: PT x PT (PT >= the rows of the sub-panel, P = 128 columns
+  // per sub-step), THR threads
+  S(*Dt)[PT + 1] = reinterpret_cast<S(*)[PT + 1]>(smem);
+  S* ys = reinterpret_cast<S*>(smem + sizeof(S) * PT * (PT + 1));
   const int c0 = j * P;
   if (nd.k <= c0) return;
   const int m = min(nd.k, c0 + P) - c0;
+  if (m > PT) return;  // not for this tile size (the launch plan never asks)
   const S* F = arena + nd.off + (int64_t)c0 * nd.f + c0;
   S* y = x + nd.start + c0;
 #pragma unroll
-  for (int it = 0; it < P * P / kTrsvThreads; ++it) {
-    const int t = it * kTrsvThreads + threadIdx.x;
-    const int i = t / P, jj = t % P;
+  for (int it = 0; it < PT * PT / THR; ++it) {
+    const int t = it * THR + threadIdx.x;
+    const int i = t / PT, jj = t % PT;
     if (i < m && jj < i) Dt[i][jj] = F[(int64_t)i * nd.f + jj];
   }
   pdl_wait();  // y[c0:c1] is the previous kernels' output
   pdl_trigger();
-  for (int t = threadIdx.x; t < m; t += kTrsvThreads) ys[t] = y[t];
+  for (int t = threadIdx.x; t < m; t += THR) ys[t] = y[t];
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = kTrsvThreads >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = THR >> 5;
   for (int b0 = 0; b0 < m; b0 += 32) {
     const int mb = min(32, m - b0);
     if (b0 > 0) {
@@ -746,7 +749,7 @@ __device__ __forceinline__ void fwd_trsv_front(const DNode& nd, const S* __restr
     }
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < m; t += kTrsvThreads) y[t] = ys[t];
+  for (int t = threadIdx.x; t < m; t += THR) y[t] = ys[t];
 }
 
 // forward, sub-step j, row q of the rows [c1, f) of the front outside the
@@ -807,28 +810,31 @@ __device__ __forceinline__ void bwd_gemv_item(const DNode& nd, const int32_t* __
 // shared memory, 32 rows at a time from the bottom; the reciprocals of the
 // diagonal are formed in parallel before each 32-row chain.
 // Shared memory (smem): Dt[P][P+1], ys[P].
-template <typename S>
+template <typename S, int PT = solve_panel<S>(), int THR = kTrsvThreads>
 __device__ __forceinline__ void bwd_trsv_front(const DNode& nd, const S* __restrict__ arena,
                                                S* __restrict__ x, int j, unsigned char* smem) {
   constexpr int P = solve_panel<S>();
-  S(*Dt)[P + 1] = reinterpret_cast<S(*)[P + 1]>(smem);
-  S* ys = reinterpret_cast<S*>(smem + sizeof(S) * P * (P + 1));
+  // the tile: PT x PT (PT >= the rows of the sub-panel, P = 128 columns
+  // per sub-step), THR threads
+  S(*Dt)[PT + 1] = reinterpret_cast<S(*)[PT + 1]>(smem);
+  S* ys = reinterpret_cast<S*>(smem + sizeof(S) * PT * (PT + 1));
   const int c0 = j * P;
   if (nd.k <= c0) return;
   const int m = min(nd.k, c0 + P) - c0;
+  if (m > PT) return;  // not for this tile size (the launch plan never asks)
   const S* F = arena + nd.off + (int64_t)c0 * nd.f + c0;
   S* y = x + nd.start + c0;
 #pragma unroll
-  for (int it = 0; it < P * P / kTrsvThreads; ++it) {
-    const int t = it * kTrsvThreads + threadIdx.x;
-    const int i = t / P, jj = t % P;
+  for (int it = 0; it < PT * PT / THR; ++it) {
+    const int t = it * THR + threadIdx.x;
+    const int i = t / PT, jj = t % PT;
     if (i < m && jj >= i && jj < m) Dt[i][jj] = F[(int64_t)i * nd.f + jj];
   }
   pdl_wait();
   pdl_trigger();
-  for (int t = threadIdx.x; t < m; t += kTrsvThreads) ys[t] = y[t];
+  for (int t = threadIdx.x; t < m; t += THR) ys[t] = y[t];
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = kTrsvThreads >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = THR >> 5;
   const int nblk = (m + 31) / 32;
   for (int bi = nblk - 1; bi >= 0; --bi) {
     const int b0 = bi * 32, b1 = min(b0 + 32, m), mb = b1 - b0;
@@ -858,17 +864,20 @@ __device__ __forceinline__ void bwd_trsv_front(const DNode& nd, const S* __restr
     }
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < m; t += kTrsvThreads) y[t] = ys[t];
+  for (int t = threadIdx.x; t < m; t += THR) y[t] = ys[t];
 }
 
 // one block per listed front (dynamic shared memory Dt[P][P+1], ys[P])
-template <typename S>
-__global__ void __launch_bounds__(1024) fwd_trsv_kernel(const int32_t* __restrict__ list, int count,
+// one block per listed front (dynamic shared memory Dt[PT][PT+1], ys[PT]);
+// the 64-row variant (PT = 64, 256 threads) serves the fronts whose
+// sub-panel holds at most 64 rows, several blocks to an SM
+template <typename S, int PT = solve_panel<S>(), int THR = kTrsvThreads>
+__global__ void __launch_bounds__(THR) fwd_trsv_kernel(const int32_t* __restrict__ list, int count,
                                 const DNode* __restrict__ nodes, const S* __restrict__ arena,
                                 S* __restrict__ x, int j) {
   extern __shared__ __align__(16) unsigned char trsv_smem[];
   if ((int)blockIdx.x >= count) return;
-  fwd_trsv_front<S>(nodes[list[blockIdx.x]], arena, x, j, trsv_smem);
+  fwd_trsv_front<S, PT, THR>(nodes[list[blockIdx.x]], arena, x, j, trsv_smem);
 }
 
 // a warp per row of the listed front blockIdx.y, rows [c1 + q_lo, c1 + q_hi)
@@ -931,13 +940,13 @@ __global__ void bwd_gemv_kernel(const int32_t* __restrict__ list, int count,
     bwd_gemv_item<S, ATOM>(nd, U, arena, x, c0, c1, cb, ce, nch, w, lane);
 }
 
-template <typename S>
-__global__ void __launch_bounds__(1024) bwd_trsv_kernel(const int32_t* __restrict__ list, int count,
+template <typename S, int PT = solve_panel<S>(), int THR = kTrsvThreads>
+__global__ void __launch_bounds__(THR) bwd_trsv_kernel(const int32_t* __restrict__ list, int count,
                                 const DNode* __restrict__ nodes, const S* __restrict__ arena,
                                 S* __restrict__ x, int j) {
   extern __shared__ __align__(16) unsigned char trsv_smem[];
   if ((int)blockIdx.x >= count) return;
-  bwd_trsv_front<S>(nodes[list[blockIdx.x]], arena, x, j, trsv_smem);
+  bwd_trsv_front<S, PT, THR>(nodes[list[blockIdx.x]], arena, x, j, trsv_smem);
 }
 
 template <typename S, typename T>
@@ -1540,6 +1549,14 @@ cudaError_t solve_prepare() {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(bwd_trsv_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
+  // the 64-row tiles (solve_launches)
+  const int smem_s = (int)(sizeof(S) * 64 * 66);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(fwd_trsv_kernel<S, 64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem_s);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(bwd_trsv_kernel<S, 64, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem_s);
   return e;
 }
 
@@ -1592,6 +1609,30 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
     while (c < (int)L.k_sorted.size() && L.k_sorted[c] > j * P) ++c;
     return c;
   };
+  // the triangular solves of a sub-step: fronts whose sub-panel holds more
+  // than 64 rows (a prefix of the k-descending list) take the 128-row tile
+  // with 1024 threads, the rest the 64-row tile with 256 threads
+  constexpr int PS = 64, TS = 256;
+  const size_t smem_s = sizeof(S) * (size_t)PS * (PS + 2);
+  auto trsv = [&](const MFLevel& L, int j, int na, bool fwd, cudaStream_t s) {
+    int nb = 0;
+    while (nb < na && L.k_sorted[nb] > j * P + PS) ++nb;
+    if (nb > 0) {
+      if (fwd)
+        launch_pdl(fwd_trsv_kernel<S>, nb, kTrsvThreads, smem, s, L.d_nodes, nb, d.d_nodes, arena, x, j);
+      else
+        launch_pdl(bwd_trsv_kernel<S>, nb, kTrsvThreads, smem, s, L.d_nodes, nb, d.d_nodes, arena, x, j);
+      ++n;
+    }
+    if (na > nb) {
+      const int32_t* rest = L.d_nodes + nb;
+      if (fwd)
+        launch_pdl(fwd_trsv_kernel<S, PS, TS>, na - nb, TS, smem_s, s, rest, na - nb, d.d_nodes, arena, x, j);
+      else
+        launch_pdl(bwd_trsv_kernel<S, PS, TS>, na - nb, TS, smem_s, s, rest, na - nb, d.d_nodes, arena, x, j);
+      ++n;
+    }
+  };
   auto fwd_width = [&](const MFLevel& L, int j, int na, int lo, int hi) {
     int64_t rows = 0;
     for (int a = 0; a < na; ++a) {
@@ -1616,11 +1657,11 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
     if (!look || nsub < 3 || !side) {
       for (int j = 0; j < nsub; ++j) {
         const int na = active(L, j);
-        launch_pdl(fwd_trsv_kernel<S>, na, kTrsvThreads, smem, st, L.d_nodes, na, d.d_nodes, arena, x, j);
+        trsv(L, j, na, true, st);
         dim3 g(fwd_width(L, j, na, 0, kAll), na);
         launch_pdl(fwd_gemv_kernel<S, false>, g, 256, 0, st, L.d_nodes, na, d.d_nodes, d.d_U, arena, x,
                                                       j, 0, kAll);
-        n += 2;
+        n += 1;
       }
       continue;
     }
@@ -1629,7 +1670,7 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
     for (int j = 0; j < nsub && ok; ++j) {
       if (j >= 2) wait(st, done_rest[j - 2]);
       const int na = active(L, j);
-      launch_pdl(fwd_trsv_kernel<S>, na, kTrsvThreads, smem, st, L.d_nodes, na, d.d_nodes, arena, x, j);
+      trsv(L, j, na, true, st);
       cudaEvent_t solved = ev();
       record(solved, st);
       // the next sub-panel's rows, then the rest beside the next sub-step
@@ -1643,7 +1684,7 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
       }
       done_rest[j] = ev();
       record(done_rest[j], side);
-      n += 3;
+      n += 2;
     }
     wait(st, done_rest[nsub - 1]);  // the side stream's launches are ordered
   }
@@ -1657,8 +1698,8 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
         dim3 g(bwd_width(L, j, na, 0, kAll), na);
         launch_pdl(bwd_gemv_kernel<S, false>, g, 256, 0, st, L.d_nodes, na, d.d_nodes, d.d_U, arena, x,
                                                       j, 0, kAll);
-        launch_pdl(bwd_trsv_kernel<S>, na, kTrsvThreads, smem, st, L.d_nodes, na, d.d_nodes, arena, x, j);
-        n += 2;
+        trsv(L, j, na, false, st);
+        n += 1;
       }
       continue;
     }
@@ -1683,10 +1724,10 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
       launch_pdl(bwd_gemv_kernel<S, true>, dim3(P / 8, na), 256, 0, st, L.d_nodes, na, d.d_nodes, d.d_U,
                                                                  arena, x, j, 0, P);
       wait(st, rest_done);
-      launch_pdl(bwd_trsv_kernel<S>, na, kTrsvThreads, smem, st, L.d_nodes, na, d.d_nodes, arena, x, j);
+      trsv(L, j, na, false, st);
       solved[j] = ev();
       record(solved[j], st);
-      n += 3;
+      n += 2;
     }
   }
   return ok ? n : -1;
