@@ -207,11 +207,13 @@ class SolveServer:
         pending = []
         n_total = len(requests)
         n_seen = 0
+        prep_errors = []
         while n_seen < n_total:
             fut = prepared.get()
             n_seen += 1
             exc = fut.exception()
             if exc is not None:
+                prep_errors.append("preparation: %s" % exc)
                 continue
             p = fut.result()
             if p.bytes > self.budget:
@@ -240,5 +242,9 @@ class SolveServer:
             "p50_ms": 1e3 * lat[len(lat) // 2] if lat else None,
             "p99_ms": 1e3 * lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)] if lat else None,
             "max_inflight": inflight_max[0], "budget_bytes": self.budget,
+            "not_converged": sum(1 for r in results.values() if r.status == "not_converged"),
+            "errors": sum(1 for r in results.values() if r.status.startswith("error")) + len(prep_errors),
+            "error_sample": ([r.status for r in results.values() if r.status.startswith("error")]
+                             + prep_errors)[:3],
         }
         return [results[r.rid] for r in requests if r.rid in results]
