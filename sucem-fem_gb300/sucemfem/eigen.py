@@ -41,21 +41,75 @@ _native.declare("sucem_combine", ctypes.c_int,
                  ctypes.c_double, c_vp, c_vp, ctypes.c_int, c_vp])
 
 
-def reduced_pattern(indptr, indices, keep_order):
+def reduced_pattern(indptr, indices, keep_order, device=None):
+    """reduced_pattern on the GPU (torch index operations on ``device``),
+    the same arrays returned as numpy: a stacked pattern of tens of millions
+    of entries takes seconds through numpy on the host."""
+    if device is None:
+        return _reduced_pattern_host(indptr, indices, keep_order)
+    n = len(indptr) - 1
+    ip = torch.as_tensor(np.asarray(indptr, dtype=np.int64), device=device)
+    ix = torch.as_tensor(np.asarray(indices, dtype=np.int64), device=device)
+    ko = torch.as_tensor(np.asarray(keep_order, dtype=np.int64), device=device)
+    new = torch.full((n,), -1, dtype=torch.int64, device=device)
+    new[ko] = torch.arange(len(keep_order), device=device)
+    nc = new[ix]
+    rl = ip[1:] - ip[:-1]
+    m = (nc >= 0) & torch.repeat_interleave(new >= 0, rl)
+    q_all = torch.nonzero(m).squeeze(1)
+    cz = torch.zeros(len(m) + 1, dtype=torch.int64, device=device)
+    cz[1:] = torch.cumsum(m.to(torch.int64), 0)
+    cnt = cz[ip[1:]] - cz[ip[:-1]]          # kept entries per old row
+    start = cz[ip[:-1]]                      # their first position in q_all
+    lens = cnt[ko]
+    r_ip = torch.zeros(len(keep_order) + 1, dtype=torch.int64, device=device)
+    r_ip[1:] = torch.cumsum(lens, 0)
+    total = int(r_ip[-1])
+    idx = torch.repeat_interleave(start[ko] - r_ip[:-1], lens) + torch.arange(total, device=device)
+    q = q_all[idx]
+    cols = nc[q]
+    rows_new = torch.repeat_interleave(torch.arange(len(keep_order), device=device), lens)
+    if total > 1 and not bool(((cols[1:] > cols[:-1]) | (rows_new[1:] != rows_new[:-1])).all()):
+        key = rows_new * (len(keep_order) + 1) + cols
+        order = torch.argsort(key)
+        q, cols = q[order], cols[order]
+    return (r_ip.cpu().numpy(), cols.to(torch.int32).cpu().numpy(), q.cpu().numpy(),
+            new.cpu().numpy())
+
+
+def _reduced_pattern_host(indptr, indices, keep_order):
     """CSR of the sub-matrix on the DOFs ``keep_order`` (old ids, in their new
     order).  Returns (indptr, indices, value_index into the full CSR)."""
     n = len(indptr) - 1
+    indptr = np.asarray(indptr, dtype=np.int64)
     new = np.full(n, -1, dtype=np.int64)
     new[keep_order] = np.arange(len(keep_order))
-    rows = np.repeat(np.arange(n), np.diff(indptr))
-    nr, nc = new[rows], new[indices]
-    m = (nr >= 0) & (nc >= 0)
-    q = np.nonzero(m)[0]
-    order = np.lexsort((nc[q], nr[q]))
-    q = q[order]
-    r_ip = np.zeros(len(keep_order) + 1, dtype=np.int64)
-    np.add.at(r_ip, nr[q] + 1, 1)
-    return np.cumsum(r_ip), nc[q].astype(np.int32), q.astype(np.int64), new
+    nc = new[indices]
+    # kept entries of every old row, in their CSR order; the new rows are
+    # the kept old rows in the new order, each row's entries a contiguous
+    # run of q_all (gathered without a sort)
+    kept_row = new >= 0
+    m = nc >= 0
+    m &= np.repeat(kept_row, np.diff(indptr))
+    q_all = np.nonzero(m)[0]
+    cnt = np.add.reduceat(m.astype(np.int64), indptr[:-1]) if len(m) else np.zeros(n, np.int64)
+    cnt[np.diff(indptr) == 0] = 0  # reduceat takes the next element for empty rows
+    start = np.concatenate([[0], np.cumsum(cnt)[:-1]])
+    lens = cnt[keep_order]
+    r_ip = np.concatenate([[0], np.cumsum(lens)])
+    idx = np.repeat(start[keep_order] - r_ip[:-1], lens) + np.arange(r_ip[-1])
+    q = q_all[idx]
+    cols = nc[q]
+    # the new column ids keep the old order inside a row when the new
+    # numbering is increasing in the old one over each row's columns (it is
+    # for segment-contiguous reorderings of disjoint problems); else sort
+    inrow = np.ones(len(cols), dtype=bool)
+    inrow[r_ip[1:-1][lens[1:] > 0]] = False
+    if len(cols) > 1 and not np.all((np.diff(cols) > 0) | ~inrow[1:]):
+        rows_new = np.repeat(np.arange(len(keep_order)), lens)
+        order = np.lexsort((cols, rows_new))
+        q, cols = q[order], cols[order]
+    return r_ip, cols.astype(np.int32), q.astype(np.int64), new
 
 
 class BatchedShiftInvertLanczos:
@@ -78,9 +132,9 @@ class BatchedShiftInvertLanczos:
         self.nseg = int(seg.max()) + 1 if n else 0
         counts = np.bincount(seg[keep], minlength=self.nseg)
         self.seg_ptr_h = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
-        ip, ix, qidx, new = reduced_pattern(V.indptr, V.indices, keep)
-        self.n = len(keep)
         dev = _device.device()
+        ip, ix, qidx, new = reduced_pattern(V.indptr, V.indices, keep, device=dev)
+        self.n = len(keep)
         self.seg_ptr = torch.as_tensor(self.seg_ptr_h, device=dev)
         self.seg_of = torch.as_tensor(np.repeat(np.arange(self.nseg), counts).astype(np.int32), device=dev)
         self.qidx = torch.as_tensor(qidx, device=dev)
