@@ -25,7 +25,8 @@ import time
 DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "sucem_gb300", "autotune.json")
 
 # the candidates of the LU plan: (super-panel width, tensor-core panel threshold)
-LU_CANDIDATES = [(256, 64), (384, 64), (512, 64), (768, 64), (512, 128), (512, 1 << 30)]
+LU_CANDIDATES = [(128, 64), (192, 64), (256, 64), (384, 64), (512, 64), (768, 64), (256, 128),
+                 (512, 128), (512, 1 << 30)]
 SLOT_CANDIDATES = [2, 4, 6, 8]
 
 
