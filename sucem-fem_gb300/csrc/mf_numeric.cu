@@ -1101,14 +1101,15 @@ void free_dev(MFDevice& d) {
 // ends get one tensor-core launch over exactly those fronts (list on the
 // device).  Narrower super-panels move panel work onto the tensor cores
 // but re-read and re-write the trailing block once per super-panel; on the
-// 20^3 order-2 box the factorisation takes 78, 72, 73, 73, 74, 77 ms for
-// widths 192, 256, 384, 512, 768, 1024.  SUCEM_LU_SUPERPANEL overrides it (a
-// multiple of 64).
+// 20^3 order-2 box the factorisation takes 48.7, 46.1, 44.5, 45.3, 45.6,
+// 46.4 ms for widths 128, 192, 256, 384, 512, 768 (the autotuner's timed
+// trials; sucem_lu_configure sets the width per handle).
+// SUCEM_LU_SUPERPANEL overrides the default (a multiple of 64).
 constexpr int kTcSuperPanel = 512;
 // levels of at least two fronts whose largest pivot block has at least this
 // many columns apply the K = 64 panel updates on the tensor cores as well (a
-// single front's panel has too few tiles to fill the GPU; on the 20^3
-// order-2 box this takes the factorisation from 73 to 69 ms);
+// single front's panel has too few tiles to fill the GPU: enabling them
+// there too measured 44.8 against 44.5 ms on the 20^3 order-2 box);
 // SUCEM_LU_TC_PANEL_K overrides the column threshold
 constexpr int kTcPanelMinK = 64;
 constexpr int kTcPanel = 64;  // panel width of the complex64 factorisation
