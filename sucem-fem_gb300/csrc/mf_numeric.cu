@@ -1564,8 +1564,9 @@ cudaError_t solve_prepare() {
 // The launches of one solve on the work vector d_x (captured into a graph);
 // returns their count, or -1 when an event or stream call failed.
 //
-// Levels of three or more sub-steps (the few large fronts at the top of the
-// tree, whose sub-steps form the solve's critical path) take a look-ahead
+// Levels of three or more sub-steps and at most kLookaheadFronts fronts
+// (the few large fronts at the top of the tree, whose sub-steps form the
+// solve's critical path) take a look-ahead
 // schedule over two streams: each sub-step's products are split into the
 // part the next sub-step's triangular solve needs (the next 128 rows
 // forward, the just-solved 128 columns backward), kept on the main stream
@@ -1601,6 +1602,10 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
   auto record = [&](cudaEvent_t e, cudaStream_t s) { ok = ok && e && cudaEventRecord(e, s) == cudaSuccess; };
   auto wait = [&](cudaStream_t s, cudaEvent_t e) { ok = ok && e && cudaStreamWaitEvent(s, e, 0) == cudaSuccess; };
   const int kAll = 1 << 30;
+  // the look-ahead pays on the few large fronts at the top of a tree, whose
+  // sub-steps are a latency chain; levels of many fronts are bound by their
+  // bytes and take the one-stream sequence
+  constexpr int kLookaheadFronts = 64;
   // the fronts a sub-step touches (the k-descending prefix with k > j P)
   // and the grid width of its products: the mean work per active front in
   // warps of 8 per block (grid-stride loops take the larger fronts), so a
@@ -1655,7 +1660,7 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
     const MFLevel& L = d.levels[lv];
     const int cnt = (int)L.nodes_by_k.size();
     const int nsub = (L.max_k + P - 1) / P;
-    if (!look || nsub < 3 || !side) {
+    if (!look || nsub < 3 || cnt > kLookaheadFronts || !side) {
       for (int j = 0; j < nsub; ++j) {
         const int na = active(L, j);
         trsv(L, j, na, true, st);
@@ -1675,8 +1680,8 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
       cudaEvent_t solved = ev();
       record(solved, st);
       // the next sub-panel's rows, then the rest beside the next sub-step
-      launch_pdl(fwd_gemv_kernel<S, true>, dim3(P / 8, na), 256, 0, st, L.d_nodes, na, d.d_nodes, d.d_U,
-                                                                 arena, x, j, 0, P);
+      launch_pdl(fwd_gemv_kernel<S, true>, dim3(fwd_width(L, j, na, 0, P), na), 256, 0, st,
+                 L.d_nodes, na, d.d_nodes, d.d_U, arena, x, j, 0, P);
       wait(side, solved);
       {
         dim3 g(fwd_width(L, j, na, P, kAll), na);
@@ -1693,7 +1698,7 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
     const MFLevel& L = d.levels[lv];
     const int cnt = (int)L.nodes_by_k.size();
     const int nsub = (L.max_k + P - 1) / P;
-    if (!look || nsub < 3 || !side) {
+    if (!look || nsub < 3 || cnt > kLookaheadFronts || !side) {
       for (int j = nsub - 1; j >= 0; --j) {
         const int na = active(L, j);
         dim3 g(bwd_width(L, j, na, 0, kAll), na);
@@ -1722,8 +1727,8 @@ int solve_launches(MFDevice& d, cudaStream_t st) {
       cudaEvent_t rest_done = ev();
       record(rest_done, side);
       // main: the columns of sub-step j + 1, just solved
-      launch_pdl(bwd_gemv_kernel<S, true>, dim3(P / 8, na), 256, 0, st, L.d_nodes, na, d.d_nodes, d.d_U,
-                                                                 arena, x, j, 0, P);
+      launch_pdl(bwd_gemv_kernel<S, true>, dim3(bwd_width(L, j, na, 0, P), na), 256, 0, st,
+                 L.d_nodes, na, d.d_nodes, d.d_U, arena, x, j, 0, P);
       wait(st, rest_done);
       trsv(L, j, na, false, st);
       solved[j] = ev();
