@@ -142,6 +142,20 @@ __device__ __forceinline__ void s_atomic_sub(double2* p, double2 v) {
   atomicAdd(&p->x, -v.x);
   atomicAdd(&p->y, -v.y);
 }
+// shuffle down within groups of `width` lanes (a power of two)
+__device__ __forceinline__ float s_shfl_down_w(float v, int o, int width) {
+  return __shfl_down_sync(~0u, v, o, width);
+}
+__device__ __forceinline__ double s_shfl_down_w(double v, int o, int width) {
+  return __shfl_down_sync(~0u, v, o, width);
+}
+__device__ __forceinline__ float2 s_shfl_down_w(float2 v, int o, int width) {
+  return make_float2(__shfl_down_sync(~0u, v.x, o, width), __shfl_down_sync(~0u, v.y, o, width));
+}
+__device__ __forceinline__ double2 s_shfl_down_w(double2 v, int o, int width) {
+  return make_double2(__shfl_down_sync(~0u, v.x, o, width), __shfl_down_sync(~0u, v.y, o, width));
+}
+
 template <typename S>
 __device__ __forceinline__ S s_shfl_down(S v, int o);
 template <>
@@ -904,8 +918,36 @@ __global__ void fwd_gemv_kernel(const int32_t* __restrict__ list, int count,
                 lane);
   pdl_wait();
   pdl_trigger();
-  for (int q = q_lo + warp; q < rows; q += nwarps)
-    fwd_gemv_row<S, ATOM>(nd, U, arena, x, c0, c1, q, lane);
+  const int w = c1 - c0;
+  if (w > 32) {
+    for (int q = q_lo + warp; q < rows; q += nwarps)
+      fwd_gemv_row<S, ATOM>(nd, U, arena, x, c0, c1, q, lane);
+    return;
+  }
+  // a narrow sub-panel (the last one of a front, or a small front): groups
+  // of lpr lanes take a row each (2 to 8 rows per warp), at most two
+  // columns per lane
+  const int lpr = w > 16 ? 16 : w > 8 ? 8 : 4, rpw = 32 / lpr;
+  const int sub = lane % lpr, grp = lane / lpr;
+  S* y = x + nd.start;
+  for (int qb = q_lo + warp * rpw; qb < rows; qb += nwarps * rpw) {
+    const int q = qb + grp;
+    S acc = s_zero(S());
+    if (q < rows) {
+      const S* row = arena + nd.off + (int64_t)(c1 + q) * nd.f;
+      for (int c = c0 + sub; c < c1; c += lpr) acc = s_fms(acc, row[c], y[c]);
+    }
+    for (int o = lpr / 2; o > 0; o >>= 1) acc = s_add(acc, s_shfl_down_w(acc, o, lpr));
+    if (sub == 0 && q < rows) {
+      const int r = c1 + q;
+      if (r < nd.k && !ATOM)
+        y[r] = s_add(y[r], acc);
+      else if (r < nd.k)
+        s_atomic_sub(&y[r], s_fms(s_zero(S()), acc, s_real(S(), 1.0)));
+      else
+        s_atomic_sub(&x[U[nd.u_off + r - nd.k]], s_fms(s_zero(S()), acc, s_real(S(), 1.0)));
+    }
+  }
 }
 
 // a warp per (row, kBwdChunk columns) of the listed front blockIdx.y, the
