@@ -748,16 +748,24 @@ __device__ __forceinline__ void fwd_trsv_front(const DNode& nd, const S* __restr
       __syncthreads();
     }
     if (warp == 0) {
-      // the chain: every step is shuffle -> multiply-add -> select on all
-      // lanes, no divergent branch (the lanes that keep v discard a product
-      // formed from whatever the unused triangle of Dt holds)
+      // the chain, two columns per step: for the pair (jj, jj + 1) every
+      // row below takes
+      //   v -= (L[i][jj] - L[i][jj+1] L[jj+1][jj]) x_jj + L[i][jj+1] v_jj+1
+      // with v_jj+1 as it stands before the pair (row jj + 1 itself takes
+      // v -= L[jj+1][jj] x_jj), so both shuffles of a pair are issued
+      // together and its coefficient is formed off the dependent path.  No
+      // divergent branch: the lanes that keep v discard a product formed
+      // from whatever the unused triangle of Dt holds.
       const int rl = min(lane, mb - 1);
       S v = lane < mb ? ys[b0 + lane] : s_zero(S());
 #pragma unroll
-      for (int jj = 0; jj < 31; ++jj) {
-        const S yj = s_shfl(v, jj);
-        const S t = s_fms(v, Dt[b0 + rl][b0 + jj], yj);
-        v = s_sel(lane > jj && lane < mb, t, v);
+      for (int jj = 0; jj < 32; jj += 2) {
+        const S l_a = Dt[b0 + rl][b0 + jj], l_b = Dt[b0 + rl][b0 + jj + 1];
+        const S m_a = s_fms(l_a, l_b, Dt[b0 + jj + 1][b0 + jj]);
+        const S xa = s_shfl(v, jj), vb = s_shfl(v, jj + 1);
+        const S t2 = s_fms(s_fms(v, m_a, xa), l_b, vb);
+        const S t1 = s_fms(v, l_a, xa);
+        v = s_sel(lane > jj + 1 && lane < mb, t2, s_sel(lane == jj + 1 && lane < mb, t1, v));
       }
       if (lane < mb) ys[b0 + lane] = v;
     }
@@ -865,13 +873,29 @@ __device__ __forceinline__ void bwd_trsv_front(const DNode& nd, const S* __restr
       const int rl = min(lane, mb - 1);
       const S rinv = lane < mb ? s_div(s_one(S()), Dt[b0 + lane][b0 + lane]) : s_zero(S());
       S v = lane < mb ? ys[b0 + lane] : s_zero(S());
+      // two columns per step, from the bottom: for the pair (a, b = a - 1),
+      // x_a = v_a / U[a][a], x_b = (v_b - U[b][a] x_a) / U[b][b], and every
+      // row above takes
+      //   v -= (U[i][a] - U[i][b] U[b][a] / U[b][b]) x_a + U[i][b] / U[b][b] v_b
+      // with v_b as it stands before the pair, so both shuffles of a pair are
+      // issued together; the branches below are uniform over the warp (mb)
 #pragma unroll
-      for (int jj = 31; jj >= 0; --jj) {
-        if (jj < mb) {  // uniform over the warp
-          v = s_sel(lane == jj, s_mul(v, rinv), v);
-          const S xj = s_shfl(v, jj);
-          const S t = s_fms(v, Dt[b0 + rl][b0 + jj], xj);
-          v = s_sel(lane < jj, t, v);
+      for (int a = 31; a >= 1; a -= 2) {
+        const int b = a - 1;
+        if (a < mb) {
+          const S u_a = Dt[b0 + rl][b0 + a], u_b = Dt[b0 + rl][b0 + b];
+          const S n_b = s_mul(u_b, s_shfl(rinv, b));
+          const S m_a = s_fms(u_a, n_b, Dt[b0 + b][b0 + a]);
+          v = s_sel(lane == a, s_mul(v, rinv), v);
+          const S xa = s_shfl(v, a), vb = s_shfl(v, b);
+          const S t2 = s_fms(s_fms(v, m_a, xa), n_b, vb);
+          const S t1 = s_mul(s_fms(v, u_a, xa), rinv);
+          v = s_sel(lane < b, t2, s_sel(lane == b, t1, v));
+        } else if (b < mb) {  // the block's last row alone
+          v = s_sel(lane == b, s_mul(v, rinv), v);
+          const S xj = s_shfl(v, b);
+          const S t = s_fms(v, Dt[b0 + rl][b0 + b], xj);
+          v = s_sel(lane < b, t, v);
         }
       }
       if (lane < mb) ys[b0 + lane] = v;
