@@ -892,11 +892,11 @@ def run_serve(args):
 
 
 def run_high_order(args):
-    """N1curl orders 3 and 4: the cell-based assembly of S, T and B on a
+    """N1curl orders 3 and 4: the entry-gather assembly of S, T and B on a
     20^3 (order 3) and 16^3 (order 4) box with eps_r ~ U[1,4), FP32 and
     FP64, device-timed after a warm-up (outputs far larger than L2), against
     the HBM roofline of its algorithmic bytes (every value of S, T, B
-    written once and the per-cell CSR position table read once); then the
+    written once and the per-entry gather lists read once); then the
     reference's two higher-order cavity cases (order 3 on the 4^3 unit cube,
     order 4 on a 1 x 0.5 x 0.25 prism of 8 x 4 x 2 cubes), ten modes above
     sigma = 1.1 each, wall-timed solve_problem after a warm-up solve, with
@@ -936,7 +936,7 @@ def run_high_order(args):
             e1.record(stream)
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / reps
-            alg = 3 * V.nnz * rb + V.nt * nd * nd * 4 + V.nt * (16 + rb)
+            alg = 3 * V.nnz * rb + V.nt * nd * nd * 4 + (V.nnz + 1) * 4 + V.nt * (16 + rb)
             gbs = alg / (ms * 1e-3) / 1e9
             out["assembly"].append({
                 "order": order, "cubes": nc, "tets": V.nt, "n_dofs": V.n, "nnz": V.nnz,

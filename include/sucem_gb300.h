@@ -86,6 +86,11 @@ int sucem_space_sizes(const sucem_space* sp, int64_t* out);
                                       index (8 bytes), flags (bit 0: faces; bits 8-23: the
                                       task's longest row, made odd) */
 #define SUCEM_COPY_STEP_WORDS 14   /* uint32[n_step_blocks*(1+slot_planes)*32] step blocks */
+#define SUCEM_COPY_ENTRY_PTR 15    /* int32[nnz+1] orders 3-4: first cell entry of each CSR entry
+                                      (empty for orders 1-2) */
+#define SUCEM_COPY_ENTRY_SRC 16    /* int32[nt*ndof*ndof] orders 3-4: the cell entries
+                                      (c*ndof + a)*ndof + b summed into each CSR entry, in
+                                      ascending cell order */
 int sucem_space_copy(const sucem_space* sp, int what, void* host_dst);
 
 /* Sizes of the order-1/2 assembly schedule (the kernel's work plan; no

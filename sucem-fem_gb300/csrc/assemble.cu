@@ -1,8 +1,8 @@
 // Assembly of the N1curl curl-curl (S), mass (T) and first-order ABC (B)
 // matrices, the GPU replacement of dolfin.assemble for the forms of
 // sucemfem/Forms.py:71-85 and sucemfem/BoundaryConditions/ABC.py:56-57.
-// Orders 3 and 4 (45 and 84 DOFs per cell) use assemble_cells_kernel below
-// instead of the entity kernel.
+// Orders 3 and 4 (45 and 84 DOFs per cell) use assemble_cell_entries_kernel
+// below instead of the entity kernel.
 //
 // Two kernels (orders 1-2):
 //  1. cell_geometry_kernel (one thread per cell) writes the cell's 12 metric
@@ -615,59 +615,67 @@ __global__ void __launch_bounds__(EntCfg<ORDER, Real, MODE>::BLOCK_WARPS * 32)
                                      nullptr, p, gcell, hcell, kt, kt_lo, S, T, B, A);
 }
 
-// Orders 3-4: one block per cell (grid-stride over the cells), a thread per
-// local entry (a, b): the cell's 12 coefficients contracted with the
-// reference tensors ([a][b][12], read through L1/L2) and added atomically
-// at the entry's precomputed CSR position (the outputs are zeroed first).
-// Every value is exact up to the order in which the cells' contributions
-// are summed, which is not fixed.
+// Orders 3-4: a thread per CSR entry (grid-stride), gathering the cell
+// entries listed for it (ascending cell order): each is the cell's 12
+// coefficients contracted with the reference tensors ([a][b][12], read
+// through L1/L2), plus the tangential term of the cell's exterior faces.
+// S, T and B are summed separately in that fixed order and every output
+// entry is written once (no atomics, no zeroing pass), so the matrices are
+// the same bits on every run.
 template <int ND, typename Real, bool WITH_B, int MODE>
 __global__ void __launch_bounds__(256)
-    assemble_cells_kernel(int64_t nt, const int32_t* __restrict__ pos,
-                          const int32_t* __restrict__ bidx, const uint8_t* __restrict__ ext_mask,
-                          const Real* __restrict__ gcell, const Real* __restrict__ hcell,
-                          const Real* __restrict__ kab, const Real* __restrict__ kt, Real* S,
-                          Real* T, Real* B, typename Cplx<Real>::T* A, Real k0) {
+    assemble_cell_entries_kernel(int64_t nnz, const int32_t* __restrict__ ptr,
+                                 const int32_t* __restrict__ src,
+                                 const int32_t* __restrict__ bidx,
+                                 const uint8_t* __restrict__ ext_mask,
+                                 const Real* __restrict__ gcell, const Real* __restrict__ hcell,
+                                 const Real* __restrict__ kab, const Real* __restrict__ kt,
+                                 Real* S, Real* T, Real* B, typename Cplx<Real>::T* A, Real k0) {
   constexpr int NN = ND * ND;
-  const Real k0sq = k0 * k0;
-  for (int64_t c = blockIdx.x; c < nt; c += gridDim.x) {
-    Real g[12];
-    load12<Real>(gcell + c * 12, g);
-    int hb = -1, mask = 0;
-    if (WITH_B) {
-      hb = __ldg(&bidx[c]);
-      if (hb >= 0) mask = __ldg(&ext_mask[c]);
-    }
-    const int32_t* pc = pos + c * NN;
-    for (int e = threadIdx.x; e < NN; e += blockDim.x) {
-      Real kk[12];
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nnz;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    Real sv = 0, tm = 0, bv = 0;
+    const int j1 = __ldg(&ptr[q + 1]);
+    for (int j = __ldg(&ptr[q]); j < j1; ++j) {
+      const int sc = __ldg(&src[j]);
+      const int c = sc / NN, e = sc - c * NN;
+      Real g[12], kk[12];
+      load12<Real>(gcell + (int64_t)c * 12, g);
       load12<Real>(kab + (int64_t)e * 12, kk);
-      Real sv = 0, tm = 0;
+      Real sc_s = 0, sc_t = 0;
 #pragma unroll
       for (int m = 0; m < 6; ++m) {
-        sv = fma(g[m], kk[m], sv);
-        tm = fma(g[6 + m], kk[6 + m], tm);
+        sc_s = fma(g[m], kk[m], sc_s);
+        sc_t = fma(g[6 + m], kk[6 + m], sc_t);
       }
-      Real bv = 0;
-      if (WITH_B && hb >= 0) {
-        const Real* hh = hcell + (int64_t)hb * 12;
+      sv += sc_s;
+      tm += sc_t;
+      if (WITH_B) {
+        const int hb = __ldg(&bidx[c]);
+        if (hb >= 0) {
+          const int mask = __ldg(&ext_mask[c]);
+          const Real* hh = hcell + (int64_t)hb * 12;
+          Real sc_b = 0;
 #pragma unroll
-        for (int f = 0; f < 4; ++f) {
-          if (!(mask >> f & 1)) continue;
+          for (int f = 0; f < 4; ++f) {
+            if (!(mask >> f & 1)) continue;
 #pragma unroll
-          for (int m = 0; m < 3; ++m)
-            bv = fma(__ldg(&hh[f * 3 + m]), __ldg(&kt[(f * 3 + m) * NN + e]), bv);
+            for (int m = 0; m < 3; ++m)
+              sc_b = fma(__ldg(&hh[f * 3 + m]), __ldg(&kt[(f * 3 + m) * NN + e]), sc_b);
+          }
+          bv += sc_b;
         }
       }
-      const int64_t q = __ldg(&pc[e]);
-      if (MODE == 1) {
-        atomicAdd(&A[q].x, sv - k0sq * tm);
-        if (WITH_B && bv != 0) atomicAdd(&A[q].y, k0 * bv);
-      } else {
-        if (S) atomicAdd(&S[q], sv);
-        if (T) atomicAdd(&T[q], tm);
-        if (WITH_B && B && bv != 0) atomicAdd(&B[q], bv);
-      }
+    }
+    if (MODE == 1) {
+      typename Cplx<Real>::T v;
+      v.x = sv - k0 * k0 * tm;
+      v.y = k0 * bv;
+      A[q] = v;
+    } else {
+      if (S) S[q] = sv;
+      if (T) T[q] = tm;
+      if (WITH_B && B) B[q] = bv;
     }
   }
 }
@@ -828,31 +836,19 @@ cudaError_t launch_cells_t(DeviceSpace& d, const AssembleArgs& a, cudaStream_t s
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
   }
-  const size_t vbytes = (size_t)d.nnz * sizeof(Real);
-  if (MODE == 1) {
-    err = cudaMemsetAsync(a.A, 0, 2 * vbytes, stream);
-  } else {
-    if (a.S) err = cudaMemsetAsync(a.S, 0, vbytes, stream);
-    if (err == cudaSuccess && a.T) err = cudaMemsetAsync(a.T, 0, vbytes, stream);
-    if (err == cudaSuccess && WITH_B && a.B) err = cudaMemsetAsync(a.B, 0, vbytes, stream);
-  }
-  if (err != cudaSuccess) return err;
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(d.nt, (int64_t)nsm * 8));
+  const int64_t grid = std::max<int64_t>(1, (d.nnz + 255) / 256);
   const Real* kab = sizeof(Real) == 4 ? (const Real*)d.kab_f : (const Real*)d.kab_d;
   const Real* kt = sizeof(Real) == 4 ? (const Real*)d.kt_f : (const Real*)d.kt_d;
-  assemble_cells_kernel<ND, Real, WITH_B, MODE><<<(unsigned)grid, 256, 0, stream>>>(
-      d.nt, d.cell_pos, d.bidx, d.ext_mask, g, h, kab, kt, (Real*)a.S, (Real*)a.T, (Real*)a.B,
-      (typename Cplx<Real>::T*)a.A, (Real)a.k0);
+  assemble_cell_entries_kernel<ND, Real, WITH_B, MODE><<<(unsigned)grid, 256, 0, stream>>>(
+      d.nnz, d.entry_ptr, d.entry_src, d.bidx, d.ext_mask, g, h, kab, kt, (Real*)a.S, (Real*)a.T,
+      (Real*)a.B, (typename Cplx<Real>::T*)a.A, (Real)a.k0);
   count_launch(2);
   return cudaGetLastError();
 }
 
 template <int ND, typename Real>
 cudaError_t dispatch_cells(DeviceSpace& d, const AssembleArgs& a, cudaStream_t stream) {
-  if (!d.cell_pos) return cudaErrorInvalidValue;
+  if (!d.entry_ptr || !d.entry_src) return cudaErrorInvalidValue;
   if (a.mode == 1) return launch_cells_t<ND, Real, true, 1>(d, a, stream);
   if (a.B) return launch_cells_t<ND, Real, true, 0>(d, a, stream);
   return launch_cells_t<ND, Real, false, 0>(d, a, stream);

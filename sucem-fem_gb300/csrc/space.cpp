@@ -253,23 +253,58 @@ std::string build_space(Space& s, const double* coords, int64_t nv, const int64_
       std::copy(ent_cols.begin() + ent_col_ptr[k], ent_cols.begin() + ent_col_ptr[k + 1],
                 s.indices.begin() + s.indptr[ent_first_dof(k) + j]);
 
-  // ---- orders 3-4: CSR position of every local entry of every cell ----
+  // ---- orders 3-4: the cell entries that sum into each CSR entry ----
+  // Row r (a DOF of entity k) receives, from every cell incident to k, the
+  // entries (a, b) with cell_dofs[c][a] = r.  Per CSR entry the list holds
+  // them in ascending cell order (within one cell only one b maps to a
+  // column), which fixes the summation order of the assembly.
   if (order >= 3) {
     if (nt * int64_t(nd) * nd >= (int64_t(1) << 31))
-      return "mesh too large for the order-3/4 position table (2^31 cell entries)";
-    s.cell_pos.resize(nt * int64_t(nd) * nd);
-    std::vector<int64_t> dof_ent(s.n);
+      return "mesh too large for the order-3/4 entry lists (2^31 cell entries)";
+    s.entry_ptr.assign(s.nnz + 1, 0);
+    s.entry_src.assign(nt * int64_t(nd) * nd, 0);
+    // first contribution of each row: entity k's rows each take ninc(k) * nd
+    std::vector<int64_t> row_first(s.n + 1, 0);
     for (int64_t k = 0; k < s.n_ent; ++k)
-      for (int j = 0; j < ent_ndof(k); ++j) dof_ent[ent_first_dof(k) + j] = k;
-#pragma omp parallel for schedule(static)
-    for (int64_t c = 0; c < nt; ++c) {
-      const int32_t* d = &s.cell_dofs[c * nd];
-      for (int a = 0; a < nd; ++a) {
-        const int64_t k = dof_ent[d[a]];
+      for (int j = 0; j < ent_ndof(k); ++j)
+        row_first[ent_first_dof(k) + j + 1] = int64_t(s.ent_ptr[k + 1] - s.ent_ptr[k]) * nd;
+    for (int64_t r = 0; r < s.n; ++r) row_first[r + 1] += row_first[r];
+    s.entry_ptr[s.nnz] = int32_t(row_first[s.n]);
+#pragma omp parallel
+    {
+      std::vector<int32_t> slot, cur;
+#pragma omp for schedule(dynamic, 256)
+      for (int64_t k = 0; k < s.n_ent; ++k) {
+        const int32_t i0 = s.ent_ptr[k], i1 = s.ent_ptr[k + 1];
         const auto b0 = ent_cols.begin() + ent_col_ptr[k], b1 = ent_cols.begin() + ent_col_ptr[k + 1];
-        for (int b = 0; b < nd; ++b)
-          s.cell_pos[(c * nd + a) * nd + b] =
-              int32_t(s.indptr[d[a]] + (std::lower_bound(b0, b1, d[b]) - b0));
+        const int64_t len = ent_col_ptr[k + 1] - ent_col_ptr[k];
+        // column slot of every local DOF of every incident cell (shared by the rows)
+        slot.resize(size_t(i1 - i0) * nd);
+        for (int32_t i = i0; i < i1; ++i) {
+          const int32_t* d = &s.cell_dofs[int64_t(s.inc_cell[i]) * nd];
+          for (int b = 0; b < nd; ++b)
+            slot[size_t(i - i0) * nd + b] = int32_t(std::lower_bound(b0, b1, d[b]) - b0);
+        }
+        for (int j = 0; j < ent_ndof(k); ++j) {
+          const int64_t r = ent_first_dof(k) + j, q0 = s.indptr[r];
+          cur.assign(len, 0);
+          for (size_t t = 0; t < slot.size(); ++t) cur[slot[t]]++;
+          int64_t run = row_first[r];
+          for (int64_t p = 0; p < len; ++p) {
+            const int32_t n_p = cur[p];
+            s.entry_ptr[q0 + p] = int32_t(run);
+            cur[p] = int32_t(run);
+            run += n_p;
+          }
+          for (int32_t i = i0; i < i1; ++i) {
+            const int64_t c = s.inc_cell[i];
+            const int32_t* d = &s.cell_dofs[c * nd];
+            int a = 0;
+            while (d[a] != r) ++a;
+            for (int b = 0; b < nd; ++b)
+              s.entry_src[cur[slot[size_t(i - i0) * nd + b]]++] = int32_t((c * nd + a) * nd + b);
+          }
+        }
       }
     }
   }

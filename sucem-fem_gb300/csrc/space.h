@@ -49,9 +49,11 @@ struct Space {
                                        //   [1..ndof_cell] column slot of each local dof
   int rec_bytes = 8;
 
-  // orders 3-4 (cell-based assembly): CSR position of every local entry,
-  // cell_pos[(c * ndof_cell + a) * ndof_cell + b] = index of (dof a, dof b)
-  std::vector<int32_t> cell_pos;
+  // orders 3-4 (entry-gather assembly): CSR entry q sums the cell entries
+  // entry_src[entry_ptr[q] .. entry_ptr[q+1]), each coded
+  // (c * ndof_cell + a) * ndof_cell + b, in ascending cell order
+  std::vector<int32_t> entry_ptr;      // nnz+1
+  std::vector<int32_t> entry_src;      // nt*ndof_cell^2
 
   // Entity-per-lane assembly schedule (orders 1-2).  Entities are grouped
   // into warp tasks of 32 (one entity per lane) that share the entity kind

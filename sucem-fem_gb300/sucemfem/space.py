@@ -123,6 +123,16 @@ class FunctionSpace:
         words = self._copy("step_words", (nblk, 1 + planes, 32), np.uint32)
         return dict(n_tasks_interior=nint, task_ent=ent, task_meta=meta, step_words=words)
 
+    def entry_lists(self):
+        """The order-3/4 assembly kernel's gather lists (host copy): CSR
+        entry q sums the cell entries src[ptr[q]:ptr[q+1]], each coded
+        (c * ndof_cell + a) * ndof_cell + b, in ascending cell order."""
+        if self.order < 3:
+            raise ValueError("entry lists exist for basis orders 3 and 4 only")
+        ptr = self._copy("entry_ptr", self.nnz + 1, np.int32)
+        src = self._copy("entry_src", self.nt * self.ndof_cell ** 2, np.int32)
+        return ptr, src
+
     def facet_closure_dofs(self, faces):
         """DOFs on the closure of the given facets (facet ids = face ids)."""
         faces = np.asarray(faces, dtype=np.int64)

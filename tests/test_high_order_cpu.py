@@ -87,6 +87,30 @@ def test_native_space_matches_oracle(order, dims):
     assert np.array_equal(V.facet_closure_dofs(topo.exterior_faces()), fem.pec_dofs(topo, order))
 
 
+@pytest.mark.parametrize("order", [3, 4])
+def test_entry_lists_cover_every_cell_entry_once_in_cell_order(order):
+    """The gather lists of the order-3/4 assembly: every cell entry (c, a, b)
+    appears exactly once, under the CSR entry (cell_dofs[c, a],
+    cell_dofs[c, b]), and each entry's list runs in ascending cell order (the
+    fixed summation order)."""
+    from sucemfem.mesh import Mesh
+    from sucemfem.space import FunctionSpace
+    coords, cells = fem.box_mesh(1.0, 0.5, 0.75, 3, 2, 2)
+    V = FunctionSpace(Mesh(coords, cells), order=order)
+    nd, nt = V.ndof_cell, V.nt
+    ptr, src = V.entry_lists()
+    assert ptr[0] == 0 and ptr[-1] == nt * nd * nd and np.all(np.diff(ptr) >= 1)
+    assert np.array_equal(np.sort(src), np.arange(nt * nd * nd))
+    c, ab = np.divmod(src.astype(np.int64), nd * nd)
+    a, b = np.divmod(ab, nd)
+    q = np.repeat(np.arange(V.nnz), np.diff(ptr))
+    rows = np.repeat(np.arange(V.n), np.diff(V.indptr))
+    assert np.array_equal(V.cell_dofs[c, a], rows[q])
+    assert np.array_equal(V.cell_dofs[c, b], V.indices[q])
+    same = q[1:] == q[:-1]
+    assert np.all(c[1:][same] > c[:-1][same])
+
+
 def analytic_k(abd, steps):
     """test_EigenProblems.py:42-65 and the mode list of its tests (TE and TM
     modes counted twice when no index is zero)."""
