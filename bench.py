@@ -936,7 +936,7 @@ def run_high_order(args):
             e1.record(stream)
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / reps
-            alg = 3 * V.nnz * rb + V.nt * nd * nd * 4 + (V.nnz + 1) * 4 + V.nt * (16 + rb)
+            alg = 3 * V.nnz * rb + V.nt * nd * nd * 4 + (2 * V.nnz + 1) * 4 + V.nt * (16 + rb)
             gbs = alg / (ms * 1e-3) / 1e9
             out["assembly"].append({
                 "order": order, "cubes": nc, "tets": V.nt, "n_dofs": V.n, "nnz": V.nnz,

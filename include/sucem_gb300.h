@@ -91,6 +91,8 @@ int sucem_space_sizes(const sucem_space* sp, int64_t* out);
 #define SUCEM_COPY_ENTRY_SRC 16    /* int32[nt*ndof*ndof] orders 3-4: the cell entries
                                       (c*ndof + a)*ndof + b summed into each CSR entry, in
                                       ascending cell order */
+#define SUCEM_COPY_ENTRY_PERM 17   /* int32[nnz] orders 3-4: the CSR entry of each assembly
+                                      thread (each row's entries by list length) */
 int sucem_space_copy(const sucem_space* sp, int what, void* host_dst);
 
 /* Sizes of the order-1/2 assembly schedule (the kernel's work plan; no

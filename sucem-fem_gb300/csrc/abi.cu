@@ -62,7 +62,7 @@ void free_device_space(DeviceSpace* d) {
                   d->cell_dofs, d->boundary_dofs, d->kc_f, d->km_f, d->kt_f,
                   d->kc_d,    d->km_d,    d->kt_d, d->bidx, d->g_f, d->g_d, d->g2_f, d->h2_f, d->kt_lo_f, d->h_f, d->h_d,
                   d->kab_f, d->kab_d, d->ext_facets, d->ntff_pts, d->bdof_pt,
-                  d->bin_ptr, d->bin_cells, d->entry_ptr, d->entry_src, d->task_ent, d->task_meta,
+                  d->bin_ptr, d->bin_cells, d->entry_ptr, d->entry_src, d->entry_perm, d->task_ent, d->task_meta,
                   d->step_words};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -170,6 +170,7 @@ std::string upload_space(Space& s, int device) {
   UP(bidx, bidx.data(), bidx.size());
   UP(entry_ptr, s.entry_ptr.data(), s.entry_ptr.size());
   UP(entry_src, s.entry_src.data(), s.entry_src.size());
+  UP(entry_perm, s.entry_perm.data(), s.entry_perm.size());
   UP(task_ent, s.task_ent.data(), s.task_ent.size());
   UP(task_meta, reinterpret_cast<const int4*>(s.task_meta.data()), s.task_meta.size() / 4);
   UP(step_words, s.step_words.data(), s.step_words.size());
@@ -275,6 +276,7 @@ int sucem_space_copy(const sucem_space* sp, int what, void* dst) {
     case SUCEM_COPY_STEP_WORDS: return cp(s.step_words.data(), s.step_words.size() * 4);
     case SUCEM_COPY_ENTRY_PTR: return cp(s.entry_ptr.data(), s.entry_ptr.size() * 4);
     case SUCEM_COPY_ENTRY_SRC: return cp(s.entry_src.data(), s.entry_src.size() * 4);
+    case SUCEM_COPY_ENTRY_PERM: return cp(s.entry_perm.data(), s.entry_perm.size() * 4);
     case SUCEM_COPY_BOUNDARY_DUAL: {
       if (s.order > 2) return fail("boundary dual functionals: basis orders 1 and 2 only", SUCEM_ERR_ARG);
       std::vector<double> pt;

@@ -615,8 +615,10 @@ __global__ void __launch_bounds__(EntCfg<ORDER, Real, MODE>::BLOCK_WARPS * 32)
                                      nullptr, p, gcell, hcell, kt, kt_lo, S, T, B, A);
 }
 
-// Orders 3-4: a thread per CSR entry (grid-stride), gathering the cell
-// entries listed for it (ascending cell order): each is the cell's 12
+// Orders 3-4: a thread per CSR entry (grid-stride; thread t takes entry
+// perm[t], each row's entries ordered by list length so that a warp's lanes
+// walk lists of similar length), gathering the cell entries listed for it
+// (ascending cell order): each is the cell's 12
 // coefficients contracted with the reference tensors ([a][b][12], read
 // through L1/L2), plus the tangential term of the cell's exterior faces.
 // S, T and B are summed separately in that fixed order and every output
@@ -624,7 +626,8 @@ __global__ void __launch_bounds__(EntCfg<ORDER, Real, MODE>::BLOCK_WARPS * 32)
 // the same bits on every run.
 template <int ND, typename Real, bool WITH_B, int MODE>
 __global__ void __launch_bounds__(256)
-    assemble_cell_entries_kernel(int64_t nnz, const int32_t* __restrict__ ptr,
+    assemble_cell_entries_kernel(int64_t nnz, const int32_t* __restrict__ perm,
+                                 const int32_t* __restrict__ ptr,
                                  const int32_t* __restrict__ src,
                                  const int32_t* __restrict__ bidx,
                                  const uint8_t* __restrict__ ext_mask,
@@ -632,8 +635,9 @@ __global__ void __launch_bounds__(256)
                                  const Real* __restrict__ kab, const Real* __restrict__ kt,
                                  Real* S, Real* T, Real* B, typename Cplx<Real>::T* A, Real k0) {
   constexpr int NN = ND * ND;
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nnz;
-       q += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nnz;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = __ldg(&perm[t]);
     Real sv = 0, tm = 0, bv = 0;
     const int j1 = __ldg(&ptr[q + 1]);
     for (int j = __ldg(&ptr[q]); j < j1; ++j) {
@@ -840,7 +844,7 @@ cudaError_t launch_cells_t(DeviceSpace& d, const AssembleArgs& a, cudaStream_t s
   const Real* kab = sizeof(Real) == 4 ? (const Real*)d.kab_f : (const Real*)d.kab_d;
   const Real* kt = sizeof(Real) == 4 ? (const Real*)d.kt_f : (const Real*)d.kt_d;
   assemble_cell_entries_kernel<ND, Real, WITH_B, MODE><<<(unsigned)grid, 256, 0, stream>>>(
-      d.nnz, d.entry_ptr, d.entry_src, d.bidx, d.ext_mask, g, h, kab, kt, (Real*)a.S, (Real*)a.T,
+      d.nnz, d.entry_perm, d.entry_ptr, d.entry_src, d.bidx, d.ext_mask, g, h, kab, kt, (Real*)a.S, (Real*)a.T,
       (Real*)a.B, (typename Cplx<Real>::T*)a.A, (Real)a.k0);
   count_launch(2);
   return cudaGetLastError();
@@ -848,7 +852,7 @@ cudaError_t launch_cells_t(DeviceSpace& d, const AssembleArgs& a, cudaStream_t s
 
 template <int ND, typename Real>
 cudaError_t dispatch_cells(DeviceSpace& d, const AssembleArgs& a, cudaStream_t stream) {
-  if (!d.entry_ptr || !d.entry_src) return cudaErrorInvalidValue;
+  if (!d.entry_ptr || !d.entry_src || !d.entry_perm) return cudaErrorInvalidValue;
   if (a.mode == 1) return launch_cells_t<ND, Real, true, 1>(d, a, stream);
   if (a.B) return launch_cells_t<ND, Real, true, 0>(d, a, stream);
   return launch_cells_t<ND, Real, false, 0>(d, a, stream);

@@ -28,6 +28,7 @@ struct DeviceSpace {
   int32_t* cell_dofs = nullptr;   // nt*nd
   int32_t* entry_ptr = nullptr;   // orders 3-4: nnz+1, cell entries summed into each CSR entry
   int32_t* entry_src = nullptr;   // nt*nd*nd, (c * nd + a) * nd + b in ascending cell order
+  int32_t* entry_perm = nullptr;  // nnz: CSR entry of each thread of the order-3/4 kernel
   int32_t* boundary_dofs = nullptr;
   int64_t n_boundary = 0;
   int32_t* bidx = nullptr;        // nt: index among cells with exterior facets, -1 otherwise

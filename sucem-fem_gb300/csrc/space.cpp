@@ -307,6 +307,18 @@ std::string build_space(Space& s, const double* coords, int64_t nv, const int64_
         }
       }
     }
+    // thread order of the kernel: within each row, entries by list length
+    // (stable), so that a warp's lanes walk lists of similar length
+    s.entry_perm.resize(s.nnz);
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t r = 0; r < s.n; ++r) {
+      const int64_t q0 = s.indptr[r], q1 = s.indptr[r + 1];
+      for (int64_t q = q0; q < q1; ++q) s.entry_perm[q] = int32_t(q);
+      std::stable_sort(s.entry_perm.begin() + q0, s.entry_perm.begin() + q1,
+                       [&](int32_t x, int32_t y) {
+                         return s.entry_ptr[x + 1] - s.entry_ptr[x] < s.entry_ptr[y + 1] - s.entry_ptr[y];
+                       });
+    }
   }
 
   // ---- DOF locations (used by the nested-dissection ordering) ----

@@ -54,6 +54,8 @@ struct Space {
   // (c * ndof_cell + a) * ndof_cell + b, in ascending cell order
   std::vector<int32_t> entry_ptr;      // nnz+1
   std::vector<int32_t> entry_src;      // nt*ndof_cell^2
+  std::vector<int32_t> entry_perm;     // nnz: the CSR entry of each kernel thread (each row's
+                                       //   entries by list length)
 
   // Entity-per-lane assembly schedule (orders 1-2).  Entities are grouped
   // into warp tasks of 32 (one entity per lane) that share the entity kind

@@ -14,7 +14,7 @@ ERR_ARG, ERR_MEMORY, ERR_CUDA, ERR_STATE, ERR_NOCONV, ERR_BREAKDOWN = -1, -2, -3
 
 COPY = dict(indptr=0, indices=1, cell_dofs=2, boundary_dofs=3, edges=4, faces=5, cells=6, ext_mask=7,
             cell_edges=8, cell_faces=9, dof_xyz=10, boundary_dual=11, task_ent=12, task_meta=13,
-            step_words=14, entry_ptr=15, entry_src=16)
+            step_words=14, entry_ptr=15, entry_src=16, entry_perm=17)
 DEV = dict(indptr=0, indices=1, cell_dofs=2, boundary_dofs=3)
 
 _lib = None

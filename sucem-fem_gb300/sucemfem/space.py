@@ -126,12 +126,15 @@ class FunctionSpace:
     def entry_lists(self):
         """The order-3/4 assembly kernel's gather lists (host copy): CSR
         entry q sums the cell entries src[ptr[q]:ptr[q+1]], each coded
-        (c * ndof_cell + a) * ndof_cell + b, in ascending cell order."""
+        (c * ndof_cell + a) * ndof_cell + b, in ascending cell order; perm[t]
+        is the CSR entry of kernel thread t (each row's entries ordered by
+        list length)."""
         if self.order < 3:
             raise ValueError("entry lists exist for basis orders 3 and 4 only")
         ptr = self._copy("entry_ptr", self.nnz + 1, np.int32)
         src = self._copy("entry_src", self.nt * self.ndof_cell ** 2, np.int32)
-        return ptr, src
+        perm = self._copy("entry_perm", self.nnz, np.int32)
+        return ptr, src, perm
 
     def facet_closure_dofs(self, faces):
         """DOFs on the closure of the given facets (facet ids = face ids)."""

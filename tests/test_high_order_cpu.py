@@ -92,19 +92,25 @@ def test_entry_lists_cover_every_cell_entry_once_in_cell_order(order):
     """The gather lists of the order-3/4 assembly: every cell entry (c, a, b)
     appears exactly once, under the CSR entry (cell_dofs[c, a],
     cell_dofs[c, b]), and each entry's list runs in ascending cell order (the
-    fixed summation order)."""
+    fixed summation order); the thread order permutes each row's entries by
+    list length."""
     from sucemfem.mesh import Mesh
     from sucemfem.space import FunctionSpace
     coords, cells = fem.box_mesh(1.0, 0.5, 0.75, 3, 2, 2)
     V = FunctionSpace(Mesh(coords, cells), order=order)
     nd, nt = V.ndof_cell, V.nt
-    ptr, src = V.entry_lists()
+    ptr, src, perm = V.entry_lists()
+    rows = np.repeat(np.arange(V.n), np.diff(V.indptr))
+    assert np.array_equal(np.sort(perm), np.arange(V.nnz))
+    assert np.array_equal(rows[perm], rows)        # threads stay within their row
+    n_list = np.diff(ptr)[perm]
+    same_row = rows[1:] == rows[:-1]
+    assert np.all(n_list[1:][same_row] >= n_list[:-1][same_row])
     assert ptr[0] == 0 and ptr[-1] == nt * nd * nd and np.all(np.diff(ptr) >= 1)
     assert np.array_equal(np.sort(src), np.arange(nt * nd * nd))
     c, ab = np.divmod(src.astype(np.int64), nd * nd)
     a, b = np.divmod(ab, nd)
     q = np.repeat(np.arange(V.nnz), np.diff(ptr))
-    rows = np.repeat(np.arange(V.n), np.diff(V.indptr))
     assert np.array_equal(V.cell_dofs[c, a], rows[q])
     assert np.array_equal(V.cell_dofs[c, b], V.indices[q])
     same = q[1:] == q[:-1]
