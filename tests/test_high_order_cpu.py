@@ -190,3 +190,13 @@ def test_high_order_space_rejects_order_1_2_only_host_queries():
     out = np.zeros(V2.n_boundary * 6)
     call("sucem_space_copy", V2._h, COPY["boundary_dual"], ptr(out))
     assert np.isfinite(out).all() and np.abs(out).max() > 0
+
+
+def test_entry_lists_exist_for_orders_3_4_only():
+    """Orders 1-2 assemble through the entity schedule: an order-2 space has
+    no gather lists and says so."""
+    from sucemfem.mesh import Mesh
+    from sucemfem.space import FunctionSpace
+    c, t = fem.unit_cube(1, 1, 1)
+    with pytest.raises(ValueError, match="orders 3 and 4"):
+        FunctionSpace(Mesh(c, t), order=2).entry_lists()
